@@ -1,0 +1,157 @@
+"""
+Seeded synthetic GWAS inputs with the shapes of the scan workloads.
+
+No public dataset is used: genotypes, covariates and phenotypes are drawn here from a fixed seed, following the
+recipe of the reference's toy simulator (fasterlmm/sim.py:21-28) widened to per-variant allele frequencies, per
+phenotype causal counts and heritabilities, and the Blom rank-inverse-normal transform the CLI applies to
+phenotypes (fasterlmm/normalize.py:21-52).
+
+Genotypes are returned as int8 dosages 0/1/2 with -1 marking a missing call, sample-major (N, M), the layout of
+the reference's ``AlignedDataset.Z`` (fasterlmm/io.py:123-140) before it is cast to float with NaN for missing.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+MISSING = -1
+
+# human autosome lengths in Mb (GRCh38, rounded); variant counts of the uneven-chromosome workload are made
+# proportional to these
+HUMAN_CHROM_MB = [248, 242, 198, 190, 181, 171, 159, 145, 138, 134, 135, 133, 114, 107, 102, 90, 83, 80, 59, 64,
+                  47, 51]
+
+
+@dataclass
+class SynthData:
+    G: np.ndarray          # (N, M) int8 dosages, -1 = missing
+    X: np.ndarray          # (N, D) float64, [intercept | N(0,1) covariates]
+    Y: np.ndarray          # (N, B) float64 phenotypes after RINT (NaN where missing)
+    chrom: np.ndarray      # (M,) int chromosome label per variant, contiguous blocks 1..n_chrom
+    h2: np.ndarray         # (B,) simulated heritability per phenotype
+    n_causal: np.ndarray   # (B,) causal variant count per phenotype
+
+    def Z_float(self) -> np.ndarray:
+        """(N, M) float64 dosages with NaN for missing calls, the reference's input convention."""
+        Z = self.G.astype(np.float64)
+        Z[self.G == MISSING] = np.nan
+        return Z
+
+
+def rint_columns(Y: np.ndarray, c: float = 3.0 / 8.0) -> np.ndarray:
+    """Blom RINT per column, average ties, NaN kept (fasterlmm/normalize.py:21-52)."""
+    from scipy.stats import norm, rankdata
+    Y = np.asarray(Y, dtype=np.float64)
+    out = np.full_like(Y, np.nan)
+    for j in range(Y.shape[1]):
+        y = Y[:, j]
+        mask = ~np.isnan(y)
+        n = int(mask.sum())
+        if n == 0:
+            continue
+        ranks = rankdata(y[mask], method="average")
+        out[mask, j] = norm.ppf((ranks - c) / (n - 2 * c + 1))
+    return out
+
+
+def chrom_sizes_even(M: int, n_chrom: int) -> list[int]:
+    base, extra = divmod(M, n_chrom)
+    return [base + (1 if i < extra else 0) for i in range(n_chrom)]
+
+
+def chrom_sizes_human(M: int, n_chrom: int = 22) -> list[int]:
+    w = np.asarray(HUMAN_CHROM_MB[:n_chrom], dtype=np.float64)
+    sizes = np.floor(M * w / w.sum()).astype(int)
+    sizes[: M - sizes.sum()] += 1
+    return sizes.tolist()
+
+
+def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19930909, config_id: int = 0,
+                 maf_lo: float = 0.05, h2_lo: float = 0.1, h2_hi: float = 0.8, k_lo: int = 5, k_hi: int = 5,
+                 chrom_sizes: list[int] | None = None, geno_missing_rate: float = 0.0,
+                 pheno_na_patterns: int = 0, na_frac_hi: float = 0.4, rint: bool = True) -> SynthData:
+    """
+    Draw one synthetic dataset.
+
+    Genotypes: Binomial(2, p_j) with p_j ~ U[maf_lo, 0.5]; optional missing calls at ``geno_missing_rate``.
+    Covariates: intercept plus D - 1 standard normals.  Phenotypes: k ~ U{k_lo..k_hi} causal variants, effects
+    N(0, 1), genetic value rescaled to variance h2 (h2 ~ U[h2_lo, h2_hi]; k = 0 or h2 = 0 gives no genetic part),
+    noise N(0, 1 - h2), then RINT.  ``pheno_na_patterns`` > 0 assigns each phenotype one of that many missingness
+    patterns (pattern 0 has none, the others drop up to ``na_frac_hi`` of the samples).
+    """
+    rng = np.random.default_rng([seed, config_id])
+    sizes = chrom_sizes if chrom_sizes is not None else chrom_sizes_even(M, n_chrom)
+    assert sum(sizes) == M
+    chrom = np.repeat(np.arange(1, len(sizes) + 1), sizes)
+    maf = rng.uniform(maf_lo, 0.5, size=M)
+    G = np.empty((N, M), dtype=np.int8)
+    step = 8192
+    for j0 in range(0, M, step):
+        j1 = min(M, j0 + step)
+        G[:, j0:j1] = rng.binomial(2, maf[j0:j1], size=(N, j1 - j0)).astype(np.int8)
+    if geno_missing_rate > 0:
+        miss = rng.random((N, M)) < geno_missing_rate
+        G[miss] = MISSING
+    X = np.concatenate([np.ones((N, 1)), rng.standard_normal((N, D - 1))], axis=1)
+
+    # per-variant stats over observed calls, used only to standardise the causal columns
+    Gf = G.astype(np.float64)
+    obs = G != MISSING
+    n_obs = np.maximum(obs.sum(axis=0), 1)
+    mu = np.where(obs, Gf, 0.0).sum(axis=0) / n_obs
+    sd = np.sqrt(np.where(obs, (Gf - mu) ** 2, 0.0).sum(axis=0) / n_obs)
+    sd = np.clip(sd, 1e-12, None)
+    del Gf
+
+    h2 = rng.uniform(h2_lo, h2_hi, size=B)
+    n_causal = rng.integers(k_lo, k_hi + 1, size=B)
+    Y = np.empty((N, B))
+    for b in range(B):
+        k = int(n_causal[b])
+        e = rng.standard_normal(N) * np.sqrt(1.0 - h2[b])
+        if k == 0 or h2[b] == 0.0:
+            Y[:, b] = e
+            continue
+        idx = rng.choice(M, size=k, replace=False)
+        Zc = np.where(obs[:, idx], (G[:, idx] - mu[idx]) / sd[idx], 0.0)
+        g = Zc @ rng.standard_normal(k)
+        gs = g.std()
+        Y[:, b] = (g / gs * np.sqrt(h2[b]) if gs > 0 else 0.0) + e
+    if pheno_na_patterns > 0:
+        masks = [np.zeros(N, dtype=bool)]
+        for _ in range(pheno_na_patterns - 1):
+            frac = rng.uniform(0.0, na_frac_hi)
+            masks.append(rng.random(N) < frac)
+        pat = rng.integers(0, pheno_na_patterns, size=B)
+        for b in range(B):
+            Y[masks[pat[b]], b] = np.nan
+    if rint:
+        Y = rint_columns(Y)
+    return SynthData(G=G, X=X, Y=Y, chrom=chrom, h2=h2, n_causal=n_causal)
+
+
+# the scan workloads, by name: (N, M, n_chrom, D, B, n_perm, grid) and the generator keywords
+WORKLOADS = {
+    # 150 samples x 1,500 variants over 16 chromosomes, 20 phenotypes x 100 permutations, 100-point grid on [-5, 5]
+    "n150_m1500_b20_perm100": dict(N=150, M=1500, n_chrom=16, D=3, B=20, n_perm=100, n_grid=100,
+                                   log_delta_min=-5.0, log_delta_max=5.0,
+                                   gen=dict(maf_lo=0.05, h2_lo=0.1, h2_hi=0.8, k_lo=5, k_hi=5, config_id=1)),
+    # 1,000 samples x 100,000 variants over 20 chromosomes, 6,484 phenotypes x 10 permutations, default grid
+    "n1000_m100k_b6484_perm10": dict(N=1000, M=100_000, n_chrom=20, D=5, B=6484, n_perm=10, n_grid=64,
+                                     log_delta_min=-10.0, log_delta_max=10.0,
+                                     gen=dict(maf_lo=0.01, h2_lo=0.0, h2_hi=0.9, k_lo=0, k_hi=50, config_id=2)),
+}
+
+
+def make_workload(name: str, *, seed: int = 19930909, B: int | None = None, M: int | None = None) -> tuple[SynthData, dict]:
+    """Generate a named workload; ``B`` / ``M`` shrink it for bounded samples (same generator, same seed)."""
+    w = dict(WORKLOADS[name])
+    gen = dict(w.pop("gen"))
+    if B is not None:
+        w["B"] = B
+    if M is not None:
+        w["M"] = M
+    data = make_dataset(w["N"], w["M"], w["n_chrom"], w["D"], w["B"], seed=seed, **gen)
+    return data, w

@@ -1,0 +1,327 @@
+"""
+CPU oracle for the FaST-ER-LMM fastlmm-compat LOCO association scan.
+
+TEST INFRASTRUCTURE ONLY.  This module is a plain numpy FP64 restatement of the reference's scan path, used as
+the checker for the GPU implementation.  Only the test suite (tests/), ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import or run it, and only as the checker or the
+timed CPU baseline -- never as the thing measured or shipped.  The product path (``fasterlmm_gb300``) never
+imports it and fails loudly when its CUDA library is missing.
+
+Pinning: tests/golden/*.npz hold outputs of the reference itself (the ``fasterlmm`` package, v1.6.2), run on
+seeded synthetic inputs by tests/golden/make_golden.py.  tests/test_oracle_golden.py checks every function here
+against those fixtures, so this restatement is pinned to the reference's own numbers.
+
+Every function cites the reference file:line it restates (paths inside the reference project).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+LOG2PI = float(np.log(2.0 * np.pi))
+
+
+# --------------------------------------------------------------------------------------------------------------
+# standardisation and kinship
+# --------------------------------------------------------------------------------------------------------------
+
+def pos_floor(dtype=np.float64) -> float:
+    """Positive clamp floor: 1e-300 in FP64, 1e-30 otherwise (fasterlmm/core.py:80-86)."""
+    return 1e-300 if np.dtype(dtype) == np.float64 else 1e-30
+
+
+def standardise_columns(Z: np.ndarray) -> np.ndarray:
+    """
+    Unit standardiser, torch branch order (fasterlmm/io.py:235-246): NaN-aware column mean and population std
+    (ddof=0, counts clamped at 1), std == 0 -> inf, subtract / divide, NaN -> 0 after scaling.
+    """
+    a = np.array(Z, dtype=np.float64, copy=True)
+    nan_mask = np.isnan(a)
+    a_stats = np.where(nan_mask, 0.0, a)
+    n_nonnan = np.maximum((~nan_mask).sum(axis=0), 1).astype(np.float64)
+    col_mean = a_stats.sum(axis=0) / n_nonnan
+    diff = np.where(nan_mask, 0.0, a_stats - col_mean[None, :])
+    col_std = np.sqrt((diff * diff).sum(axis=0) / n_nonnan)
+    col_std = np.where(col_std == 0, np.inf, col_std)
+    with np.errstate(invalid="ignore"):
+        out = (a - col_mean[None, :]) / col_std[None, :]
+    return np.where(nan_mask, 0.0, out)
+
+
+def grm(Z: np.ndarray) -> np.ndarray:
+    """K = Z Z^T / M for a pre-standardised Z (fasterlmm/io.py:257-265)."""
+    return (Z @ Z.T) / Z.shape[1]
+
+
+# --------------------------------------------------------------------------------------------------------------
+# compat rotation, delta fit, Wald scan
+# --------------------------------------------------------------------------------------------------------------
+
+def compat_rotate(K: np.ndarray, X: np.ndarray, Y: np.ndarray) -> dict:
+    """
+    fastlmm projection rotation (fasterlmm/core.py:487-519): Xpinv = pinv(X); Kp = (I - PX)(K + I)(I - PX);
+    eigh; keep eigenpairs D..N-1 with s = max(s - 1, 0); UY = U_eff^T (Y - X Xpinv Y).
+    """
+    N = K.shape[0]
+    D = X.shape[1]
+    Xpinv = np.linalg.pinv(X)
+    Iperp = np.eye(N) - X @ Xpinv
+    Kp = (Iperp @ (K + np.eye(N))) @ Iperp
+    s_full, U_full = np.linalg.eigh(Kp)
+    s = np.maximum(s_full[D:N] - 1.0, 0.0)
+    U_eff = np.ascontiguousarray(U_full[:, D:N])
+    Y_r = Y - X @ (Xpinv @ Y)
+    UY = U_eff.T @ Y_r
+    return {"s": s, "U_eff": U_eff, "X": X, "Xpinv": Xpinv, "UY": UY}
+
+
+def profile_loss_compat(log_delta: np.ndarray, s: np.ndarray, UY: np.ndarray) -> np.ndarray:
+    """(G, P) ML -2 log-likelihood on a grid (fasterlmm/core.py:525-542)."""
+    Neff = s.shape[0]
+    delta = np.exp(log_delta)
+    Sd = s[None, :] + delta[:, None]
+    w = 1.0 / Sd
+    yWy = w @ (UY * UY)
+    rWr = np.maximum(yWy, pos_floor())
+    sum_log_Sd = np.log(Sd).sum(axis=1)
+    sigma2 = rWr / Neff
+    return Neff * (LOG2PI + np.log(sigma2) + 1.0) + sum_log_Sd[:, None]
+
+
+def profile_loss_compat_per_pheno(log_delta: np.ndarray, s: np.ndarray, UY: np.ndarray) -> np.ndarray:
+    """(P,) loss, one log delta per phenotype column (fasterlmm/core.py:545-558)."""
+    Neff = s.shape[0]
+    delta = np.exp(log_delta)
+    Sd = s[None, :] + delta[:, None]
+    w = 1.0 / Sd
+    yWy = (w * UY.T * UY.T).sum(axis=1)
+    rWr = np.maximum(yWy, pos_floor())
+    sum_log_Sd = np.log(Sd).sum(axis=1)
+    sigma2 = rWr / Neff
+    return Neff * (LOG2PI + np.log(sigma2) + 1.0) + sum_log_Sd
+
+
+def delta_grid(n_grid: int, log_delta_min: float, log_delta_max: float) -> np.ndarray:
+    """The grid the reference builds with torch.linspace (fasterlmm/core.py:569)."""
+    import torch  # torch.linspace's node values are the ones the reference compares against
+    return torch.linspace(log_delta_min, log_delta_max, n_grid, dtype=torch.float64).numpy()
+
+
+def fit_delta_grid_compat(s: np.ndarray, UY: np.ndarray, *, n_grid: int = 64, log_delta_min: float = -10.0,
+                          log_delta_max: float = 10.0, refine: bool = True, return_idx: bool = False):
+    """
+    Grid argmin then 50 golden-section steps on [grid[i-1], grid[i+1]] (fasterlmm/core.py:561-595).
+    The bracket update order, inv_phi constants and final 0.5 (a + b) clamp follow the reference exactly.
+    """
+    grid = delta_grid(n_grid, log_delta_min, log_delta_max)
+    loss = profile_loss_compat(grid, s, UY)
+    idx = loss.argmin(axis=0)
+    if not refine:
+        out = grid[idx]
+        return (out, idx) if return_idx else out
+    lo_idx = np.clip(idx - 1, 0, n_grid - 1)
+    hi_idx = np.clip(idx + 1, 0, n_grid - 1)
+    a = grid[lo_idx].copy()
+    b = grid[hi_idx].copy()
+    inv_phi = 2.0 / (1.0 + 5.0 ** 0.5)
+    inv_phi2 = inv_phi * inv_phi
+    c = a + inv_phi2 * (b - a)
+    d = a + inv_phi * (b - a)
+    fc = profile_loss_compat_per_pheno(c, s, UY)
+    fd = profile_loss_compat_per_pheno(d, s, UY)
+    for _ in range(50):
+        cond = fc < fd
+        b = np.where(cond, d, b)
+        a = np.where(cond, a, c)
+        c = a + inv_phi2 * (b - a)
+        d = a + inv_phi * (b - a)
+        fc = profile_loss_compat_per_pheno(c, s, UY)
+        fd = profile_loss_compat_per_pheno(d, s, UY)
+    out = np.clip(0.5 * (a + b), log_delta_min, log_delta_max)
+    return (out, idx) if return_idx else out
+
+
+def snp_wald_scan_compat(spec: dict, log_delta: np.ndarray, S: np.ndarray, *, n_real: int | None = None) -> dict:
+    """
+    Per-(variant, column) Wald test in the projected basis (fasterlmm/core.py:601-671).  The reference tiles the
+    pheno / variant axes; tiling does not change the maths (its own chunking-invariance test, tests/
+    test_core_compat.py:244-258), so the oracle evaluates one tile.
+    """
+    s, UY, X, Xpinv, U_eff = spec["s"], spec["UY"], spec["X"], spec["Xpinv"], spec["U_eff"]
+    Neff = s.shape[0]
+    P = UY.shape[1]
+    M = S.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    floor = pos_floor()
+    S_r = S - X @ (Xpinv @ S)
+    US = U_eff.T @ S_r
+    delta = np.exp(log_delta)
+    w = 1.0 / (s[None, :] + delta[:, None])
+    rWr = np.maximum((w * UY.T * UY.T).sum(axis=1), floor)
+    sWy = (w * UY.T) @ US
+    sWs = w @ (US * US)
+    denom = np.maximum(sWs, floor)
+    beta = sWy / denom
+    rss = np.maximum(rWr[:, None] - sWy * sWy / denom, floor)
+    var_beta = rss / (Neff - 1) / denom
+    F = beta * beta / var_beta
+    max_F = F.max(axis=1) if M > 0 else np.full(P, -np.inf)
+    r = slice(0, n_real)
+    sfve = np.sqrt(np.maximum((sWy[r] * sWy[r]) / (denom[r] * rWr[r, None]), 0.0))
+    h2 = 1.0 / (1.0 + np.exp(log_delta[:n_real]))
+    return {"f": F[r].T.copy(), "beta": beta[r].T.copy(), "se": np.sqrt(var_beta[r]).T.copy(), "sfve": sfve.T.copy(),
+            "nullh2": np.broadcast_to(h2[None, :], (M, n_real)).copy(), "max_F": max_F}
+
+
+def loco_scan_compat(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, chrom: np.ndarray, *, n_real: int | None = None,
+                     Z_kin: np.ndarray | None = None, chrom_kin: np.ndarray | None = None, n_grid: int = 64,
+                     log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
+                     on_chrom=None, keep_spectra: bool = False) -> dict:
+    """
+    LOCO driver (fasterlmm/core.py:677-726): per chromosome c, K from the variants not on c (or from the kinship
+    panel without c), compat rotation, delta fit, Wald scan of the variants on c, scatter, running genome max.
+    The grid options are the reference's fit_delta_grid_compat keywords (fasterlmm/core.py:561-562), which its
+    LOCO loop leaves at their defaults (fasterlmm/core.py:715).
+    Also returns the per-chromosome log delta, which the reference computes but does not return, and with
+    ``keep_spectra`` the per-chromosome (s, UY) used to judge log delta by its loss.
+    """
+    if (Z_kin is None) != (chrom_kin is None):
+        raise ValueError("Z_kin and chrom_kin go together")
+    chrom = np.asarray(chrom)
+    M = Z.shape[1]
+    P = Y.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    out = {k: np.zeros((M, n_real)) for k in ("f", "beta", "se", "sfve", "nullh2")}
+    max_F = np.full(P, -np.inf)
+    chroms = sorted(np.unique(chrom).tolist())
+    log_deltas = {}
+    spectra = {}
+    for k_idx, c in enumerate(chroms):
+        test_mask = chrom == c
+        K = grm(Z[:, chrom != c]) if Z_kin is None else grm(Z_kin[:, np.asarray(chrom_kin) != c])
+        spec = compat_rotate(K, X, Y)
+        ld = fit_delta_grid_compat(spec["s"], spec["UY"], n_grid=n_grid, log_delta_min=log_delta_min,
+                                   log_delta_max=log_delta_max, refine=refine)
+        log_deltas[c] = ld
+        if keep_spectra:
+            spectra[c] = (spec["s"], spec["UY"])
+        res = snp_wald_scan_compat(spec, ld, Z[:, test_mask], n_real=n_real)
+        if n_real > 0:
+            for key in out:
+                out[key][test_mask, :] = res[key]
+        max_F = np.maximum(max_F, res["max_F"])
+        if on_chrom is not None:
+            on_chrom(k_idx + 1, len(chroms))
+    out["max_F"] = max_F
+    out["log_delta"] = log_deltas
+    if keep_spectra:
+        out["spectra"] = spectra
+    return out
+
+
+def single_k_scan_compat(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, *, n_real: int | None = None,
+                         Z_kin: np.ndarray | None = None, n_grid: int = 64, log_delta_min: float = -10.0,
+                         log_delta_max: float = 10.0, refine: bool = True) -> dict:
+    """One K over every kinship variant, one rotation / fit / scan (fasterlmm/core.py:729-740)."""
+    K = grm(Z if Z_kin is None else Z_kin)
+    spec = compat_rotate(K, X, Y)
+    ld = fit_delta_grid_compat(spec["s"], spec["UY"], n_grid=n_grid, log_delta_min=log_delta_min,
+                               log_delta_max=log_delta_max, refine=refine)
+    res = snp_wald_scan_compat(spec, ld, Z, n_real=n_real)
+    res["log_delta"] = ld
+    res["spectra"] = {0: (spec["s"], spec["UY"])}
+    return res
+
+
+# --------------------------------------------------------------------------------------------------------------
+# permutations and the batch driver
+# --------------------------------------------------------------------------------------------------------------
+
+def perm_orders(N: int, seed_cols, n_perm: int, seed: int = 19930909) -> np.ndarray:
+    """
+    (N, B, n_perm) int64 row orders: per phenotype a PCG64 stream seeded on [seed, column], n_perm rows of N
+    uniforms, argsort along the row (fasterlmm/perms.py:51-55).
+    """
+    seed_cols = list(seed_cols)
+    orders = np.empty((N, len(seed_cols), n_perm), dtype=np.int64)
+    for b_pos, p in enumerate(seed_cols):
+        rng = np.random.default_rng([seed, int(p)])
+        orders[:, b_pos, :] = rng.random((n_perm, N)).argsort(axis=1).T
+    return orders
+
+
+def pack_perms(y_real: np.ndarray, orders: np.ndarray) -> np.ndarray:
+    """
+    Y_all = [y_real | b0 perms | b1 perms | ...], pheno-major perm columns (fasterlmm/perms.py:56-59).
+    """
+    N, B = y_real.shape
+    n_perm = orders.shape[2]
+    y_perms = np.take_along_axis(np.broadcast_to(y_real[:, :, None], (N, B, n_perm)), orders, axis=0)
+    return np.concatenate([y_real, y_perms.reshape(N, B * n_perm)], axis=1)
+
+
+def perm_threshold(Z_raw: np.ndarray, X: np.ndarray, Y: np.ndarray, chrom: np.ndarray, pheno_idx, *,
+                   n_perm: int = 100, seed: int = 19930909, loco: bool = True, seed_idx=None,
+                   Z_kin_raw: np.ndarray | None = None, chrom_kin: np.ndarray | None = None,
+                   n_grid: int = 64, log_delta_min: float = -10.0, log_delta_max: float = 10.0,
+                   on_chrom=None, keep_spectra: bool = False) -> tuple[dict, np.ndarray]:
+    """
+    Batch driver (fasterlmm/perms.py:21-68): standardise Z (and the kinship panel), pack the B real columns with
+    their B * n_perm permutation columns, run the LOCO (or single-K) scan with n_real = B, slice perm_max_F.
+    """
+    Z_std = standardise_columns(Z_raw)
+    Z_kin_std = standardise_columns(Z_kin_raw) if Z_kin_raw is not None else None
+    pheno_idx = list(pheno_idx)
+    B = len(pheno_idx)
+    y_real = Y[:, pheno_idx]
+    N = y_real.shape[0]
+    seed_cols = pheno_idx if seed_idx is None else list(seed_idx)
+    orders = perm_orders(N, seed_cols, n_perm, seed)
+    Y_all = pack_perms(y_real, orders)
+    kw = dict(n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max)
+    if loco:
+        res = loco_scan_compat(Z_std, X, Y_all, chrom, n_real=B, Z_kin=Z_kin_std, chrom_kin=chrom_kin,
+                               on_chrom=on_chrom, keep_spectra=keep_spectra, **kw)
+    else:
+        res = single_k_scan_compat(Z_std, X, Y_all, n_real=B, Z_kin=Z_kin_std, **kw)
+    perm_max_F = res["max_F"][B:].reshape(B, n_perm)
+    return res, perm_max_F
+
+
+# --------------------------------------------------------------------------------------------------------------
+# post-scan statistics and NA grouping
+# --------------------------------------------------------------------------------------------------------------
+
+def f_sf(F: np.ndarray, df2: int) -> np.ndarray:
+    """p = F(1, df2) survival function, as the CLI computes it (fasterlmm/cli.py:405-406)."""
+    import scipy.stats as ss
+    return ss.f.sf(F, 1, df2)
+
+
+def neg_log10_p(F: np.ndarray, df2: int) -> np.ndarray:
+    """-log10 of the F(1, df2) tail, through scipy's log survival function so huge F does not underflow."""
+    import scipy.stats as ss
+    return -ss.f.logsf(F, 1, df2) / np.log(10.0)
+
+
+def perm_quantile_threshold(perm_min_p: np.ndarray, q: float = 0.05) -> float:
+    """Genome-wide threshold = linear-interpolated q quantile of the per-perm min p (fasterlmm/cli.py:128)."""
+    return float(np.quantile(perm_min_p, q))
+
+
+def effect_size(beta: np.ndarray, g_var: np.ndarray, p_var: float) -> np.ndarray:
+    """EffectSize = beta^2 var(g) / var(y) (fasterlmm/cli.py:131-132)."""
+    return beta * beta * g_var / p_var
+
+
+def group_by_na(Y: np.ndarray, cols) -> list:
+    """Group columns by NaN pattern (packbits key), keep rows observed in the group (fasterlmm/io.py:187-203)."""
+    mask = np.isnan(Y[:, list(cols)])
+    groups: dict = {}
+    for j, c in enumerate(cols):
+        groups.setdefault(np.packbits(mask[:, j]).tobytes(), []).append(j)
+    out = []
+    for js in groups.values():
+        keep = np.flatnonzero(~mask[:, js[0]]).tolist()
+        out.append((keep, [list(cols)[j] for j in js]))
+    return out

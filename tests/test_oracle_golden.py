@@ -1,0 +1,114 @@
+"""
+Pin the CPU oracle (oracle/flmm_oracle.py) to the reference's own outputs in tests/golden/*.npz.
+
+The fixtures were produced by the reference implementation (tests/golden/make_golden.py); the oracle is a numpy
+restatement with its own summation order and LAPACK call.  Everything that does not go through the golden-section
+search agrees to FP64 rounding; log delta is judged by loss equivalence (tests/parity.py) and the scan outputs by
+the reference's parity tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import flmm_oracle as orc
+from conftest import z_float
+from parity import DETAIL, assert_log_delta_equivalent, assert_scan_close
+
+
+def _close(a, b, rtol=1e-7, atol=1e-9):
+    np.testing.assert_allclose(a, b, rtol=rtol, atol=atol)
+
+
+def _check_log_delta(res, ref_ld):
+    for i, c in enumerate(sorted(res["log_delta"])):
+        s, UY = res["spectra"][c]
+        assert_log_delta_equivalent(res["log_delta"][c], ref_ld[i], s, UY)
+
+
+def test_oracle_components(golden):
+    g = golden("components")
+    spec = orc.compat_rotate(g["K"], g["X"], g["Y"])
+    _close(spec["s"], g["s"], atol=1e-10)
+    _close(spec["Xpinv"], g["Xpinv"], atol=1e-12)
+    # UY depends on the basis only through eigenvector signs: compare the sign-invariant squares and the loss
+    _close(spec["UY"] ** 2, g["UY"] ** 2, atol=1e-10)
+    grid = orc.delta_grid(64, -10.0, 10.0)
+    _close(orc.profile_loss_compat(grid, spec["s"], spec["UY"]), g["grid_loss"], rtol=1e-12, atol=1e-9)
+    ld_grid = orc.fit_delta_grid_compat(spec["s"], spec["UY"], refine=False)
+    assert np.array_equal(ld_grid, g["log_delta_grid"])  # the grid argmin is exact
+    ld = orc.fit_delta_grid_compat(spec["s"], spec["UY"])
+    assert_log_delta_equivalent(ld, g["log_delta"], spec["s"], spec["UY"])
+    res = orc.snp_wald_scan_compat(spec, g["log_delta"], g["Z_std"], n_real=4)
+    for k in DETAIL + ("max_F",):
+        _close(res[k], g[k])
+        _close(res[k], g["tiled_" + k])  # the reference's tiled run (17-variant x 2-column chunks)
+
+
+@pytest.mark.parametrize("name", ["loco_n150_m1500", "edge_intercept_only", "edge_rank_deficient"])
+def test_oracle_perm_threshold(golden, name):
+    g = golden(name)
+    B = g["f"].shape[1]
+    n_perm = int(g["n_perm"])
+    seen = []
+    res, pmf = orc.perm_threshold(z_float(g["G"]), g["X"], g["Y"], g["chrom"], range(B), n_perm=n_perm,
+                                  on_chrom=lambda k, n: seen.append((k, n)), keep_spectra=True)
+    n_chr = len(np.unique(g["chrom"]))
+    assert seen == [(k + 1, n_chr) for k in range(n_chr)]
+    _check_log_delta(res, g["log_delta"])
+    assert_scan_close(res, g)
+    assert_scan_close({"perm_max_F": pmf}, g, keys=("perm_max_F",))
+
+
+def test_oracle_grid100(golden):
+    g = golden("loco_n150_m1500_grid100")
+    B = g["f"].shape[1]
+    n_perm = int(g["n_perm"])
+    N = g["G"].shape[0]
+    orders = orc.perm_orders(N, range(B), n_perm)
+    assert np.array_equal(orders, g["orders"].astype(np.int64))  # permutation index sets are bit-exact
+    Y_all = orc.pack_perms(g["Y"][:, :B], orders)
+    res = orc.loco_scan_compat(orc.standardise_columns(z_float(g["G"])), g["X"], Y_all, g["chrom"], n_real=B,
+                               n_grid=100, log_delta_min=-5.0, log_delta_max=5.0, keep_spectra=True)
+    _check_log_delta(res, g["log_delta"])
+    assert_scan_close(res, g)
+
+
+def test_oracle_post_scan(golden):
+    g = golden("loco_n150_m1500")
+    N, D = g["X"].shape
+    df2 = N - D - 1
+    _close(orc.f_sf(g["f"], df2), g["p"], rtol=1e-12, atol=0)
+    _close(orc.neg_log10_p(g["f"], df2), g["neglog10p"], rtol=1e-12, atol=1e-12)
+    thr = [orc.perm_quantile_threshold(g["perm_min_p"][b]) for b in range(g["f"].shape[1])]
+    _close(np.asarray(thr), g["threshold"], rtol=1e-12, atol=0)
+
+
+def test_oracle_kin_panel_and_single_k(golden):
+    g = golden("kin_panel_single_k")
+    B = g["f"].shape[1]
+    n_perm = int(g["n_perm"])
+    res, pmf = orc.perm_threshold(z_float(g["G"]), g["X"], g["Y"], g["chrom"], range(B), n_perm=n_perm,
+                                  Z_kin_raw=z_float(g["G_kin"]), chrom_kin=g["chrom_kin"], keep_spectra=True)
+    _check_log_delta(res, g["log_delta"])
+    assert_scan_close(res, g)
+    assert_scan_close({"perm_max_F": pmf}, g, keys=("perm_max_F",))
+    res, pmf = orc.perm_threshold(z_float(g["G"]), g["X"], g["Y"], g["chrom"], range(B), n_perm=n_perm, loco=False)
+    _check_log_delta({"log_delta": {0: res["log_delta"]}, "spectra": res["spectra"]}, g["sk_log_delta"])
+    assert_scan_close(res, g, prefix="sk_")
+    assert_scan_close({"perm_max_F": pmf}, g, keys=("perm_max_F",), prefix="sk_")
+    with pytest.raises(ValueError):
+        orc.loco_scan_compat(np.zeros((4, 4)), np.ones((4, 1)), np.zeros((4, 1)), np.arange(4), Z_kin=np.zeros((4, 4)))
+
+
+def test_oracle_na_groups(golden):
+    g = golden("na_groups")
+    Z = z_float(g["G"])
+    groups = orc.group_by_na(g["Y"], list(range(g["Y"].shape[1])))
+    assert len(groups) == int(g["n_groups"])
+    for gi, (keep, cols) in enumerate(groups):
+        assert np.array_equal(keep, g[f"g{gi}_keep"]) and np.array_equal(cols, g[f"g{gi}_cols"])
+        res, pmf = orc.perm_threshold(Z[keep], g["X"][keep], g["Y"][keep][:, cols], g["chrom"], range(len(cols)),
+                                      n_perm=int(g["n_perm"]), seed_idx=cols)
+        assert_scan_close(res, g, prefix=f"g{gi}_")
+        assert_scan_close({"perm_max_F": pmf}, g, keys=("perm_max_F",), prefix=f"g{gi}_")
