@@ -1,0 +1,225 @@
+// Library-level entry points: status strings, per-thread last error, the per-device context (cuSOLVER handle),
+// and the two FP64 factorisations that go through cuSOLVER: the covariate SVD (the pseudo-inverse of
+// fasterlmm/core.py:498) and the kinship eigendecomposition (fasterlmm/core.py:54-77, :510).
+#include <cusolverDn.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "flmm_common.cuh"
+
+struct flmm_context {
+    int device = 0;
+    int sm_count = 0;
+    cusolverDnHandle_t solver = nullptr;
+};
+
+namespace flmm {
+
+static thread_local char g_last_error[512] = {0};
+
+int fail(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+
+int check_cuda(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(FLMM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return FLMM_OK;
+}
+
+int check_launch(const char* what) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return check_cuda(what);
+}
+
+static int solver_fail(cusolverStatus_t st, const char* what) {
+    return fail(FLMM_ERR_SOLVER, "%s: cusolver status %d", what, static_cast<int>(st));
+}
+
+}  // namespace flmm
+
+using namespace flmm;
+
+extern "C" int flmm_version(void) { return 100; }
+
+extern "C" const char* flmm_status_string(int status) {
+    switch (status) {
+        case FLMM_OK: return "ok";
+        case FLMM_ERR_ARG: return "invalid argument";
+        case FLMM_ERR_CUDA: return "CUDA error";
+        case FLMM_ERR_SOLVER: return "cuSOLVER error";
+        case FLMM_ERR_WORKSPACE: return "workspace too small";
+        case FLMM_ERR_DEVICE: return "unsupported device (needs sm_103, GB300)";
+        case FLMM_ERR_TIMEOUT: return "bounded device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+extern "C" const char* flmm_last_error(void) { return g_last_error; }
+
+extern "C" uint64_t flmm_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+extern "C" int flmm_context_create(int device, flmm_context** out) {
+    FLMM_REQUIRE(out != nullptr, "flmm_context_create: out is NULL");
+    *out = nullptr;
+    cudaDeviceProp prop;
+    FLMM_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(FLMM_ERR_DEVICE, "device %d is sm_%d%d (%s); this build targets sm_103a", device, prop.major,
+                    prop.minor, prop.name);
+    FLMM_CUDA(cudaSetDevice(device));
+    flmm_context* ctx = new (std::nothrow) flmm_context();
+    if (!ctx) return fail(FLMM_ERR_ARG, "flmm_context_create: out of host memory");
+    ctx->device = device;
+    ctx->sm_count = prop.multiProcessorCount;
+    cusolverStatus_t st = cusolverDnCreate(&ctx->solver);
+    if (st != CUSOLVER_STATUS_SUCCESS) {
+        delete ctx;
+        return solver_fail(st, "cusolverDnCreate");
+    }
+    *out = ctx;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_context_destroy(flmm_context* ctx) {
+    if (!ctx) return FLMM_OK;
+    if (ctx->solver) cusolverDnDestroy(ctx->solver);
+    delete ctx;
+    return FLMM_OK;
+}
+
+// ---- eigendecomposition -------------------------------------------------------------------------------------
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+extern "C" int flmm_eigh_workspace_bytes(flmm_context* ctx, int N, size_t* bytes) {
+    FLMM_REQUIRE(ctx && bytes && N > 0, "flmm_eigh_workspace_bytes: bad arguments");
+    int lwork = 0;
+    cusolverStatus_t st = cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                      N, nullptr, N, nullptr, &lwork);
+    if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnDsyevd_bufferSize");
+    *bytes = align_up(sizeof(double) * static_cast<size_t>(lwork), 256) + 256;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_eigh(flmm_context* ctx, double* A, int N, double* evals, void* work, size_t work_bytes,
+                         void* stream) {
+    FLMM_REQUIRE(ctx && A && evals && work && N > 0, "flmm_eigh: bad arguments");
+    size_t need = 0;
+    int rc = flmm_eigh_workspace_bytes(ctx, N, &need);
+    if (rc) return rc;
+    if (work_bytes < need) return fail(FLMM_ERR_WORKSPACE, "flmm_eigh: need %zu bytes, got %zu", need, work_bytes);
+    int lwork = static_cast<int>((need - 256) / sizeof(double));
+    double* dwork = static_cast<double*>(work);
+    int* info = reinterpret_cast<int*>(static_cast<char*>(work) + need - 256);
+    cusolverDnSetStream(ctx->solver, as_stream(stream));
+    // symmetric input: row-major and column-major views coincide; the eigenvector k comes back as column k of the
+    // column-major result, i.e. row k of the row-major view
+    cusolverStatus_t st = cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N,
+                                           evals, dwork, lwork, info);
+    if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnDsyevd");
+    return check_cuda("cusolverDnDsyevd");
+}
+
+// ---- covariate basis (thin SVD of X) --------------------------------------------------------------------------
+
+namespace {
+
+// row-major X (N, D) -> column-major copy for gesvd
+__global__ void k_to_colmajor(const double* __restrict__ X, int N, int D, double* __restrict__ Xc) {
+    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t >= static_cast<int64_t>(N) * D) return;
+    int i = static_cast<int>(t / D), d = static_cast<int>(t % D);
+    Xc[static_cast<int64_t>(d) * N + i] = X[t];
+}
+
+// rank by torch.linalg.pinv's default cut (sigma > eps * max(N, D) * sigma_max), the orthonormal basis rows and
+// Xpinv = V diag(1 / sigma) U^T over the kept singular triplets.  S is descending (gesvd).
+__global__ void k_basis_from_svd(const double* __restrict__ U, const double* __restrict__ S,
+                                 const double* __restrict__ VT, int N, int D, double* __restrict__ Qx,
+                                 double* __restrict__ Xpinv, int32_t* __restrict__ rank_dev) {
+    const double cut = 2.220446049250313e-16 * static_cast<double>(N > D ? N : D) * S[0];
+    int rank = 0;
+    for (int r = 0; r < D; ++r) rank += (S[r] > cut) ? 1 : 0;
+    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t == 0) *rank_dev = rank;
+    if (t >= static_cast<int64_t>(N) * D) return;
+    int d = static_cast<int>(t / N), i = static_cast<int>(t % N);
+    Qx[t] = (d < rank) ? U[static_cast<int64_t>(d) * N + i] : 0.0;
+    double acc = 0.0;
+    for (int r = 0; r < rank; ++r) acc += VT[static_cast<int64_t>(d) * D + r] * (U[static_cast<int64_t>(r) * N + i] / S[r]);
+    Xpinv[t] = acc;
+}
+
+struct SvdLayout {
+    size_t xc, u, s, vt, rwork, work, info, total;
+    int lwork;
+};
+
+int svd_layout(flmm_context* ctx, int N, int D, SvdLayout* L) {
+    int lwork = 0;
+    cusolverStatus_t st = cusolverDnDgesvd_bufferSize(ctx->solver, N, D, &lwork);
+    if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnDgesvd_bufferSize");
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L->xc = take(sizeof(double) * N * D);
+    L->u = take(sizeof(double) * N * D);
+    L->s = take(sizeof(double) * D);
+    L->vt = take(sizeof(double) * D * D);
+    L->rwork = take(sizeof(double) * D);
+    L->work = take(sizeof(double) * static_cast<size_t>(lwork));
+    L->info = take(sizeof(int));
+    L->total = off;
+    L->lwork = lwork;
+    return FLMM_OK;
+}
+
+}  // namespace
+
+extern "C" int flmm_covariate_basis_workspace_bytes(flmm_context* ctx, int N, int D, size_t* bytes) {
+    FLMM_REQUIRE(ctx && bytes && N >= D && D > 0, "flmm_covariate_basis_workspace_bytes: need N >= D > 0");
+    SvdLayout L;
+    int rc = svd_layout(ctx, N, D, &L);
+    if (rc) return rc;
+    *bytes = L.total;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_covariate_basis(flmm_context* ctx, const double* X, int N, int D, double* Qx, double* Xpinv,
+                                    int32_t* rank_dev, void* work, size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(ctx && X && Qx && Xpinv && rank_dev && work, "flmm_covariate_basis: NULL argument");
+    FLMM_REQUIRE(N >= D && D > 0, "flmm_covariate_basis: need N >= D > 0 (N=%d, D=%d)", N, D);
+    SvdLayout L;
+    int rc = svd_layout(ctx, N, D, &L);
+    if (rc) return rc;
+    if (work_bytes < L.total)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_covariate_basis: need %zu bytes, got %zu", L.total, work_bytes);
+    char* w = static_cast<char*>(work);
+    double* Xc = reinterpret_cast<double*>(w + L.xc);
+    double* U = reinterpret_cast<double*>(w + L.u);
+    double* S = reinterpret_cast<double*>(w + L.s);
+    double* VT = reinterpret_cast<double*>(w + L.vt);
+    double* rwork = reinterpret_cast<double*>(w + L.rwork);
+    double* dwork = reinterpret_cast<double*>(w + L.work);
+    int* info = reinterpret_cast<int*>(w + L.info);
+    cudaStream_t st = as_stream(stream);
+    int64_t nd = static_cast<int64_t>(N) * D;
+    k_to_colmajor<<<ceil_div(nd, 256), 256, 0, st>>>(X, N, D, Xc);
+    if ((rc = check_launch("k_to_colmajor"))) return rc;
+    cusolverDnSetStream(ctx->solver, st);
+    cusolverStatus_t cs = cusolverDnDgesvd(ctx->solver, 'S', 'S', N, D, Xc, N, S, U, N, VT, D, dwork, L.lwork,
+                                           rwork, info);
+    if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail(cs, "cusolverDnDgesvd");
+    k_basis_from_svd<<<ceil_div(nd, 256), 256, 0, st>>>(U, S, VT, N, D, Qx, Xpinv, rank_dev);
+    return check_launch("k_basis_from_svd");
+}

@@ -1,0 +1,75 @@
+// Shared helpers of the fasterlmm_gb300 CUDA library: status handling, argument checks, warp reductions and the
+// FP64 atomic max used by the per-column genome max.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fasterlmm_gb300.h"
+
+namespace flmm {
+
+// Records a printf-style message as this thread's last error (read back by flmm_last_error) and returns `status`.
+int fail(int status, const char* fmt, ...);
+
+// Counts one kernel launch of this library and converts the pending CUDA error (if any) into FLMM_ERR_CUDA with
+// the kernel's name.  Call once right after each <<<...>>> launch.
+int check_launch(const char* what);
+
+// Same error conversion without counting a launch (after library calls such as cuSOLVER).
+int check_cuda(const char* what);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned ceil_div(int64_t a, int64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
+
+#define FLMM_REQUIRE(cond, ...)                                                       \
+    do {                                                                              \
+        if (!(cond)) return ::flmm::fail(FLMM_ERR_ARG, __VA_ARGS__);                  \
+    } while (0)
+
+#define FLMM_CUDA(call)                                                               \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return ::flmm::fail(FLMM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// max over non-negative (or NaN) doubles stored as their bit patterns: for x >= 0 the IEEE bit pattern read as a
+// signed 64-bit integer is monotone in x, -inf (the initial value) reads negative, and NaN reads above +inf, so
+// a NaN column statistic propagates as torch.maximum would.
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+    atomicMax(reinterpret_cast<long long*>(addr), __double_as_longlong(v));
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(float* addr, float v) {
+    atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+}
+
+// FP64 helpers that are never contracted into an FMA, so an expression evaluates with the same roundings as the
+// reference's separate tensor operations.
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// Positive clamp floor of the FP64 path (fasterlmm/core.py:80-86).
+constexpr double kPosFloor = 1e-300;
+
+}  // namespace flmm

@@ -1,0 +1,120 @@
+"""
+ctypes binding of the C ABI in include/fasterlmm_gb300.h.
+
+The library is loaded once per process.  There is no fallback: if ``libfasterlmm_gb300.so`` has not been built,
+every call raises.  Status codes other than FLMM_OK raise :class:`FlmmError` carrying the library's message.
+ctypes releases the GIL for the duration of each call.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfasterlmm_gb300.so"
+
+_i, _i64, _d, _p, _sz = C.c_int, C.c_int64, C.c_double, C.c_void_p, C.c_size_t
+_pi32 = C.POINTER(C.c_int32)
+_psz = C.POINTER(C.c_size_t)
+
+# name -> argument types (all return int status unless listed in _RESTYPE)
+SIGNATURES: dict[str, list] = {
+    "flmm_version": [],
+    "flmm_status_string": [_i],
+    "flmm_last_error": [],
+    "flmm_kernel_launches": [],
+    "flmm_context_create": [_i, C.POINTER(_p)],
+    "flmm_context_destroy": [_p],
+    "flmm_standardise_f64": [_p, _i64, _i, _i, _p, _i64, _p],
+    "flmm_standardise_dosage": [_p, _i64, _i, _i, _p, _i64, _p],
+    "flmm_transpose_f64": [_p, _i64, _i, _i, _p, _i64, _p],
+    "flmm_gram_f64": [_p, _i64, _i, _i, _d, _p, _i64, _p],
+    "flmm_loco_kinship": [_p, _p, _i64, _i, _d, _p, _p],
+    "flmm_covariate_basis_workspace_bytes": [_p, _i, _i, _psz],
+    "flmm_covariate_basis": [_p, _p, _i, _i, _p, _p, _p, _p, _sz, _p],
+    "flmm_project_kinship_workspace_bytes": [_i, _i, _psz],
+    "flmm_project_kinship": [_p, _i64, _p, _i, _i, _p, _i64, _p, _sz, _p],
+    "flmm_eigh_workspace_bytes": [_p, _i, _psz],
+    "flmm_eigh": [_p, _p, _i, _p, _p, _sz, _p],
+    "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
+    "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],
+    "flmm_gemm_nt_f64": [_p, _i64, _p, _i64, _p, _i64, _i, _i, _i, _d, _p],
+    "flmm_delta_grid_nodes": [_d, _d, _i, _p, _p],
+    "flmm_fit_delta_f64_workspace_bytes": [_i, _i, _psz],
+    "flmm_fit_delta_f64": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
+    "flmm_wald_f64_workspace_bytes": [_i, _i, _psz],
+    "flmm_wald_f64": [_p, _i, _p, _i64, _p, _i, _i, _p, _i64, _i, _p, _p, _p, _p, _p, _i64, _p, _p, _sz, _p],
+    "flmm_axpy_f64": [_i64, _d, _p, _p, _p],
+    "flmm_pack_perm_columns": [_p, _i64, _i, _i, _p, _i, _p, _i64, _p],
+    "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
+    "flmm_fill_f64": [_p, _i64, _d, _p],
+    "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+}
+_RESTYPE = {"flmm_status_string": C.c_char_p, "flmm_last_error": C.c_char_p, "flmm_kernel_launches": C.c_uint64}
+
+
+class FlmmError(RuntimeError):
+    def __init__(self, fn: str, status: int, message: str):
+        super().__init__(f"{fn} failed: {message} (status {status})")
+        self.status = status
+
+
+_lock = threading.RLock()
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it is missing (build it with ``fasterlmm_gb300.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(f"fasterlmm_gb300 CUDA library not built ({LIB_PATH} missing); "
+                                   "run fasterlmm_gb300.build() -- there is no CPU fallback")
+            h = C.CDLL(str(LIB_PATH))
+            for name, argtypes in SIGNATURES.items():
+                fn = getattr(h, name)
+                fn.argtypes = argtypes
+                fn.restype = _RESTYPE.get(name, C.c_int)
+            _lib = h
+    return _lib
+
+
+def call(name: str, *args) -> None:
+    """Call an int-status entry point; raise FlmmError on failure."""
+    h = lib()
+    rc = getattr(h, name)(*args)
+    if rc != 0:
+        msg = h.flmm_last_error().decode(errors="replace") or h.flmm_status_string(rc).decode()
+        raise FlmmError(name, rc, msg)
+
+
+def query_bytes(name: str, *args) -> int:
+    out = C.c_size_t(0)
+    call(name, *args, C.byref(out))
+    return int(out.value)
+
+
+_contexts: dict[int, C.c_void_p] = {}
+
+
+def context(device: int) -> C.c_void_p:
+    """Per-device library context (cuSOLVER handle), created on first use and kept for the process."""
+    with _lock:
+        ctx = _contexts.get(device)
+        if ctx is None:
+            ctx = C.c_void_p()
+            h = lib()
+            rc = h.flmm_context_create(device, C.byref(ctx))
+            if rc != 0:
+                raise FlmmError("flmm_context_create", rc, h.flmm_last_error().decode(errors="replace"))
+            _contexts[device] = ctx
+        return ctx
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(lib().flmm_kernel_launches())

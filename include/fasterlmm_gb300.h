@@ -1,0 +1,166 @@
+/*
+ * fasterlmm_gb300 -- C ABI of the GB300 (sm_103a) batched LMM association scan.
+ *
+ * Every entry point takes caller-owned DEVICE pointers, plain sizes and leading dimensions, a CUDA stream passed as
+ * `void*` (NULL = legacy default stream), and returns an int status (FLMM_OK = 0).  Launches are asynchronous on
+ * that stream unless stated otherwise; an entry point never synchronises the device.  Scratch memory is passed in
+ * by the caller (`work`, `work_bytes`), sized by the matching *_workspace_bytes query.  No entry point allocates
+ * except flmm_context_create.
+ *
+ * Matrix layouts (row-major, element (i, j) at ptr[i * ld + j]):
+ *   Zt    (M, N)     standardised variants, variant-major: row m = one variant's N samples
+ *   Yt    (P, N)     phenotype columns, column-major in the reference's terms: row p = one column's N samples
+ *   Ut    (Neff, N)  kept eigenvectors, one per row (the transpose of the reference's U_eff)
+ *   UYt   (P, Neff)  rotated phenotypes (transpose of the reference's UY)
+ *   USt   (Mc, Neff) rotated variants of one chromosome (transpose of the reference's US)
+ *   out   (M, B)     per-variant detail of the B real columns, variant-major like the reference's ScanResult
+ *
+ * The interface replaces the Python functions of the reference's scan path (paths inside the reference project);
+ * each declaration cites the function whose work it does.
+ */
+#ifndef FASTERLMM_GB300_H
+#define FASTERLMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------------------------------------------- */
+#define FLMM_OK 0
+#define FLMM_ERR_ARG 1          /* null pointer, bad size, bad leading dimension or misalignment */
+#define FLMM_ERR_CUDA 2         /* a CUDA runtime call or kernel launch failed */
+#define FLMM_ERR_SOLVER 3       /* cuSOLVER returned an error */
+#define FLMM_ERR_WORKSPACE 4    /* work_bytes smaller than the *_workspace_bytes query */
+#define FLMM_ERR_DEVICE 5       /* the device is not an sm_103 (GB300) part */
+#define FLMM_ERR_TIMEOUT 6      /* a bounded device-side wait gave up; the kernel returned without its result */
+
+typedef struct flmm_context flmm_context;
+
+/* Version of this ABI (major * 10000 + minor * 100 + patch). */
+int flmm_version(void);
+/* Static string for a status code. */
+const char* flmm_status_string(int status);
+/* Text of the last CUDA / cuSOLVER error seen on this thread (empty if none). */
+const char* flmm_last_error(void);
+
+/* Number of kernels this library has launched in this process (library calls such as cuSOLVER not counted). */
+uint64_t flmm_kernel_launches(void);
+
+/* Create / destroy a per-device context (cuSOLVER handle, device properties).  Allocates host memory and library
+ * handles; the only allocating entry point.  `device` must be an sm_103 GPU. */
+int flmm_context_create(int device, flmm_context** out);
+int flmm_context_destroy(flmm_context* ctx);
+
+/* ---- input preparation ------------------------------------------------------------------------------------ */
+
+/* Unit standardiser (fasterlmm/io.py:223-246, torch branch): NaN-aware column mean and population std (ddof = 0),
+ * std == 0 -> inf, (z - mean) / std, NaN -> 0.  Input Z (N, M) sample-major FP64 with NaN for missing calls, leading
+ * dimension ldz >= M; output Zt (M, N) variant-major, leading dimension ldzt >= N. */
+int flmm_standardise_f64(const double* Z, int64_t ldz, int N, int M, double* Zt, int64_t ldzt, void* stream);
+
+/* Same standardiser from int8 dosages Gt (M, N) variant-major (0/1/2, negative = missing).  Statistics are exact
+ * integer sums, so mean and std are exact to one rounding. */
+int flmm_standardise_dosage(const int8_t* Gt, int64_t ldg, int N, int M, double* Zt, int64_t ldzt, void* stream);
+
+/* Out-of-place FP64 transpose: At (cols, rows) = A (rows, cols)^T; moves the reference's sample-major (N, M)
+ * layouts into the variant-major layout of this library. */
+int flmm_transpose_f64(const double* A, int64_t lda, int rows, int cols, double* At, int64_t ldat, void* stream);
+
+/* ---- kinship ---------------------------------------------------------------------------------------------- */
+
+/* Gram of a variant block, the GRM numerator (fasterlmm/io.py:257-265): Gc (N, N) = sum over rows m of
+ * Zt[m]^T Zt[m], FP64; beta = 0 overwrites Gc, beta = 1 accumulates.  Used per chromosome so that every LOCO
+ * kinship is (total - own chromosome) / M_loco (hoisting fasterlmm/core.py:711 out of the chromosome loop). */
+int flmm_gram_f64(const double* Zt, int64_t ldzt, int M, int N, double beta, double* Gc, int64_t ldg, void* stream);
+
+/* K (N, N) = (Gtot - Gc) / m_loco.  Gc may be NULL (single-K: K = Gtot / m_loco). */
+int flmm_loco_kinship(const double* Gtot, const double* Gc, int64_t ld, int N, double m_loco, double* K, void* stream);
+
+/* ---- compat rotation (fasterlmm/core.py:487-519) ------------------------------------------------------------ */
+
+/* Covariate basis: thin SVD of X (N, D) row-major in FP64 on the device (cuSOLVER gesvd), rank by the same
+ * relative cut as torch.linalg.pinv (sigma > eps * max(N, D) * sigma_max).  Outputs Qx (D, N): the first `rank`
+ * rows are an orthonormal basis of range(X), the rest zero; Xpinv (D, N) = pinv(X); rank on the device. */
+int flmm_covariate_basis_workspace_bytes(flmm_context* ctx, int N, int D, size_t* bytes);
+int flmm_covariate_basis(flmm_context* ctx, const double* X, int N, int D, double* Qx, double* Xpinv,
+                         int32_t* rank_dev, void* work, size_t work_bytes, void* stream);
+
+/* Kp (N, N) = (I - PX)(K + I)(I - PX) with PX = Qx^T Qx (fasterlmm/core.py:499-506), formed as a rank-2D update
+ * of K + I (no N^3 products); rows of Qx beyond the rank are zero and drop out.  Workspace: 2 N D + D D doubles. */
+int flmm_project_kinship_workspace_bytes(int N, int D, size_t* bytes);
+int flmm_project_kinship(const double* K, int64_t ldk, const double* Qx, int N, int D, double* Kp, int64_t ldkp,
+                         void* work, size_t work_bytes, void* stream);
+
+/* Symmetric eigendecomposition in FP64 (cuSOLVER syevd; fasterlmm/core.py:54-77).  A (N, N) is overwritten by
+ * the eigenvectors, stored one per row (ascending eigenvalue order), so rows D.. are Ut.  evals (N,) ascending. */
+int flmm_eigh_workspace_bytes(flmm_context* ctx, int N, size_t* bytes);
+int flmm_eigh(flmm_context* ctx, double* A, int N, double* evals, void* work, size_t work_bytes, void* stream);
+
+/* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514). */
+int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream);
+
+/* OLS regress-out of the covariates, row-wise: R[i] = A[i] - X (Xpinv A[i]^T) for rows of A (rows, N)
+ * (fasterlmm/core.py:517 for phenotypes, :628 for variants).  R may alias A. */
+int flmm_regress_out(const double* A, int64_t lda, int rows, int N, const double* X, int D, const double* Xpinv,
+                     double* R, int64_t ldr, void* stream);
+
+/* FP64 C (Mr, Nr) = alpha * A (Mr, K) * B (Nr, K)^T, both operands K-contiguous (the rotations UY = U_eff^T Y_r
+ * and US = U_eff^T S_r, fasterlmm/core.py:518, :629, computed transposed). */
+int flmm_gemm_nt_f64(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int Mr,
+                     int Nr, int K, double alpha, void* stream);
+
+/* ---- null-model delta fit (fasterlmm/core.py:525-595) --------------------------------------------------------- */
+
+/* Grid node values exactly as torch.linspace(lo, hi, n_grid) in FP64. */
+int flmm_delta_grid_nodes(double lo, double hi, int n_grid, double* grid, void* stream);
+
+/* Plain FP64 form: (G, P) grid loss, first argmin, then the reference's 50-step golden-section search on
+ * [grid[i-1], grid[i+1]] with its update order, result clamped to [lo, hi]; refine = 0 returns the grid node.
+ * Outputs log_delta (P,) and grid_idx (P,).  Workspace holds the (G, Neff) weights. */
+int flmm_fit_delta_f64_workspace_bytes(int Neff, int n_grid, size_t* bytes);
+int flmm_fit_delta_f64(const double* s, int Neff, const double* UYt, int64_t ldu, int P, int n_grid, double lo,
+                       double hi, int refine, double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
+                       void* stream);
+
+/* ---- Wald scan (fasterlmm/core.py:601-671) -------------------------------------------------------------------- */
+
+/* Plain FP64 form: for every column p < P and variant m < Mc: sWy = sum_n w UY US, sWs = sum_n w US^2 with
+ * w = 1 / (s + exp(log_delta[p])), then beta, var_beta (df Neff - 1), F with the reference's clamps; max_F[p] is
+ * raised to the column max (int64 atomic max on the FP64 bit pattern, F >= 0).  Real columns p < n_real write
+ * f / beta / se / sfve at out[rows[m] * ldo + p].  Workspace holds w and w * UY (2 P Neff doubles). */
+int flmm_wald_f64_workspace_bytes(int P, int Neff, size_t* bytes);
+int flmm_wald_f64(const double* s, int Neff, const double* UYt, int64_t ldu, const double* log_delta, int P,
+                  int n_real, const double* USt, int64_t ldus, int Mc, const int64_t* rows, double* f, double* beta,
+                  double* se, double* sfve, int64_t ldo, double* max_F, void* work, size_t work_bytes, void* stream);
+
+/* y[i] += alpha * x[i], FP64 (sums the per-chromosome Grams into the all-variant Gram). */
+int flmm_axpy_f64(int64_t n, double alpha, const double* x, double* y, void* stream);
+
+/* Permutation packing (fasterlmm/perms.py:56-59): Yt_all (B + B n_perm, N) gets the B real columns Yt_real (B, N)
+ * as its first rows, then for each real column b its n_perm shuffles, pheno-major: row B + b n_perm + j holds
+ * Yt_real[b, orders[(b n_perm + j) N + n]] at sample n.  orders are 0-based row indices < N. */
+int flmm_pack_perm_columns(const double* Yt_real, int64_t ldy, int B, int N, const int32_t* orders, int n_perm,
+                           double* Yt_all, int64_t lda, void* stream);
+
+/* nullh2 = 1 / (1 + exp(log_delta[p])) for p < n_real at out[rows[m] * ldo + p] (fasterlmm/core.py:669-670). */
+int flmm_fill_nullh2(const double* log_delta, int n_real, const int64_t* rows, int Mc, double* nullh2, int64_t ldo,
+                     void* stream);
+
+/* Fill x[0..n) with a constant (max_F starts at -inf, fasterlmm/core.py:706). */
+int flmm_fill_f64(double* x, int64_t n, double value, void* stream);
+
+/* ---- post-scan statistics (fasterlmm/cli.py:405-406) ----------------------------------------------------------- */
+
+/* out[i] = -log10 P(F(1, df2) > F[i]) in FP64, from the regularized incomplete beta I_{df2/(df2+F)}(df2/2, 1/2)
+ * evaluated in log space by the modified Lentz continued fraction, so large F gives a finite value where
+ * scipy.stats.f.sf underflows to 0. */
+int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTERLMM_GB300_H */

@@ -1,0 +1,67 @@
+"""
+CPU checks of the C ABI: the library builds for sm_103a, loads without a GPU, and exports every entry point that
+include/*.h declares; the Python binding declares exactly those entry points.  No compute call is made here.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def _declared() -> set[str]:
+    names = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(flmm_\w+)\s*\(", text, flags=re.M))
+    return names
+
+
+@pytest.fixture(scope="module")
+def built():
+    from fasterlmm_gb300 import build
+    return build()
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(str(built))
+    declared = _declared()
+    assert len(declared) >= 20
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, f"declared in include/ but not exported: {missing}"
+
+
+def test_binding_matches_header(built):
+    from fasterlmm_gb300 import _lib
+    assert set(_lib.SIGNATURES) == _declared()
+    h = _lib.lib()
+    assert h.flmm_version() >= 100
+    assert h.flmm_status_string(0).decode() == "ok"
+    assert "workspace" in h.flmm_status_string(4).decode()
+
+
+def test_argument_errors_without_gpu(built):
+    """Argument validation happens on the host before any CUDA call, so it is testable without a device."""
+    from fasterlmm_gb300 import _lib
+    with pytest.raises(_lib.FlmmError) as e:
+        _lib.call("flmm_fill_f64", None, 10, 0.0, None)
+    assert e.value.status == 1
+    with pytest.raises(_lib.FlmmError):
+        _lib.call("flmm_neglog10_pvalue", None, 5, 0, None, None)
+    size = ctypes.c_size_t(0)
+    _lib.call("flmm_wald_f64_workspace_bytes", 100, 50, ctypes.byref(size))
+    assert size.value >= 8 * (2 * 100 * 50 + 100)
+
+
+def test_no_cpu_fallback_without_cuda():
+    """The product path refuses to run without a CUDA device instead of computing on the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from fasterlmm_gb300 import core
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        core.grm(torch.zeros(4, 4, dtype=torch.float64))
