@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""
+Benchmark of the batched LMM association scan (FaST-ER-LMM's perm_threshold -> loco_scan_compat path) on GB300.
+
+Metric: variant-phenotype tests per second, tests = M variants x B phenotypes x (1 + n_perm) (the reference's
+"Wald ops", fasterlmm/watch.py:194-199).  Workload: 1,000 samples x 100,000 variants over 20 chromosomes, 6,484
+phenotypes x 10 permutations (71,324 scan columns), 5 covariate columns, seeded synthetic inputs.
+
+One step = one full permutation scan of that workload through fasterlmm_gb300.perms.perm_threshold: standardise,
+per-chromosome kinship Grams, 20 x (projection, FP64 eigendecomposition, rotations, delta fit, fused Wald scan),
+permutation orders drawn per step.  ``value`` times steps with the inputs already on the device; ``e2e`` times the
+same call with host (pinned) inputs and host outputs, copies included.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast|plain] [--impl ours|reference]
+
+``--impl reference`` times the CPU restatement of the reference's algorithm (oracle/flmm_oracle.py) on the host's
+cores on a bounded sample of the same workload (one chromosome x one 256-phenotype batch per step).
+Under torchrun (N > 1) every rank runs its own replica of the workload (the scan has no cross-GPU exchange) and
+the line reports the total over ranks against the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+from types import SimpleNamespace
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT / "fast-er-lmm_gb300", ROOT / "oracle"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "n1000_m100k_b6484_perm10"
+METRIC = "variant-phenotype tests/s, 1 GB300: chosen vs plain form at |Δ-log10p|≤1e-3"
+UNIT = "tests/s"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.device_index = device_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "tensor_tflops": d.get("bf16_tflops"),
+                "tensor_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "tensor_tflops": 1900.0, "tensor_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def make_inputs(B: int | None, M: int | None):
+    from fasterlmm_gb300.synth import make_workload
+    d, w = make_workload(WORKLOAD, B=B, M=M)
+    return d, w
+
+
+# ---- CPU baseline: the oracle on a bounded sample ------------------------------------------------------------------
+
+def cpu_sample_run(d, w, B_sample: int, chrom_id: int = 1) -> tuple[float, int]:
+    """One CLI-sized batch (B_sample phenotypes + their permutations) through one LOCO chromosome, oracle on CPU."""
+    import flmm_oracle as orc
+    Z = orc.standardise_columns(d.Z_float())
+    n_perm = w["n_perm"]
+    orders = orc.perm_orders(Z.shape[0], range(B_sample), n_perm)
+    Y_all = orc.pack_perms(d.Y[:, :B_sample], orders)
+    t0 = time.perf_counter()
+    mask = d.chrom == chrom_id
+    K = orc.grm(Z[:, ~mask])
+    spec = orc.compat_rotate(K, d.X, Y_all)
+    ld = orc.fit_delta_grid_compat(spec["s"], spec["UY"], n_grid=w["n_grid"], log_delta_min=w["log_delta_min"],
+                                   log_delta_max=w["log_delta_max"])
+    orc.snp_wald_scan_compat(spec, ld, Z[:, mask], n_real=B_sample)
+    dt = time.perf_counter() - t0
+    return dt, int(mask.sum()) * B_sample * (1 + n_perm)
+
+
+def cpu_baseline(d, w, target_s: float = 12.0) -> dict:
+    B_sample = min(256, w["B"])
+    total_t, total_tests, runs = 0.0, 0, 0
+    chroms = sorted(np.unique(d.chrom).tolist())
+    while total_t < target_s and runs < len(chroms):
+        dt, n = cpu_sample_run(d, w, B_sample, chroms[runs])
+        total_t += dt
+        total_tests += n
+        runs += 1
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": total_tests / total_t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{runs} LOCO chromosome(s) x one {B_sample}-phenotype batch with {w['n_perm']} permutations each "
+                      f"(GRM, compat rotation, 64-point grid + golden section, Wald), numpy FP64 on {cores} host "
+                      f"threads; {total_tests} tests in {total_t:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    d, w = make_inputs(args.B, args.M)
+    B_sample = min(256, w["B"])
+    chroms = sorted(np.unique(d.chrom).tolist())
+    for i in range(args.warmup):
+        cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)])
+    times, tests = [], []
+    for i in range(args.steps):
+        dt, n = cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)])
+        times.append(dt)
+        tests.append(n)
+    value = sum(tests) / sum(times)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "N": w["N"], "M": w["M"], "B": w["B"], "n_perm": w["n_perm"],
+                       "step": f"one LOCO chromosome x one {B_sample}-phenotype batch (+{w['n_perm']} perms each)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"one chromosome x {B_sample} phenotypes per step, numpy FP64"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU arm ----------------------------------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from fasterlmm_gb300 import _lib, build, perms
+    build()
+    d, w = make_inputs(args.B, args.M)
+    N, M, B, n_perm = w["N"], w["M"], w["B"], w["n_perm"]
+    P = B * (1 + n_perm)
+    tests_per_step = M * B * (1 + n_perm)
+    grid_kw = dict(n_grid=w["n_grid"], log_delta_min=w["log_delta_min"], log_delta_max=w["log_delta_max"])
+    Zf = d.Z_float()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a))
+    data_dev = SimpleNamespace(Z=t(Zf).to(dev), Y=t(d.Y).to(dev), X=t(d.X).to(dev), chrom=d.chrom, Z_kin=None,
+                               chrom_kin=None)
+    pheno = list(range(B))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    timers: dict = {}
+
+    def step(tm=None):
+        return perms.perm_threshold(data_dev, pheno, n_perm=n_perm, form=args.form, timers=tm, **grid_kw)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    launches0 = _lib.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        res, pmf = step(timers)
+        del res, pmf
+    ev1.record()
+    barrier()
+    wall = time.perf_counter() - w0
+    launches = _lib.kernel_launches() - launches0
+    clk = clocks.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    value = world * tests_per_step * args.steps / elapsed
+
+    # dominant kernel: the fused Wald scan, timed by events around its launches inside the timed steps
+    wald_ms = [a.elapsed_time(b) for a, b in timers.get("wald", []) if b is not None]
+    peaks = measured_peaks()
+    Neff = N - w["D"]
+    mc_mean = M / w["n_chrom"]
+    roof = None
+    if wald_ms:
+        mean_s = statistics.mean(wald_ms) / 1e3
+        alg_flop = 4.0 * Neff * P * mc_mean
+        achieved = alg_flop / mean_s / 1e12
+        peak = peaks["tensor_tflops"]
+        traffic = None
+        tp = ROOT / "profiles" / "wald_traffic.json"
+        if tp.exists():
+            traffic = json.loads(tp.read_text()).get("bytes_per_launch_scaled")
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "k_tc<wald> (fused split-FP16 Wald)", "launch_ms": 1e3 * mean_s,
+                "algorithmic_flop_per_launch": alg_flop, "executed_tensor_frac": 3 * achieved / peak,
+                "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp16x2-split tensor (FP32 acc) + f64" if args.form == "fast" else "f64",
+            "data": "synthetic (seeded: Binomial(2, MAF~U[0.01,0.5]) genotypes, RINT phenotypes, 0-50 causal)",
+            "config": {"workload": WORKLOAD, "N": N, "M": M, "B": B, "n_perm": n_perm, "P": P, "chromosomes": w["n_chrom"],
+                       "covariates": w["D"], "grid": w["n_grid"], "form": args.form,
+                       "l2": "inputs larger than L2 (Z 0.8 GB FP64, operands >100 MB per chromosome)",
+                       "parallelism": f"{world} replica(s), no cross-GPU exchange"},
+            "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "clocks": clk}
+
+    if rank == 0 and world == 1 and not args.no_e2e:
+        line["e2e"] = e2e_leg(args, d, w, pheno, grid_kw)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(d, w)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def e2e_leg(args, d, w, pheno, grid_kw) -> dict:
+    """Same scan through the public call with pinned host inputs and preallocated pinned host outputs."""
+    import torch
+    from fasterlmm_gb300 import perms
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    data_host = SimpleNamespace(Z=t(d.Z_float()), Y=t(d.Y), X=t(d.X), chrom=d.chrom, Z_kin=None, chrom_kin=None)
+    M, B, n_perm = w["M"], w["B"], w["n_perm"]
+    out = {k: torch.empty((M, B), dtype=torch.float64).pin_memory() for k in ("f", "beta", "se", "sfve", "nullh2")}
+    out["max_F"] = torch.empty(B * (1 + n_perm), dtype=torch.float64).pin_memory()
+    steps = max(1, min(args.steps, 3))
+    perms.perm_threshold(data_host, pheno, n_perm=n_perm, form=args.form, out=out, **grid_kw)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        perms.perm_threshold(data_host, pheno, n_perm=n_perm, form=args.form, out=out, **grid_kw)
+    dt = (time.perf_counter() - t0) / steps
+    h2d = sum(x.numel() * x.element_size() for x in (data_host.Z, data_host.Y, data_host.X))
+    d2h = sum(x.numel() * x.element_size() for x in out.values())
+    return {"value": M * B * (1 + n_perm) / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": 1e3 * dt, "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=["fast", "plain"], default="fast")
+    ap.add_argument("--B", type=int, default=None, help="override the phenotype count (quick runs)")
+    ap.add_argument("--M", type=int, default=None, help="override the variant count (quick runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

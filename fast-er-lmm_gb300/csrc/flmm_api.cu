@@ -15,6 +15,7 @@ struct flmm_context {
     int device = 0;
     int sm_count = 0;
     cusolverDnHandle_t solver = nullptr;
+    int* err_flag = nullptr;  // device int raised by kernels whose bounded waits time out
 };
 
 namespace flmm {
@@ -87,13 +88,34 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
         delete ctx;
         return solver_fail(st, "cusolverDnCreate");
     }
+    if (cudaMalloc(&ctx->err_flag, sizeof(int)) != cudaSuccess || cudaMemset(ctx->err_flag, 0, sizeof(int)) != cudaSuccess) {
+        cusolverDnDestroy(ctx->solver);
+        delete ctx;
+        return fail(FLMM_ERR_CUDA, "flmm_context_create: cannot allocate the device error flag");
+    }
     *out = ctx;
+    return FLMM_OK;
+}
+
+int flmm_ctx_sm_count(flmm_context* ctx) { return ctx->sm_count; }
+int* flmm_ctx_err_flag(flmm_context* ctx) { return ctx->err_flag; }
+
+extern "C" int flmm_context_check(flmm_context* ctx, void* stream) {
+    FLMM_REQUIRE(ctx, "flmm_context_check: NULL context");
+    int h = 0;
+    FLMM_CUDA(cudaMemcpyAsync(&h, ctx->err_flag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
+    FLMM_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    if (h != 0) {
+        FLMM_CUDA(cudaMemsetAsync(ctx->err_flag, 0, sizeof(int), as_stream(stream)));
+        return fail(FLMM_ERR_TIMEOUT, "a tensor-core kernel gave up a bounded wait (code %d)", h);
+    }
     return FLMM_OK;
 }
 
 extern "C" int flmm_context_destroy(flmm_context* ctx) {
     if (!ctx) return FLMM_OK;
     if (ctx->solver) cusolverDnDestroy(ctx->solver);
+    if (ctx->err_flag) cudaFree(ctx->err_flag);
     delete ctx;
     return FLMM_OK;
 }

@@ -1,0 +1,279 @@
+// Fast form of the null-model delta fit (fasterlmm/core.py:561-595).
+//
+// Grid: the (G, P) ML loss in FP32 from w[g, n] = 1 / (s_n + delta_g) and UY^2 (a tiled (G x Neff) x (Neff x P)
+// product), first argmin per column.  The bracket is the reference's [grid[i-1], grid[i+1]].
+//
+// Refinement: where the reference runs 50 golden-section steps on the loss, this finds the stationary point of the
+// loss in the bracket directly.  With x = log delta, r_n = 1 / (s_n + delta), S_k = sum u_n^2 r_n^k, T_k = sum r_n^k,
+//     dL/dx = delta (T1 - Neff S2 / S1),  d/dx (T1 - Neff S2 / S1) = delta (-T2 + Neff (2 S3 / S1 - S2^2 / S1^2)),
+// and a sign-safeguarded Newton iteration on g = T1 - Neff S2 / S1 keeps g(lo) < 0 < g(hi), so it always converges
+// to a local minimum of the loss in the bracket (never a maximum).  When g does not change sign the minimum is a
+// bracket edge, which is where the golden-section search converges as well.  S1, S2, T1 are accumulated with
+// Neumaier-compensated FP32 sums and combined across lanes in FP64, so g is accurate to the rounding of the
+// individual terms (~1e-7 relative each, averaging out over Neff); log delta comes out within ~1e-7 of the exact
+// stationary point, well inside the FP64 noise of the reference's own search on flat likelihoods.
+#include <math.h>
+
+#include "flmm_common.cuh"
+
+using namespace flmm;
+
+namespace {
+
+__global__ void k_grid_weights_f32(const double* __restrict__ s, int Neff, const double* __restrict__ grid,
+                                   float* __restrict__ Wg, float* __restrict__ sum_log) {
+    __shared__ double red[32];
+    const int g = blockIdx.x;
+    const double delta = exp(grid[g]);
+    double acc = 0.0;
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) {
+        const double sd = s[n] + delta;
+        Wg[static_cast<int64_t>(g) * Neff + n] = static_cast<float>(1.0 / sd);
+        acc += log(sd);
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) sum_log[g] = static_cast<float>(v);
+    }
+}
+
+constexpr int TG = 64, TP = 64, TK = 32, NT = 256;
+
+// loss[g, p] = Neff log(yWy) + sum_log[g] (+ constants that do not move the argmin), first argmin over g
+__global__ void __launch_bounds__(NT)
+k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_log, const float* __restrict__ UYt,
+                  int64_t ldu, int Neff, int P, int G, int32_t* __restrict__ idx_out) {
+    __shared__ float Ws[TK][TG + 1];
+    __shared__ float Us[TK][TP + 1];
+    __shared__ float red_v[16][TP];
+    __shared__ int red_i[16][TP];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int p0 = blockIdx.x * TP;
+    const float neff = static_cast<float>(Neff);
+    float best = INFINITY;
+    int best_g = 0;
+    for (int g0 = 0; g0 < G; g0 += TG) {
+        float acc[4][4] = {};
+        for (int k0 = 0; k0 < Neff; k0 += TK) {
+#pragma unroll
+            for (int l = 0; l < (TG * TK) / NT; ++l) {
+                int t = tid + l * NT, g = t / TK, k = t % TK;
+                int gg = g0 + g, gk = k0 + k;
+                Ws[k][g] = (gg < G && gk < Neff) ? Wg[static_cast<int64_t>(gg) * Neff + gk] : 0.0f;
+            }
+#pragma unroll
+            for (int l = 0; l < (TP * TK) / NT; ++l) {
+                int t = tid + l * NT, p = t / TK, k = t % TK;
+                int gp = p0 + p, gk = k0 + k;
+                float u = (gp < P && gk < Neff) ? UYt[static_cast<int64_t>(gp) * ldu + gk] : 0.0f;
+                Us[k][p] = u * u;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < TK; ++k) {
+                float a[4], b[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) a[r] = Ws[k][ty + 16 * r];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) b[c] = Us[k][tx + 16 * c];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float bv = INFINITY;
+            int bi = G;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                int g = g0 + ty + 16 * r;
+                if (g < G) {
+                    float v = neff * logf(fmaxf(acc[r][c], 1e-30f)) + sum_log[g];
+                    if (v < bv) { bv = v; bi = g; }
+                }
+            }
+            red_v[ty][tx + 16 * c] = bv;
+            red_i[ty][tx + 16 * c] = bi;
+        }
+        __syncthreads();
+        if (tid < TP) {
+            for (int r = 0; r < 16; ++r) {
+                float v = red_v[r][tid];
+                int gi = red_i[r][tid];
+                if (v < best || (v == best && gi < best_g)) { best = v; best_g = gi; }
+            }
+        }
+        __syncthreads();
+    }
+    if (tid < TP && p0 + tid < P) idx_out[p0 + tid] = best_g;
+}
+
+struct NewtonEval {
+    double g;      // T1 - Neff S2 / S1 (sign of d loss / d log delta)
+    double gp;     // dg / dx
+    double loss;   // Neff log S1 + sum log (s + delta), up to constants
+};
+
+__device__ __forceinline__ void neumaier(float& sum, float& comp, float x) {
+    const float t = sum + x;
+    comp += (fabsf(sum) >= fabsf(x)) ? ((sum - t) + x) : ((x - t) + sum);
+    sum = t;
+}
+
+// One evaluation by a warp at x = log delta (x is warp-uniform).
+//
+// g is formed around the centre c = 1 / (sbar + delta), sbar the mean eigenvalue: with d_n = r_n - c =
+// (sbar - s_n) r_n c,
+//     g = sum d - Neff (c E1 + E2) / (c U + E1),   U = sum u^2, E1 = sum u^2 d, E2 = sum u^2 d^2,
+// which is T1 - Neff S2 / S1 rearranged so that no O(r) terms cancel: when delta >> s the r_n are nearly equal and
+// the information in g is in their O(s / delta) spread, which the centred terms carry at full FP32 precision.
+__device__ NewtonEval newton_eval(const float* __restrict__ s32, float sbar, const float* __restrict__ u, int Neff,
+                                  double x, bool want_loss) {
+    const int lane = threadIdx.x & 31;
+    const double delta_d = exp(x);
+    const float delta = static_cast<float>(delta_d);
+    const float c = static_cast<float>(1.0 / (static_cast<double>(sbar) + delta_d));
+    float d1 = 0.f, cd1 = 0.f, e1 = 0.f, ce1 = 0.f, e2 = 0.f, e3 = 0.f, f2 = 0.f, uu_s = 0.f, cu = 0.f, sl = 0.f;
+    for (int n = lane; n < Neff; n += 32) {
+        const float sd = s32[n] + delta;
+        const float r = 1.0f / sd;
+        const float d = (sbar - s32[n]) * r * c;
+        const float uu = u[n] * u[n];
+        neumaier(d1, cd1, d);
+        neumaier(e1, ce1, uu * d);
+        e2 += uu * d * d;
+        e3 += uu * d * d * d;
+        f2 += d * d;
+        neumaier(uu_s, cu, uu);
+        if (want_loss) sl += __logf(sd);
+    }
+    const double D1 = warp_sum(static_cast<double>(d1) + static_cast<double>(cd1));
+    const double E1 = warp_sum(static_cast<double>(e1) + static_cast<double>(ce1));
+    const double E2 = warp_sum(static_cast<double>(e2));
+    const double E3 = warp_sum(static_cast<double>(e3));
+    const double F2 = warp_sum(static_cast<double>(f2));
+    const double U = warp_sum(static_cast<double>(uu_s) + static_cast<double>(cu));
+    NewtonEval e;
+    const double neff = static_cast<double>(Neff);
+    const double cc = static_cast<double>(c);
+    if (U > 0.0) {
+        e.g = D1 - neff * (cc * E1 + E2) / (cc * U + E1);
+        // dg/dx = delta (-T2 + Neff (2 S3 / S1 - (S2 / S1)^2)) in the same centred sums: with F2 = sum d^2,
+        // E3 = sum u^2 d^3, a = E1 / (c U), b = E2 / (c^2 U), t3 = E3 / (c^3 U) one has T2 = Neff c^2 + 2 c D1 + F2,
+        // S1 = c U (1 + a), S2 = c^2 U (1 + 2a + b), S3 = c^3 U (1 + 3a + 3b + t3), and the O(1) terms cancel exactly
+        const double a = E1 / (cc * U), b = E2 / (cc * cc * U), t3 = E3 / (cc * cc * cc * U);
+        const double br = -2.0 * D1 / (cc * neff) - F2 / (cc * cc * neff) + (2.0 * a + 4.0 * b + 2.0 * t3) / (1.0 + a) -
+                          (a + b) * (a + b) / ((1.0 + a) * (1.0 + a));
+        e.gp = delta_d * neff * cc * cc * br;
+    } else {  // all-zero rotated column: the loss only grows with delta
+        e.g = 1.0;
+        e.gp = 1.0;
+    }
+    e.loss = 0.0;
+    if (want_loss) e.loss = neff * log(fmax(cc * U + E1, 1e-300)) + warp_sum(static_cast<double>(sl));
+    return e;
+}
+
+__global__ void k_newton_refine(const double* __restrict__ s, int Neff, const float* __restrict__ UYt, int64_t ldu,
+                                int P, const double* __restrict__ grid, int G, const int32_t* __restrict__ idx,
+                                int refine, double* __restrict__ log_delta) {
+    extern __shared__ float s32[];
+    __shared__ float sbar_s;
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) s32[n] = static_cast<float>(s[n]);
+    if (threadIdx.x < 32) {
+        double acc = 0.0;
+        for (int n = threadIdx.x; n < Neff; n += 32) acc += s[n];
+        acc = warp_sum(acc);
+        if (threadIdx.x == 0) sbar_s = static_cast<float>(acc / Neff);
+    }
+    __syncthreads();
+    const float sbar = sbar_s;
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    if (p >= P) return;
+    int i = idx[p];
+    double out = grid[i];
+    if (refine && G > 1) {
+        const float* u = UYt + p * ldu;
+        // the FP32 grid can misplace the argmin by a node on flat losses: walk it with exact derivative signs
+        // until the loss rises on both sides of the bracket centre (bounded walk)
+        for (int step = 0; step < 8; ++step) {
+            if (i < G - 1 && newton_eval(s32, sbar, u, Neff, grid[i + 1], false).g < 0.0) { ++i; continue; }
+            if (i > 0 && newton_eval(s32, sbar, u, Neff, grid[i - 1], false).g > 0.0) { --i; continue; }
+            break;
+        }
+        const double a = grid[max(i - 1, 0)], b = grid[min(i + 1, G - 1)];
+        const NewtonEval ea = newton_eval(s32, sbar, u, Neff, a, false);
+        const NewtonEval eb = newton_eval(s32, sbar, u, Neff, b, false);
+        if (ea.g >= 0.0 && eb.g <= 0.0) {
+            // loss rises from a and falls towards b: the minimum is an edge
+            const NewtonEval la = newton_eval(s32, sbar, u, Neff, a, true);
+            const NewtonEval lb = newton_eval(s32, sbar, u, Neff, b, true);
+            out = (la.loss <= lb.loss) ? a : b;
+        } else if (ea.g >= 0.0) {
+            out = a;
+        } else if (eb.g <= 0.0) {
+            out = b;
+        } else {
+            double lo = a, hi = b;
+            double x = (grid[i] > lo && grid[i] < hi) ? grid[i] : 0.5 * (lo + hi);
+            for (int it = 0; it < 60; ++it) {
+                const NewtonEval e = newton_eval(s32, sbar, u, Neff, x, false);
+                if (e.g == 0.0) break;
+                if (e.g < 0.0) lo = x; else hi = x;
+                double xn = x - e.g / e.gp;
+                if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+                const double stepx = fabs(xn - x);
+                x = xn;
+                if (stepx < 1e-10 || hi - lo < 1e-10) break;
+            }
+            out = x;
+        }
+    }
+    if (lane == 0) log_delta[p] = out;
+}
+
+size_t fast_ws(int Neff, int G) {
+    return sizeof(float) * (static_cast<size_t>(G) * Neff + static_cast<size_t>(G)) + sizeof(double) * G + 512;
+}
+
+}  // namespace
+
+extern "C" int flmm_fit_delta_fast_workspace_bytes(int Neff, int n_grid, size_t* bytes) {
+    FLMM_REQUIRE(bytes && Neff > 0 && n_grid > 0, "flmm_fit_delta_fast_workspace_bytes: bad arguments");
+    *bytes = fast_ws(Neff, n_grid);
+    return FLMM_OK;
+}
+
+extern "C" int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
+                                   double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* work,
+                                   size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(s && UYt && log_delta && grid_idx && work && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
+                 "flmm_fit_delta_fast: bad arguments");
+    FLMM_REQUIRE(Neff <= 12288, "flmm_fit_delta_fast: Neff must be <= 12288 (shared-memory spectrum)");
+    if (work_bytes < fast_ws(Neff, n_grid))
+        return fail(FLMM_ERR_WORKSPACE, "flmm_fit_delta_fast: need %zu bytes, got %zu", fast_ws(Neff, n_grid), work_bytes);
+    if (P == 0) return FLMM_OK;
+    cudaStream_t st = as_stream(stream);
+    double* grid = static_cast<double*>(work);
+    float* Wg = reinterpret_cast<float*>(grid + n_grid);
+    float* sum_log = Wg + static_cast<size_t>(n_grid) * Neff;
+    int rc = flmm_delta_grid_nodes(lo, hi, n_grid, grid, stream);
+    if (rc) return rc;
+    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, grid, Wg, sum_log);
+    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
+    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
+    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
+    const size_t smem = sizeof(float) * static_cast<size_t>(Neff);
+    if (smem > 48 * 1024) FLMM_CUDA(cudaFuncSetAttribute(k_newton_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, st>>>(s, Neff, UYt, ldu, P, grid,
+                                                                                    n_grid, grid_idx, refine, log_delta);
+    return check_launch("k_newton_refine");
+}

@@ -1,0 +1,560 @@
+// Split-precision tensor-core form of the scan.
+//
+// Operands are carried as FP16 pairs x = (hi + lo) * 2^-e with one power-of-two exponent e per row (chosen so
+// the row's largest |x| 2^e lies in [2^14, 2^15)); |x - (hi + lo) 2^-e| <= 2^-22 |x| in the normal range.  A product
+// of two split operands is summed as hi*hi + hi*lo + lo*hi (the dropped lo*lo term is below 2^-22 relative), each
+// term a tcgen05.mma kind::f16 with FP32 accumulation in tensor memory, and the two row exponents are applied in
+// the epilogue.  This gives ~21-bit operand precision at FP16 tensor rate.
+//
+// One persistent kernel template serves both uses:
+//   NG = 1: C = A B^T for the eigenbasis rotations (UY = U_eff^T Y_r, US = U_eff^T S_r; fasterlmm/core.py:518, 629)
+//           and the per-chromosome Gram (fasterlmm/io.py:264);
+//   NG = 2: the Wald scan (fasterlmm/core.py:649-667): sWy = (w o UY) US^T and sWs = w (US o US)^T accumulated
+//           side by side, with beta, var_beta, F, SE, SFVE and the per-column genome max computed in the epilogue.
+// Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, warps 2-5 run the epilogue
+// (warp w reads TMEM lanes 32 (w % 4) .. +31).  Shared memory holds 3 stages of operand tiles; tensor memory holds
+// two accumulator sets so the epilogue of one tile overlaps the MMAs of the next.
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+#include <math.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "flmm_common.cuh"
+#include "flmm_tc.cuh"
+
+using namespace flmm;
+using namespace flmm::tc;
+
+namespace {
+
+constexpr int kBM = 128;  // A rows per tile (TMEM lanes)
+constexpr int kBN = 128;  // B rows per tile (accumulator columns)
+constexpr int kThreads = 192;
+
+template <int NG, int BK>
+struct Cfg {
+    static constexpr int kTileBytes = 128 * BK * 2;
+    static constexpr int kStageBytes = NG * 4 * kTileBytes;  // A hi, A lo, B hi, B lo per product
+    static constexpr int kStages = 3;
+    static constexpr uint32_t kSwizzle = (BK == 64) ? 2u : 4u;  // 128-byte / 64-byte swizzle
+    static constexpr uint32_t kSBO = 8u * BK * 2u;             // bytes between 8-row groups
+    static constexpr int kTmemCols = NG * kBN * 2;
+    static constexpr int kBarBytes = 256;
+    static constexpr int kSmemBytes = kStages * kStageBytes + kBarBytes + 1024;  // + alignment slack
+    static_assert(kStageBytes * kStages + kBarBytes + 1024 <= 227 * 1024, "shared memory budget");
+};
+
+struct TcMaps {
+    CUtensorMap m[8];  // [g * 4 + {0: A hi, 1: A lo, 2: B hi, 3: B lo}]
+};
+
+struct TcArgs {
+    int Mr, Nr, K;  // A rows, B rows, reduction length
+    int* err;       // device error flag (bounded waits)
+    // NG == 1 epilogue
+    const float* sa;
+    const float* sb;
+    float* C;
+    int64_t ldc;
+    int accumulate;
+    // NG == 2 (Wald) epilogue
+    const float* sa2;
+    const float* sb2;
+    const float* rWr;
+    int n_real;
+    float var_df;
+    const int64_t* rows;
+    double* f;
+    double* beta;
+    double* se;
+    double* sfve;
+    int64_t ldo;
+    double* max_F;
+};
+
+template <int NG, int BK>
+__global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMaps maps, const TcArgs args) {
+    using C = Cfg<NG, BK>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kStageBytes);
+    uint64_t* full = bars;                  // [kStages]
+    uint64_t* empty = bars + C::kStages;    // [kStages]
+    uint64_t* acc_full = bars + 2 * C::kStages;      // [2]
+    uint64_t* acc_empty = acc_full + 2;              // [2]
+    uint64_t* final_bar = acc_empty + 2;             // [1]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(final_bar + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_b = (args.Nr + kBN - 1) / kBN;
+    const int n_tiles = ((args.Mr + kBM - 1) / kBM) * tiles_b;
+    const int n_kb = (args.K + BK - 1) / BK;
+    constexpr uint32_t idesc = idesc_f16_f32(kBM, kBN);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 128);
+        }
+        mbar_init(final_bar, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0 && lane == 0) {
+        for (int i = 0; i < NG * 4; ++i) tma_prefetch_desc(&maps.m[i]);
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, C::kTmemCols);
+        tmem_relinquish();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ---- TMA producer ----
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool armed[C::kStages] = {};
+            uint32_t armed_phase[C::kStages] = {};
+            bool ok = true;
+            for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+                const int ta = t / tiles_b, tb = t % tiles_b;
+                for (int kb = 0; kb < n_kb; ++kb) {
+                    if (!mbar_wait(&empty[stage], phase ^ 1u, args.err, 1)) { ok = false; break; }
+                    mbar_arrive_expect_tx(&full[stage], C::kStageBytes);
+                    armed[stage] = true;
+                    armed_phase[stage] = phase;
+                    uint8_t* base = smem + stage * C::kStageBytes;
+#pragma unroll
+                    for (int g = 0; g < NG; ++g) {
+                        tma_load_2d(base + (g * 4 + 0) * C::kTileBytes, &maps.m[g * 4 + 0], kb * BK, ta * kBM, &full[stage]);
+                        tma_load_2d(base + (g * 4 + 1) * C::kTileBytes, &maps.m[g * 4 + 1], kb * BK, ta * kBM, &full[stage]);
+                        tma_load_2d(base + (g * 4 + 2) * C::kTileBytes, &maps.m[g * 4 + 2], kb * BK, tb * kBN, &full[stage]);
+                        tma_load_2d(base + (g * 4 + 3) * C::kTileBytes, &maps.m[g * 4 + 3], kb * BK, tb * kBN, &full[stage]);
+                    }
+                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                }
+            }
+            // never leave the CTA with copies still landing in shared memory
+            for (int s = 0; s < C::kStages; ++s)
+                if (armed[s]) mbar_drain(&full[s], armed_phase[s]);
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int ab = 0;
+            uint32_t aphase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+                if (!mbar_wait(&acc_empty[ab], aphase ^ 1u, args.err, 2)) break;
+                fence_after_sync();
+                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * NG * kBN);
+                for (int kb = 0; kb < n_kb; ++kb) {
+                    if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                    fence_after_sync();
+                    const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+#pragma unroll
+                        for (int g = 0; g < NG; ++g) {
+                            const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
+                            const uint32_t tg = sbase + static_cast<uint32_t>(g * 4 * C::kTileBytes);
+                            const uint64_t ah = smem_desc(tg + 0 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t al = smem_desc(tg + 1 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bh = smem_desc(tg + 2 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bl = smem_desc(tg + 3 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            mma_f16(d, ah, bh, idesc, (kb | kk) ? 1u : 0u);
+                            mma_f16(d, ah, bl, idesc, 1u);
+                            mma_f16(d, al, bh, idesc, 1u);
+                        }
+                    }
+                    mma_commit(&empty[stage]);
+                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                }
+                if (!ok) break;
+                mma_commit(&acc_full[ab]);
+                if (++ab == 2) { ab = 0; aphase ^= 1u; }
+            }
+            // every MMA this thread issued has completed before tensor memory is released
+            mma_commit(final_bar);
+            mbar_drain(final_bar, 0);
+        }
+    } else {
+        // ---- epilogue: warps 2..5, thread = one accumulator row ----
+        const int q = warp & 3;
+        const int r = q * 32 + lane;
+        int ab = 0;
+        uint32_t aphase = 0;
+        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+            const int ta = t / tiles_b, tb = t % tiles_b;
+            if (!mbar_wait(&acc_full[ab], aphase, args.err, 4)) break;
+            fence_after_sync();
+            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
+            const int i = ta * kBM + r;  // A row
+            const bool row_ok = i < args.Mr;
+            if constexpr (NG == 1) {
+                const float sa = row_ok ? args.sa[i] : 0.0f;
+                for (int c0 = 0; c0 < kBN; c0 += 16) {
+                    float v[16];
+                    tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
+                    if (!row_ok) continue;
+                    float* crow = args.C + static_cast<int64_t>(i) * args.ldc;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int col = tb * kBN + c0 + j;
+                        if (col < args.Nr) {
+                            const float x = v[j] * sa * args.sb[col];
+                            crow[col] = args.accumulate ? crow[col] + x : x;
+                        }
+                    }
+                }
+            } else {
+                // Wald statistics, the reference's formulas (fasterlmm/core.py:651-667) in FP32 on unscaled sums
+                const int p = i;
+                const float sa1 = row_ok ? args.sa[p] : 0.0f;
+                const float sa2 = row_ok ? args.sa2[p] : 0.0f;
+                const float rwr = row_ok ? args.rWr[p] : 1.0f;
+                const bool real = row_ok && p < args.n_real;
+                float colmax = -INFINITY;
+                bool col_nan = false;
+                for (int c0 = 0; c0 < kBN; c0 += 16) {
+                    float vy[16], vs[16];
+                    tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
+                    if (!row_ok) continue;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int m = tb * kBN + c0 + j;
+                        if (m >= args.Nr) continue;
+                        const float swy = vy[j] * sa1 * args.sb[m];
+                        const float denom = fmaxf(vs[j] * sa2 * args.sb2[m], 1e-30f);
+                        const float inv_d = 1.0f / denom;
+                        const float b = swy * inv_d;
+                        const float qq = swy * swy;
+                        const float rss = fmaxf(rwr - qq * inv_d, 1e-30f);
+                        const float var_b = rss / args.var_df * inv_d;
+                        const float F = b * b / var_b;
+                        colmax = fmaxf(colmax, F);
+                        col_nan |= isnan(F);
+                        if (real) {
+                            const int64_t o = args.rows[m] * args.ldo + p;
+                            args.f[o] = F;
+                            args.beta[o] = b;
+                            args.se[o] = sqrtf(var_b);
+                            args.sfve[o] = sqrtf(fmaxf(qq * inv_d / rwr, 0.0f));
+                        }
+                    }
+                }
+                if (row_ok && (colmax >= 0.0f || col_nan)) atomic_max_nonneg(args.max_F + p, col_nan ? NAN : (double)colmax);
+            }
+            fence_before_sync();
+            mbar_arrive(&acc_empty[ab]);
+            if (++ab == 2) { ab = 0; aphase ^= 1u; }
+        }
+    }
+
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after_sync();
+        tmem_dealloc(tmem_base, C::kTmemCols);
+    }
+}
+
+// ---- operand preparation ---------------------------------------------------------------------------------------
+
+__device__ __forceinline__ float row_scale_exp(float amax, int* e_out) {
+    // exponent e with amax * 2^e in [2^14, 2^15); rows of zeros keep e = 0
+    int e = 0;
+    if (amax > 0.0f && isfinite(amax)) {
+        int ex;
+        frexpf(amax, &ex);  // amax = m 2^ex, m in [0.5, 1)
+        e = 15 - ex;
+    }
+    *e_out = e;
+    return ldexpf(1.0f, e);
+}
+
+__device__ __forceinline__ void split_store(float x, float mul, __half* hi, __half* lo, int64_t o) {
+    const float xs = x * mul;  // exact: power-of-two scale
+    const __half h = __float2half_rn(xs);
+    hi[o] = h;
+    lo[o] = __float2half_rn(xs - __half2float(h));
+}
+
+template <typename T>
+__global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __restrict__ hi,
+                             __half* __restrict__ lo, int64_t ldo, float* __restrict__ scale) {
+    __shared__ float red[32];
+    const int64_t r = blockIdx.x;
+    if (r >= rows) return;
+    const T* x = X + r * ldx;
+    float amax = 0.0f;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = amax;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) red[0] = v;
+    }
+    __syncthreads();
+    int e;
+    const float mul = row_scale_exp(red[0], &e);
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        // FP64 inputs are rounded to FP32 before the split only after scaling, so the split keeps 22 bits
+        const double xd = static_cast<double>(x[k]) * static_cast<double>(mul);
+        const __half h = __double2half(xd);
+        hi[r * ldo + k] = h;
+        lo[r * ldo + k] = __double2half(xd - static_cast<double>(__half2float(h)));
+    }
+    if (threadIdx.x == 0) scale[r] = ldexpf(1.0f, -e);
+}
+
+// Wald column side (fasterlmm/core.py:639-643): w = 1 / (s + delta_p), A1 = w UY, A2 = w, rWr = sum w UY^2 (FP64
+// accumulation), each row split with its own exponent.  One warp per column p.
+__global__ void k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __restrict__ UYt,
+                                    int64_t ldu, const double* __restrict__ ld, int P, __half* __restrict__ A1h,
+                                    __half* __restrict__ A1l, __half* __restrict__ A2h, __half* __restrict__ A2l,
+                                    int64_t lda, float* __restrict__ sa1, float* __restrict__ sa2,
+                                    float* __restrict__ rWr) {
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    if (p >= P) return;
+    const float delta = static_cast<float>(exp(ld[p]));
+    const float* u = UYt + p * ldu;
+    float m1 = 0.0f, m2 = 0.0f;
+    double acc = 0.0;
+    for (int n = lane; n < Neff; n += 32) {
+        const float w = 1.0f / (s32[n] + delta);
+        const float a = w * u[n];
+        m1 = fmaxf(m1, fabsf(a));
+        m2 = fmaxf(m2, w);
+        acc += static_cast<double>(a) * static_cast<double>(u[n]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+        m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    }
+    acc = warp_sum(acc);
+    int e1, e2;
+    const float mul1 = row_scale_exp(m1, &e1), mul2 = row_scale_exp(m2, &e2);
+    for (int n = lane; n < Neff; n += 32) {
+        const float w = 1.0f / (s32[n] + delta);
+        split_store(w * u[n], mul1, A1h, A1l, p * lda + n);
+        split_store(w, mul2, A2h, A2l, p * lda + n);
+    }
+    if (lane == 0) {
+        sa1[p] = ldexpf(1.0f, -e1);
+        sa2[p] = ldexpf(1.0f, -e2);
+        rWr[p] = static_cast<float>(fmax(acc, 1e-300));
+    }
+}
+
+// Wald variant side: B1 = US, B2 = US o US, each row split.  One warp per variant m.
+__global__ void k_wald_prep_variants(const float* __restrict__ USt, int64_t ldus, int Mc, int Neff,
+                                     __half* __restrict__ B1h, __half* __restrict__ B1l, __half* __restrict__ B2h,
+                                     __half* __restrict__ B2l, int64_t ldb, float* __restrict__ sb1,
+                                     float* __restrict__ sb2) {
+    const int lane = threadIdx.x & 31;
+    const int64_t m = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    if (m >= Mc) return;
+    const float* u = USt + m * ldus;
+    float m1 = 0.0f;
+    for (int n = lane; n < Neff; n += 32) m1 = fmaxf(m1, fabsf(u[n]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    int e1, e2;
+    const float mul1 = row_scale_exp(m1, &e1), mul2 = row_scale_exp(m1 * m1, &e2);
+    for (int n = lane; n < Neff; n += 32) {
+        const float x = u[n];
+        split_store(x, mul1, B1h, B1l, m * ldb + n);
+        split_store(x * x, mul2, B2h, B2l, m * ldb + n);
+    }
+    if (lane == 0) {
+        sb1[m] = ldexpf(1.0f, -e1);
+        sb2[m] = ldexpf(1.0f, -e2);
+    }
+}
+
+// ---- host side: TMA descriptors and launches ---------------------------------------------------------------
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+int encode_fn(PFN_cuTensorMapEncodeTiled_v12000* out) {
+    std::call_once(g_encode_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    if (!g_encode) return fail(FLMM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    *out = g_encode;
+    return FLMM_OK;
+}
+
+// FP16 matrix (rows, K) with row pitch ld elements -> tiled map with box {BK, 128} and the matching swizzle.
+int make_map(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc;
+    int rc = encode_fn(&enc);
+    if (rc) return rc;
+    if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (ld * 2) % 16 != 0)
+        return fail(FLMM_ERR_ARG, "split operand must be 16-byte aligned with a row pitch that is a multiple of 8");
+    cuuint64_t gdim[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
+    cuuint64_t gstride[1] = {static_cast<cuuint64_t>(ld * 2)};
+    cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), 128u};
+    cuuint32_t estride[2] = {1u, 1u};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), gdim, gstride, box, estride,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     BK == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(FLMM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(r));
+    return FLMM_OK;
+}
+
+template <int NG, int BK>
+int launch_tc(const TcMaps& maps, const TcArgs& args, int sm_count, cudaStream_t st) {
+    using C = Cfg<NG, BK>;
+    FLMM_CUDA(cudaFuncSetAttribute(k_tc<NG, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmemBytes));
+    const int tiles = ((args.Mr + kBM - 1) / kBM) * ((args.Nr + kBN - 1) / kBN);
+    if (tiles == 0 || args.K <= 0) return FLMM_OK;
+    const int grid = tiles < sm_count ? tiles : sm_count;
+    k_tc<NG, BK><<<grid, kThreads, C::kSmemBytes, st>>>(maps, args);
+    return check_launch(NG == 1 ? "k_tc<gemm>" : "k_tc<wald>");
+}
+
+}  // namespace
+
+// ---- C ABI -----------------------------------------------------------------------------------------------------
+
+int flmm_ctx_sm_count(flmm_context* ctx);
+int* flmm_ctx_err_flag(flmm_context* ctx);
+
+extern "C" int flmm_split_rows_f16(const void* X, int x_is_f64, int64_t ldx, int rows, int K, void* hi, void* lo,
+                                   int64_t ldo, float* scale, void* stream) {
+    FLMM_REQUIRE(X && hi && lo && scale && rows >= 0 && K > 0 && ldx >= K && ldo >= K,
+                 "flmm_split_rows_f16: bad arguments");
+    if (rows == 0) return FLMM_OK;
+    cudaStream_t st = as_stream(stream);
+    if (x_is_f64)
+        k_split_rows<double><<<rows, 256, 0, st>>>(static_cast<const double*>(X), ldx, rows, K,
+                                                    static_cast<__half*>(hi), static_cast<__half*>(lo), ldo, scale);
+    else
+        k_split_rows<float><<<rows, 256, 0, st>>>(static_cast<const float*>(X), ldx, rows, K,
+                                                   static_cast<__half*>(hi), static_cast<__half*>(lo), ldo, scale);
+    return check_launch("k_split_rows");
+}
+
+extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void* Al, const float* sa, int64_t lda,
+                                   int Mr, const void* Bh, const void* Bl, const float* sb, int64_t ldb, int Nr, int K,
+                                   float* Cout, int64_t ldc, int accumulate, void* stream) {
+    FLMM_REQUIRE(ctx && Ah && Al && sa && Bh && Bl && sb && Cout && Mr >= 0 && Nr >= 0 && K > 0 && lda >= K &&
+                     ldb >= K && ldc >= Nr,
+                 "flmm_gemm_split_f16: bad arguments");
+    if (Mr == 0 || Nr == 0) return FLMM_OK;
+    TcMaps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    int rc;
+    if ((rc = make_map(&maps.m[0], Ah, Mr, K, lda, 64))) return rc;
+    if ((rc = make_map(&maps.m[1], Al, Mr, K, lda, 64))) return rc;
+    if ((rc = make_map(&maps.m[2], Bh, Nr, K, ldb, 64))) return rc;
+    if ((rc = make_map(&maps.m[3], Bl, Nr, K, ldb, 64))) return rc;
+    TcArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.Mr = Mr;
+    a.Nr = Nr;
+    a.K = K;
+    a.err = flmm_ctx_err_flag(ctx);
+    a.sa = sa;
+    a.sb = sb;
+    a.C = Cout;
+    a.ldc = ldc;
+    a.accumulate = accumulate;
+    return launch_tc<1, 64>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+}
+
+extern "C" int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu,
+                                            const double* log_delta, int P, void* A1h, void* A1l, void* A2h,
+                                            void* A2l, int64_t lda, float* sa1, float* sa2, float* rWr,
+                                            void* stream) {
+    FLMM_REQUIRE(s32 && UYt && log_delta && A1h && A1l && A2h && A2l && sa1 && sa2 && rWr && Neff > 0 &&
+                     ldu >= Neff && lda >= Neff && P >= 0,
+                 "flmm_wald_split_prep_columns: bad arguments");
+    if (P == 0) return FLMM_OK;
+    k_wald_prep_columns<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, as_stream(stream)>>>(
+        s32, Neff, UYt, ldu, log_delta, P, static_cast<__half*>(A1h), static_cast<__half*>(A1l),
+        static_cast<__half*>(A2h), static_cast<__half*>(A2l), lda, sa1, sa2, rWr);
+    return check_launch("k_wald_prep_columns");
+}
+
+extern "C" int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Neff, void* B1h, void* B1l,
+                                             void* B2h, void* B2l, int64_t ldb, float* sb1, float* sb2,
+                                             void* stream) {
+    FLMM_REQUIRE(USt && B1h && B1l && B2h && B2l && sb1 && sb2 && Neff > 0 && ldus >= Neff && ldb >= Neff && Mc >= 0,
+                 "flmm_wald_split_prep_variants: bad arguments");
+    if (Mc == 0) return FLMM_OK;
+    k_wald_prep_variants<<<ceil_div(static_cast<int64_t>(Mc) * 32, 256), 256, 0, as_stream(stream)>>>(
+        USt, ldus, Mc, Neff, static_cast<__half*>(B1h), static_cast<__half*>(B1l), static_cast<__half*>(B2h),
+        static_cast<__half*>(B2l), ldb, sb1, sb2);
+    return check_launch("k_wald_prep_variants");
+}
+
+extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, const void* A2h,
+                                   const void* A2l, int64_t lda, const float* sa1, const float* sa2, const float* rWr,
+                                   int P, int n_real, const void* B1h, const void* B1l, const void* B2h,
+                                   const void* B2l, int64_t ldb, const float* sb1, const float* sb2, int Mc, int Neff,
+                                   const int64_t* rows, double* f, double* beta, double* se, double* sfve, int64_t ldo,
+                                   double* max_F, void* stream) {
+    FLMM_REQUIRE(ctx && A1h && A1l && A2h && A2l && sa1 && sa2 && rWr && B1h && B1l && B2h && B2l && sb1 && sb2 &&
+                     max_F && Neff > 1 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
+                     ldb >= Neff,
+                 "flmm_wald_split_f16: bad arguments");
+    FLMM_REQUIRE(n_real == 0 || Mc == 0 || (rows && f && beta && se && sfve && ldo >= n_real),
+                 "flmm_wald_split_f16: real-column outputs missing");
+    if (P == 0 || Mc == 0) return FLMM_OK;
+    TcMaps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    const void* srcs[8] = {A1h, A1l, B1h, B1l, A2h, A2l, B2h, B2l};
+    for (int i = 0; i < 8; ++i) {
+        const bool a_side = (i % 4) < 2;
+        int rc = make_map(&maps.m[i], srcs[i], a_side ? P : Mc, Neff, a_side ? lda : ldb, 32);
+        if (rc) return rc;
+    }
+    TcArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.Mr = P;
+    a.Nr = Mc;
+    a.K = Neff;
+    a.err = flmm_ctx_err_flag(ctx);
+    a.sa = sa1;
+    a.sb = sb1;
+    a.sa2 = sa2;
+    a.sb2 = sb2;
+    a.rWr = rWr;
+    a.n_real = n_real;
+    a.var_df = static_cast<float>(Neff - 1);
+    a.rows = rows;
+    a.f = f;
+    a.beta = beta;
+    a.se = se;
+    a.sfve = sfve;
+    a.ldo = ldo;
+    a.max_F = max_F;
+    return launch_tc<2, 32>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+}

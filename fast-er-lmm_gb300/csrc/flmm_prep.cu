@@ -389,3 +389,45 @@ extern "C" int flmm_pack_perm_columns(const double* Yt_real, int64_t ldy, int B,
     k_pack_perms<<<ceil_div(total, 256), 256, 0, as_stream(stream)>>>(Yt_real, ldy, B, N, orders, n_perm, Yt_all, lda);
     return check_launch("k_pack_perms");
 }
+
+namespace {
+
+__global__ void k_f64_to_f32(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
+    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t < n) y[t] = static_cast<float>(x[t]);
+}
+
+__global__ void k_acc_f32_f64(int64_t n, const float* __restrict__ x, double* __restrict__ y) {
+    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t < n) y[t] += static_cast<double>(x[t]);
+}
+
+__global__ void k_loco_kinship_f32(const double* __restrict__ Gtot, const float* __restrict__ Gc, int64_t nn,
+                                   double m_loco, double* __restrict__ K) {
+    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t < nn) K[t] = (Gtot[t] - (Gc ? static_cast<double>(Gc[t]) : 0.0)) / m_loco;
+}
+
+}  // namespace
+
+extern "C" int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream) {
+    FLMM_REQUIRE((x && y) || n == 0, "flmm_convert_f64_f32: NULL argument");
+    if (n == 0) return FLMM_OK;
+    k_f64_to_f32<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(n, x, y);
+    return check_launch("k_f64_to_f32");
+}
+
+extern "C" int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream) {
+    FLMM_REQUIRE((x && y) || n == 0, "flmm_accumulate_f32_f64: NULL argument");
+    if (n == 0) return FLMM_OK;
+    k_acc_f32_f64<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(n, x, y);
+    return check_launch("k_acc_f32_f64");
+}
+
+extern "C" int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K,
+                                     void* stream) {
+    FLMM_REQUIRE(Gtot && K && N > 0 && m_loco > 0, "flmm_loco_kinship_f32: bad arguments");
+    const int64_t nn = static_cast<int64_t>(N) * N;
+    k_loco_kinship_f32<<<ceil_div(nn, 256), 256, 0, as_stream(stream)>>>(Gtot, Gc, nn, m_loco, K);
+    return check_launch("k_loco_kinship_f32");
+}

@@ -46,10 +46,23 @@ SIGNATURES: dict[str, list] = {
     "flmm_wald_f64_workspace_bytes": [_i, _i, _psz],
     "flmm_wald_f64": [_p, _i, _p, _i64, _p, _i, _i, _p, _i64, _i, _p, _p, _p, _p, _p, _i64, _p, _p, _sz, _p],
     "flmm_axpy_f64": [_i64, _d, _p, _p, _p],
+    "flmm_perm_orders": [_p, _i, C.c_uint64, _i, _i, _p, _p],
     "flmm_pack_perm_columns": [_p, _i64, _i, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_context_check": [_p, _p],
+    "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
+    "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],
+    "flmm_fit_delta_fast_workspace_bytes": [_i, _i, _psz],
+    "flmm_fit_delta_fast": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
+    "flmm_wald_split_prep_columns": [_p, _i, _p, _i64, _p, _i, _p, _p, _p, _p, _i64, _p, _p, _p, _p],
+    "flmm_wald_split_prep_variants": [_p, _i64, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _p],
+    "flmm_wald_split_f16": [_p, _p, _p, _p, _p, _i64, _p, _p, _p, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _i, _i, _p,
+                            _p, _p, _p, _p, _i64, _p, _p],
+    "flmm_convert_f64_f32": [_i64, _p, _p, _p],
+    "flmm_accumulate_f32_f64": [_i64, _p, _p, _p],
+    "flmm_loco_kinship_f32": [_p, _p, _i, _d, _p, _p],
 }
 _RESTYPE = {"flmm_status_string": C.c_char_p, "flmm_last_error": C.c_char_p, "flmm_kernel_launches": C.c_uint64}
 

@@ -356,7 +356,7 @@ def _take_rows(Zt: Tensor, blk) -> Tensor:
 def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int, on_chrom=None,
            Zt_kin: Tensor | None = None, chrom_kin: np.ndarray | None = None, loco: bool = True, n_grid: int = 64,
            log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
-           form: str = "plain") -> ScanResult:
+           form: str = "plain", timers: dict | None = None) -> ScanResult:
     """
     Core engine on device tensors: Zt (M, N) standardised tested variants, X (N, D), Yt (P, N) columns, chromosome
     labels (M,).  The kinship Gram of every chromosome is computed once and each LOCO kinship is the total minus
@@ -366,7 +366,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         from . import fast
         return fast.scan_t(Zt, X, Yt, chrom, n_real=n_real, on_chrom=on_chrom, Zt_kin=Zt_kin, chrom_kin=chrom_kin,
                            loco=loco, n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max,
-                           refine=refine)
+                           refine=refine, timers=timers)
     if form != "plain":
         raise ValueError(f"unknown form {form!r} (expected 'plain' or 'fast')")
     dev = Zt.device

@@ -1,0 +1,251 @@
+"""
+Split-precision ("fast") form of the LOCO scan engine.
+
+Same algorithm and outputs as the plain form (fasterlmm_gb300.core.scan_t), with the O(N^2 M), O(N Neff P) and
+O(Neff P M) products on the tensor cores:
+
+* the kinship Gram of each chromosome, the rotations UY = U_eff^T Y_r and US = U_eff^T S_r, and the Wald sums
+  sWy / sWs are split-FP16 tcgen05 products (three MMAs per product, FP32 accumulation, ~21-bit operands);
+* the delta fit is an FP32 grid plus a Newton solve of d loss / d log delta = 0 in the reference's bracket;
+* the kinship eigendecomposition, the covariate SVD and the projection of K + I stay FP64.
+
+Device layouts: tested variants are grouped by chromosome (a stable reorder, undone by the output row map), so every
+chromosome is one contiguous row block of the split variant matrix; the kinship panel is also kept sample-major
+with each chromosome's columns starting on a 64-column boundary, so the Gram of a chromosome is one K range.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+from torch import Tensor
+
+from . import _lib
+from .core import F64, CovariateBasis, ScanResult, _alloc_outputs, _ptr, _stream, _work, compat_eigh
+
+F16 = torch.float16
+F32 = torch.float32
+
+
+def _pad(k: int, m: int = 8) -> int:
+    return (k + m - 1) // m * m
+
+
+class SplitRows:
+    """hi / lo FP16 pair of a row-major matrix with one power-of-two scale per row: x ~= (hi + lo) * scale."""
+
+    def __init__(self, rows: int, K: int, dev: torch.device, ld: int | None = None):
+        self.rows, self.K = rows, K
+        self.ld = ld or _pad(K)
+        self.hi = torch.empty((rows, self.ld), dtype=F16, device=dev)
+        self.lo = torch.empty((rows, self.ld), dtype=F16, device=dev)
+        self.scale = torch.empty(rows, dtype=F32, device=dev)
+
+    @classmethod
+    def of(cls, X: Tensor) -> "SplitRows":
+        rows, K = X.shape
+        out = cls(rows, K, X.device)
+        if rows:
+            _lib.call("flmm_split_rows_f16", _ptr(X), int(X.dtype == F64), X.stride(0), rows, K, _ptr(out.hi),
+                      _ptr(out.lo), out.ld, _ptr(out.scale), _stream(X.device))
+        return out
+
+    def view(self, r0: int = 0, rows: int | None = None, k0: int = 0, K: int | None = None) -> "SplitView":
+        """A row range and K range of the pair, as raw pointers for the C ABI (keeps the buffers alive)."""
+        rows = self.rows - r0 if rows is None else rows
+        K = self.K - k0 if K is None else K
+        return SplitView(self, (_ptr(self.hi[r0:, k0:]), _ptr(self.lo[r0:, k0:]), _ptr(self.scale[r0:]), self.ld,
+                                rows, K))
+
+
+class SplitView(tuple):
+    """(hi, lo, scale, ld, rows, K) pointers of a SplitRows range; holds the owning SplitRows so that the device
+    buffers outlive every launch that reads them."""
+
+    def __new__(cls, owner: SplitRows, fields: tuple):
+        obj = super().__new__(cls, fields)
+        obj.owner = owner
+        return obj
+
+
+def gemm_split(ctx, A: SplitView, B: SplitView, C: Tensor, accumulate: bool = False) -> None:
+    """C (Mr, Nr) FP32 = A B^T for split views A, B (from SplitRows.view) with equal K."""
+    ah, al, sa, lda, Mr, K = A
+    bh, bl, sb, ldb, Nr, Kb = B
+    assert K == Kb
+    _lib.call("flmm_gemm_split_f16", ctx, ah, al, sa, lda, Mr, bh, bl, sb, ldb, Nr, K, _ptr(C), C.stride(0),
+              int(accumulate), _stream(C.device))
+
+
+def fit_delta_fast(s: Tensor, UYt: Tensor, *, n_grid: int = 64, log_delta_min: float = -10.0,
+                   log_delta_max: float = 10.0, refine: bool = True) -> tuple[Tensor, Tensor]:
+    dev = s.device
+    Neff = s.shape[0]
+    P = UYt.shape[0]
+    ld = torch.empty(P, dtype=F64, device=dev)
+    idx = torch.empty(P, dtype=torch.int32, device=dev)
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_fit_delta_fast_workspace_bytes", Neff, n_grid))
+    _lib.call("flmm_fit_delta_fast", _ptr(s), Neff, _ptr(UYt), UYt.stride(0), P, n_grid, float(log_delta_min),
+              float(log_delta_max), int(bool(refine)), _ptr(ld), _ptr(idx), w, wb, _stream(dev))
+    return ld, idx
+
+
+def _chrom_order(chrom: np.ndarray) -> tuple[np.ndarray | None, list]:
+    """Stable grouping by chromosome: (order or None if already grouped, [(c, start, count)] in sorted c)."""
+    chrom = np.asarray(chrom)
+    order = np.argsort(chrom, kind="stable")
+    grouped = chrom[order]
+    cs, starts, counts = np.unique(grouped, return_index=True, return_counts=True)
+    blocks = [(c.item(), int(a), int(n)) for c, a, n in zip(cs, starts, counts)]
+    return (None if np.array_equal(order, np.arange(chrom.size)) else order), blocks
+
+
+class KinshipPanel:
+    """Sample-major split of a standardised panel with 64-aligned chromosome column blocks, and its Grams."""
+
+    def __init__(self, Zt: Tensor, chrom: np.ndarray, ctx):
+        dev = Zt.device
+        M, N = Zt.shape
+        order, blocks = _chrom_order(chrom)
+        offs, off = [], 0
+        for _, _, n in blocks:
+            offs.append(off)
+            off += _pad(n, 64)
+        Mpad = max(off, 64)
+        Zg = torch.zeros((N, Mpad), dtype=F64, device=dev)
+        st = _stream(dev)
+        src = Zt if order is None else Zt.index_select(0, torch.from_numpy(order).to(dev))
+        for (c, a, n), o in zip(blocks, offs):
+            if n:
+                _lib.call("flmm_transpose_f64", _ptr(src[a:a + n]), N, n, N, _ptr(Zg[:, o:]), Mpad, st)
+        del src
+        self.split = SplitRows.of(Zg)
+        del Zg
+        self.M = M
+        self.counts = {c: n for (c, _, n) in blocks}
+        self.grams: dict = {}
+        self.Gtot = torch.zeros((N, N), dtype=F64, device=dev)
+        for (c, a, n), o in zip(blocks, offs):
+            G = torch.empty((N, N), dtype=F32, device=dev)
+            v = self.split.view(0, N, o, n)
+            gemm_split(ctx, v, v, G)
+            self.grams[c] = G
+            _lib.call("flmm_accumulate_f32_f64", N * N, _ptr(G), _ptr(self.Gtot), st)
+
+    def kinship(self, c) -> Tensor:
+        """LOCO kinship without chromosome c (c = None: all chromosomes)."""
+        N = self.Gtot.shape[0]
+        K = torch.empty((N, N), dtype=F64, device=self.Gtot.device)
+        Gc = self.grams.get(c) if c is not None else None
+        m = self.M - (self.counts.get(c, 0) if c is not None else 0)
+        _lib.call("flmm_loco_kinship_f32", _ptr(self.Gtot), _ptr(Gc), N, float(m), _ptr(K), _stream(K.device))
+        return K
+
+
+class WaldOperands:
+    """Split operand buffers of the fused Wald kernel, reused across chromosomes (grow-only)."""
+
+    def __init__(self, dev: torch.device):
+        self.dev = dev
+        self.cols = None
+        self.vars = None
+
+    def _cols(self, P: int, ld: int):
+        if self.cols is None or self.cols[0].shape[0] < P or self.cols[0].shape[1] != ld:
+            self.cols = [torch.empty((P, ld), dtype=F16, device=self.dev) for _ in range(4)] + \
+                        [torch.empty(P, dtype=F32, device=self.dev) for _ in range(3)]
+        return self.cols
+
+    def _vars(self, Mc: int, ld: int):
+        if self.vars is None or self.vars[0].shape[0] < Mc or self.vars[0].shape[1] != ld:
+            self.vars = [torch.empty((Mc, ld), dtype=F16, device=self.dev) for _ in range(4)] + \
+                        [torch.empty(Mc, dtype=F32, device=self.dev) for _ in range(2)]
+        return self.vars
+
+
+def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: Tensor, n_real: int, rows: Tensor,
+              out: dict, max_F: Tensor, mark=None, done=None) -> None:
+    dev = s.device
+    st = _stream(dev)
+    Neff = s.shape[0]
+    P = UYt.shape[0]
+    Mc = USt.shape[0]
+    ldk = _pad(Neff)
+    s32 = torch.empty(Neff, dtype=F32, device=dev)
+    _lib.call("flmm_convert_f64_f32", Neff, _ptr(s), _ptr(s32), st)
+    A1h, A1l, A2h, A2l, sa1, sa2, rWr = ops._cols(P, ldk)
+    _lib.call("flmm_wald_split_prep_columns", _ptr(s32), Neff, _ptr(UYt), UYt.stride(0), _ptr(ld), P, _ptr(A1h),
+              _ptr(A1l), _ptr(A2h), _ptr(A2l), ldk, _ptr(sa1), _ptr(sa2), _ptr(rWr), st)
+    B1h, B1l, B2h, B2l, sb1, sb2 = ops._vars(Mc, ldk)
+    _lib.call("flmm_wald_split_prep_variants", _ptr(USt), USt.stride(0), Mc, Neff, _ptr(B1h), _ptr(B1l), _ptr(B2h),
+              _ptr(B2l), ldk, _ptr(sb1), _ptr(sb2), st)
+    slot = mark("wald") if mark else None
+    _lib.call("flmm_wald_split_f16", ctx, _ptr(A1h), _ptr(A1l), _ptr(A2h), _ptr(A2l), ldk, _ptr(sa1), _ptr(sa2),
+              _ptr(rWr), P, n_real, _ptr(B1h), _ptr(B1l), _ptr(B2h), _ptr(B2l), ldk, _ptr(sb1), _ptr(sb2), Mc, Neff,
+              _ptr(rows), _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]), _ptr(out["sfve"]), n_real,
+              _ptr(max_F), st)
+    if done:
+        done(slot)
+    _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, st)
+
+
+def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int, on_chrom=None,
+           Zt_kin: Tensor | None = None, chrom_kin: np.ndarray | None = None, loco: bool = True, n_grid: int = 64,
+           log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
+           timers: dict | None = None) -> ScanResult:
+    """
+    Fast-form engine on device tensors (same contract as fasterlmm_gb300.core.scan_t).  ``timers``, if given, maps
+    a stage name to a list that receives (start, end) CUDA event pairs recorded around that stage.
+    """
+    dev = Zt.device
+    ctx = _lib.context(dev.index)
+    st = _stream(dev)
+    M, N = Zt.shape
+    P = Yt.shape[0]
+
+    def mark(name):
+        if timers is None:
+            return None
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        timers.setdefault(name, []).append([ev, None])
+        return timers[name][-1]
+
+    def done(slot):
+        if slot is not None:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            slot[1] = ev
+
+    out, max_F = _alloc_outputs(M, n_real, P, dev)
+    basis = CovariateBasis(X)
+    Ys = SplitRows.of(basis.regress_out(Yt))
+    order, blocks = _chrom_order(chrom)
+    order_t = None if order is None else torch.from_numpy(order).to(dev)
+    Zs = SplitRows.of(Zt if order_t is None else Zt.index_select(0, order_t))
+    row_map = torch.arange(M, dtype=torch.int64, device=dev) if order_t is None else order_t.to(torch.int64)
+
+    kin = KinshipPanel(Zt if Zt_kin is None else Zt_kin, np.asarray(chrom if Zt_kin is None else chrom_kin), ctx)
+    units = [(c, a, n) for (c, a, n) in blocks] if loco else [(None, 0, M)]
+    ops = WaldOperands(dev)
+    log_deltas = {}
+    D = X.shape[1]
+    Neff = N - D
+    ldk = _pad(Neff)
+    UYt = torch.empty((P, ldk), dtype=F32, device=dev)
+    for k_idx, (c, a, n) in enumerate(units):
+        K = kin.kinship(c)
+        s, Ut = compat_eigh(K, basis)
+        Us = SplitRows.of(Ut)
+        gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
+        ld, _ = fit_delta_fast(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
+                               log_delta_max=log_delta_max, refine=refine)
+        USt = torch.empty((n, ldk), dtype=F32, device=dev)
+        gemm_split(ctx, Zs.view(a, n), Us.view(), USt[:, :Neff])
+        wald_fast(ctx, ops, s, UYt[:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,
+                  mark=mark, done=done)
+        log_deltas[c if c is not None else 0] = ld
+        if on_chrom is not None:
+            on_chrom(k_idx + 1, len(units))
+    _lib.call("flmm_context_check", ctx, st)
+    return ScanResult(max_F=max_F, log_delta=log_deltas, **out)

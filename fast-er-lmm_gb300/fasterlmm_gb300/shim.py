@@ -1,0 +1,74 @@
+"""
+Install this package's GPU scan under an existing ``fasterlmm`` (FaST-ER-LMM) installation.
+
+``install()`` rebinds, in the reference's own modules, the names its callers look up at call time:
+``fasterlmm.core.{loco_scan_compat, single_k_scan_compat, fastlmm_compat_rotate, fit_delta_grid_compat,
+snp_wald_scan_compat}``, the copies ``fasterlmm.perms`` imported by name (fasterlmm/perms.py:17), and
+``perm_threshold`` in ``fasterlmm.perms`` and in ``fasterlmm.cli`` when that module is loaded (it imports the
+function by name).  The CLI and any user code that goes through those names then runs on the GPU unchanged.
+``uninstall()`` restores the originals.
+"""
+from __future__ import annotations
+
+import functools
+import sys
+
+_saved: dict = {}
+
+_CORE_NAMES = ("loco_scan_compat", "single_k_scan_compat", "fastlmm_compat_rotate", "fit_delta_grid_compat",
+               "snp_wald_scan_compat")
+
+
+def _set(mod, name, value):
+    key = (mod.__name__, name)
+    if key not in _saved:
+        _saved[key] = getattr(mod, name)
+    setattr(mod, name, value)
+
+
+def install(form: str = "fast", modules: dict | None = None) -> list[str]:
+    """
+    Patch the reference's modules (imported from sys.modules, or given as ``modules`` = {"core": ..., "perms":
+    ..., "cli": ...}).  ``form`` picks the numeric form of the scan drivers.  Returns the patched qualified names.
+    """
+    from . import core, perms
+    mods = dict(modules or {})
+    if not mods:
+        import importlib
+        mods["core"] = importlib.import_module("fasterlmm.core")
+        mods["perms"] = importlib.import_module("fasterlmm.perms")
+        if "fasterlmm.cli" in sys.modules:
+            mods["cli"] = sys.modules["fasterlmm.cli"]
+    ours = {
+        "loco_scan_compat": functools.partial(core.loco_scan_compat, form=form),
+        "single_k_scan_compat": functools.partial(core.single_k_scan_compat, form=form),
+        "fastlmm_compat_rotate": core.fastlmm_compat_rotate,
+        "fit_delta_grid_compat": core.fit_delta_grid_compat,
+        "snp_wald_scan_compat": core.snp_wald_scan_compat,
+    }
+    patched = []
+    for name in _CORE_NAMES:
+        if hasattr(mods.get("core"), name):
+            _set(mods["core"], name, ours[name])
+            patched.append(f"{mods['core'].__name__}.{name}")
+    pt = functools.partial(perms.perm_threshold, form=form)
+    for key in ("perms", "cli"):
+        m = mods.get(key)
+        if m is None:
+            continue
+        for name in ("loco_scan_compat", "single_k_scan_compat"):
+            if hasattr(m, name):
+                _set(m, name, ours[name])
+                patched.append(f"{m.__name__}.{name}")
+        if hasattr(m, "perm_threshold"):
+            _set(m, "perm_threshold", pt)
+            patched.append(f"{m.__name__}.perm_threshold")
+    return patched
+
+
+def uninstall() -> None:
+    for (modname, name), value in list(_saved.items()):
+        mod = sys.modules.get(modname)
+        if mod is not None:
+            setattr(mod, name, value)
+    _saved.clear()

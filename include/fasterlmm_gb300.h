@@ -139,6 +139,12 @@ int flmm_wald_f64(const double* s, int Neff, const double* UYt, int64_t ldu, con
 /* y[i] += alpha * x[i], FP64 (sums the per-chromosome Grams into the all-variant Gram). */
 int flmm_axpy_f64(int64_t n, double alpha, const double* x, double* y, void* stream);
 
+/* Permutation row orders (fasterlmm/perms.py:51-55), bit-identical to the reference's numpy draw: for each of the B
+ * columns, PCG64 seeded by numpy's SeedSequence([seed, seed_cols[b]]), n_perm rows of N uniforms, argsort of each
+ * row.  orders (B, n_perm, N) int32, orders[(b n_perm + j) N + i] = row landing at position i.  N <= 16384. */
+int flmm_perm_orders(const int64_t* seed_cols, int B, uint64_t seed, int n_perm, int N, int32_t* orders,
+                     void* stream);
+
 /* Permutation packing (fasterlmm/perms.py:56-59): Yt_all (B + B n_perm, N) gets the B real columns Yt_real (B, N)
  * as its first rows, then for each real column b its n_perm shuffles, pheno-major: row B + b n_perm + j holds
  * Yt_real[b, orders[(b n_perm + j) N + n]] at sample n.  orders are 0-based row indices < N. */
@@ -158,6 +164,59 @@ int flmm_fill_f64(double* x, int64_t n, double value, void* stream);
  * evaluated in log space by the modified Lentz continued fraction, so large F gives a finite value where
  * scipy.stats.f.sf underflows to 0. */
 int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double* out, void* stream);
+
+/* ---- split-precision tensor-core form --------------------------------------------------------------------------
+ * Operands are FP16 pairs with one power-of-two exponent per row: x ~= (hi[k] + lo[k]) * scale[row].  Products of
+ * two split operands are hi*hi + hi*lo + lo*hi on the tensor cores (tcgen05.mma kind::f16) with FP32 accumulation.
+ * Split operands need 16-byte aligned base pointers and a row pitch (in elements) that is a multiple of 8.  These
+ * kernels use bounded device-side waits; flmm_context_check reports a wait that gave up. */
+
+/* Synchronise `stream` and return FLMM_ERR_TIMEOUT (clearing the flag) if a kernel of this context gave up a
+ * bounded wait since the last check. */
+int flmm_context_check(flmm_context* ctx, void* stream);
+
+/* Split rows of X (rows, K) -- FP64 when x_is_f64, else FP32 -- into hi / lo FP16 (rows, ldo) and scale (rows,). */
+int flmm_split_rows_f16(const void* X, int x_is_f64, int64_t ldx, int rows, int K, void* hi, void* lo, int64_t ldo,
+                        float* scale, void* stream);
+
+/* C (Mr, Nr) FP32 = sa[i] sb[j] sum_k (Ah + Al)[i, k] (Bh + Bl)[j, k]  (+ C when accumulate): the eigenbasis
+ * rotations UY = U_eff^T Y_r and US = U_eff^T S_r (fasterlmm/core.py:518, :629) and the per-chromosome Gram of the
+ * kinship (fasterlmm/io.py:264), all computed as row-major "rows x rows" products. */
+int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void* Al, const float* sa, int64_t lda, int Mr,
+                        const void* Bh, const void* Bl, const float* sb, int64_t ldb, int Nr, int K, float* C,
+                        int64_t ldc, int accumulate, void* stream);
+
+/* Fast delta fit (fasterlmm/core.py:561-595): FP32 grid argmin, then the stationary point of the loss in the
+ * reference's bracket [grid[i-1], grid[i+1]] by a sign-safeguarded Newton iteration on d loss / d log delta with
+ * compensated sums.  UYt is FP32.  Outputs as flmm_fit_delta_f64. */
+int flmm_fit_delta_fast_workspace_bytes(int Neff, int n_grid, size_t* bytes);
+int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid, double lo,
+                        double hi, int refine, double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
+                        void* stream);
+
+/* Wald operands (fasterlmm/core.py:639-650).  Column side: w = 1 / (s + exp(log_delta[p])) from s32 (FP32 copy of
+ * s), A1 = w o UY and A2 = w split per column, rWr[p] = max(sum w UY^2, 1e-300).  Variant side: B1 = US and
+ * B2 = US o US split per variant. */
+int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu, const double* log_delta,
+                                 int P, void* A1h, void* A1l, void* A2h, void* A2l, int64_t lda, float* sa1,
+                                 float* sa2, float* rWr, void* stream);
+int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Neff, void* B1h, void* B1l, void* B2h,
+                                  void* B2l, int64_t ldb, float* sb1, float* sb2, void* stream);
+
+/* Fused split-precision Wald scan (fasterlmm/core.py:601-671): sWy = A1 B1^T and sWs = A2 B2^T on the tensor cores,
+ * then in the epilogue beta, var_beta (df Neff - 1), F, SE, SFVE with the reference's clamps; real columns p < n_real
+ * write out[rows[m] * ldo + p]; max_F[p] is raised to the column max. */
+int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, const void* A2h, const void* A2l,
+                        int64_t lda, const float* sa1, const float* sa2, const float* rWr, int P, int n_real,
+                        const void* B1h, const void* B1l, const void* B2h, const void* B2l, int64_t ldb,
+                        const float* sb1, const float* sb2, int Mc, int Neff, const int64_t* rows, double* f,
+                        double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
+
+/* Small conversions of the fast form: y[i] = (float)x[i]; y[i] += x[i] (FP32 into FP64); the LOCO kinship from an FP64
+ * total and an FP32 chromosome Gram, K = (Gtot - Gc) / m_loco. */
+int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
+int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
+int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
 
 #ifdef __cplusplus
 }
