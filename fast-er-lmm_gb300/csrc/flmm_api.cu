@@ -11,11 +11,19 @@
 
 #include "flmm_common.cuh"
 
+constexpr int kEighWorkers = 8;
+
 struct flmm_context {
     int device = 0;
     int sm_count = 0;
     cusolverDnHandle_t solver = nullptr;
     int* err_flag = nullptr;  // device int raised by kernels whose bounded waits time out
+    // worker streams / handles for running independent eigendecompositions side by side
+    cudaStream_t workers[kEighWorkers] = {};
+    cusolverDnHandle_t wsolver[kEighWorkers] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kEighWorkers] = {};
+    cusolverDnParams_t params = nullptr;
 };
 
 namespace flmm {
@@ -70,6 +78,8 @@ extern "C" const char* flmm_last_error(void) { return g_last_error; }
 
 extern "C" uint64_t flmm_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
+extern "C" int flmm_context_destroy(flmm_context* ctx);
+
 extern "C" int flmm_context_create(int device, flmm_context** out) {
     FLMM_REQUIRE(out != nullptr, "flmm_context_create: out is NULL");
     *out = nullptr;
@@ -92,6 +102,18 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
         cusolverDnDestroy(ctx->solver);
         delete ctx;
         return fail(FLMM_ERR_CUDA, "flmm_context_create: cannot allocate the device error flag");
+    }
+    bool ok = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cusolverDnCreateParams(&ctx->params) == CUSOLVER_STATUS_SUCCESS;
+    for (int w = 0; ok && w < kEighWorkers; ++w) {
+        ok = cudaStreamCreateWithFlags(&ctx->workers[w], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->join[w], cudaEventDisableTiming) == cudaSuccess &&
+             cusolverDnCreate(&ctx->wsolver[w]) == CUSOLVER_STATUS_SUCCESS &&
+             cusolverDnSetStream(ctx->wsolver[w], ctx->workers[w]) == CUSOLVER_STATUS_SUCCESS;
+    }
+    if (!ok) {
+        flmm_context_destroy(ctx);
+        return fail(FLMM_ERR_CUDA, "flmm_context_create: cannot create worker streams / solver handles");
     }
     *out = ctx;
     return FLMM_OK;
@@ -116,6 +138,13 @@ extern "C" int flmm_context_destroy(flmm_context* ctx) {
     if (!ctx) return FLMM_OK;
     if (ctx->solver) cusolverDnDestroy(ctx->solver);
     if (ctx->err_flag) cudaFree(ctx->err_flag);
+    for (int w = 0; w < kEighWorkers; ++w) {
+        if (ctx->wsolver[w]) cusolverDnDestroy(ctx->wsolver[w]);
+        if (ctx->workers[w]) cudaStreamDestroy(ctx->workers[w]);
+        if (ctx->join[w]) cudaEventDestroy(ctx->join[w]);
+    }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->params) cusolverDnDestroyParams(ctx->params);
     delete ctx;
     return FLMM_OK;
 }
@@ -151,6 +180,91 @@ extern "C" int flmm_eigh(flmm_context* ctx, double* A, int N, double* evals, voi
                                            evals, dwork, lwork, info);
     if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnDsyevd");
     return check_cuda("cusolverDnDsyevd");
+}
+
+// ---- batched eigendecomposition: all LOCO kinships of a scan at once --------------------------------------------
+
+namespace {
+
+struct BatchedLayout {
+    size_t dev_bytes, host_bytes;
+};
+
+int batched_api_sizes(flmm_context* ctx, int N, int batch, BatchedLayout* L) {
+    size_t dbytes = 0, hbytes = 0;
+    cusolverStatus_t st = cusolverDnXsyevBatched_bufferSize(ctx->solver, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
+                                                            CUBLAS_FILL_MODE_LOWER, N, CUDA_R_64F, nullptr, N,
+                                                            CUDA_R_64F, nullptr, CUDA_R_64F, &dbytes, &hbytes, batch);
+    if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnXsyevBatched_bufferSize");
+    L->dev_bytes = align_up(dbytes, 256) + align_up(sizeof(int) * batch, 256);
+    L->host_bytes = hbytes;
+    return FLMM_OK;
+}
+
+}  // namespace
+
+extern "C" int flmm_eigh_batched_workspace_bytes(flmm_context* ctx, int N, int batch, int mode, size_t* bytes) {
+    FLMM_REQUIRE(ctx && bytes && N > 0 && batch > 0 && (mode == 1 || mode == 2),
+                 "flmm_eigh_batched_workspace_bytes: bad arguments (mode 1 = batched API, 2 = concurrent syevd)");
+    if (mode == 1) {
+        BatchedLayout L;
+        int rc = batched_api_sizes(ctx, N, batch, &L);
+        if (rc) return rc;
+        if (L.host_bytes != 0)
+            return fail(FLMM_ERR_SOLVER, "cusolverDnXsyevBatched needs %zu bytes of host workspace", L.host_bytes);
+        *bytes = L.dev_bytes;
+        return FLMM_OK;
+    }
+    size_t one = 0;
+    int rc = flmm_eigh_workspace_bytes(ctx, N, &one);
+    if (rc) return rc;
+    const int slots = batch < kEighWorkers ? batch : kEighWorkers;
+    *bytes = one * static_cast<size_t>(slots);
+    return FLMM_OK;
+}
+
+extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, void* work,
+                                 size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(ctx && A && evals && work && N > 0 && batch > 0, "flmm_eigh_batched: bad arguments");
+    size_t need = 0;
+    int rc = flmm_eigh_batched_workspace_bytes(ctx, N, batch, mode, &need);
+    if (rc) return rc;
+    if (work_bytes < need)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_eigh_batched: need %zu bytes, got %zu", need, work_bytes);
+    cudaStream_t st = as_stream(stream);
+    const size_t nn = static_cast<size_t>(N) * N;
+    if (mode == 1) {
+        BatchedLayout L;
+        if ((rc = batched_api_sizes(ctx, N, batch, &L))) return rc;
+        int* info = reinterpret_cast<int*>(static_cast<char*>(work) + (L.dev_bytes - align_up(sizeof(int) * batch, 256)));
+        cusolverDnSetStream(ctx->solver, st);
+        cusolverStatus_t cs = cusolverDnXsyevBatched(ctx->solver, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
+                                                     CUBLAS_FILL_MODE_LOWER, N, CUDA_R_64F, A, N, CUDA_R_64F, evals,
+                                                     CUDA_R_64F, work, L.dev_bytes, nullptr, 0, info, batch);
+        if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail(cs, "cusolverDnXsyevBatched");
+        return check_cuda("cusolverDnXsyevBatched");
+    }
+    // mode 2: independent syevd calls spread over the worker streams, forked from and joined back into `stream`
+    size_t one = 0;
+    if ((rc = flmm_eigh_workspace_bytes(ctx, N, &one))) return rc;
+    const int slots = batch < kEighWorkers ? batch : kEighWorkers;
+    const int lwork = static_cast<int>((one - 256) / sizeof(double));
+    FLMM_CUDA(cudaEventRecord(ctx->fork, st));
+    for (int w = 0; w < slots; ++w) FLMM_CUDA(cudaStreamWaitEvent(ctx->workers[w], ctx->fork, 0));
+    for (int b = 0; b < batch; ++b) {
+        const int w = b % slots;
+        char* wbase = static_cast<char*>(work) + one * static_cast<size_t>(w);
+        int* info = reinterpret_cast<int*>(wbase + one - 256);
+        cusolverStatus_t cs = cusolverDnDsyevd(ctx->wsolver[w], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N,
+                                               A + nn * b, N, evals + static_cast<size_t>(N) * b,
+                                               reinterpret_cast<double*>(wbase), lwork, info);
+        if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail(cs, "cusolverDnDsyevd (worker)");
+    }
+    for (int w = 0; w < slots; ++w) {
+        FLMM_CUDA(cudaEventRecord(ctx->join[w], ctx->workers[w]));
+        FLMM_CUDA(cudaStreamWaitEvent(st, ctx->join[w], 0));
+    }
+    return check_cuda("flmm_eigh_batched");
 }
 
 // ---- covariate basis (thin SVD of X) --------------------------------------------------------------------------

@@ -127,19 +127,43 @@ __device__ __forceinline__ void neumaier(float& sum, float& comp, float x) {
     sum = t;
 }
 
-// One evaluation by a warp at x = log delta (x is warp-uniform).
+// exact sum and error of a + b (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// warp-wide sum of a compensated pair (hi + lo), TwoSum at every level of the butterfly
+__device__ __forceinline__ float warp_sum_pair(float hi, float lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        float sum, err;
+        two_sum(hi, oh, sum, err);
+        hi = sum;
+        lo = lo + ol + err;
+    }
+    return hi + lo;
+}
+
+// One evaluation by a warp at x = log delta (x is warp-uniform), all in FP32.
 //
 // g is formed around the centre c = 1 / (sbar + delta), sbar the mean eigenvalue: with d_n = r_n - c =
 // (sbar - s_n) r_n c,
 //     g = sum d - Neff (c E1 + E2) / (c U + E1),   U = sum u^2, E1 = sum u^2 d, E2 = sum u^2 d^2,
 // which is T1 - Neff S2 / S1 rearranged so that no O(r) terms cancel: when delta >> s the r_n are nearly equal and
-// the information in g is in their O(s / delta) spread, which the centred terms carry at full FP32 precision.
+// the information in g is in their O(s / delta) spread, which the centred terms carry at full FP32 precision
+// (compensated sums for the first-order terms).  delta = exp(x) is formed from a hi / lo split of x so that it is
+// exact to FP32 rounding at any x.
 __device__ NewtonEval newton_eval(const float* __restrict__ s32, float sbar, const float* __restrict__ u, int Neff,
                                   double x, bool want_loss) {
     const int lane = threadIdx.x & 31;
-    const double delta_d = exp(x);
-    const float delta = static_cast<float>(delta_d);
-    const float c = static_cast<float>(1.0 / (static_cast<double>(sbar) + delta_d));
+    const float xh = static_cast<float>(x);
+    const float xl = static_cast<float>(x - static_cast<double>(xh));
+    const float delta = expf(xh) * (1.0f + xl);
+    const float c = 1.0f / (sbar + delta);
     float d1 = 0.f, cd1 = 0.f, e1 = 0.f, ce1 = 0.f, e2 = 0.f, e3 = 0.f, f2 = 0.f, uu_s = 0.f, cu = 0.f, sl = 0.f;
     for (int n = lane; n < Neff; n += 32) {
         const float sd = s32[n] + delta;
@@ -148,36 +172,36 @@ __device__ NewtonEval newton_eval(const float* __restrict__ s32, float sbar, con
         const float uu = u[n] * u[n];
         neumaier(d1, cd1, d);
         neumaier(e1, ce1, uu * d);
-        e2 += uu * d * d;
-        e3 += uu * d * d * d;
+        const float ud = uu * d * d;
+        e2 += ud;
+        e3 += ud * d;
         f2 += d * d;
         neumaier(uu_s, cu, uu);
         if (want_loss) sl += __logf(sd);
     }
-    const double D1 = warp_sum(static_cast<double>(d1) + static_cast<double>(cd1));
-    const double E1 = warp_sum(static_cast<double>(e1) + static_cast<double>(ce1));
-    const double E2 = warp_sum(static_cast<double>(e2));
-    const double E3 = warp_sum(static_cast<double>(e3));
-    const double F2 = warp_sum(static_cast<double>(f2));
-    const double U = warp_sum(static_cast<double>(uu_s) + static_cast<double>(cu));
+    const float D1 = warp_sum_pair(d1, cd1);
+    const float E1 = warp_sum_pair(e1, ce1);
+    const float U = warp_sum_pair(uu_s, cu);
+    const float E2 = warp_sum(e2);
+    const float E3 = warp_sum(e3);
+    const float F2 = warp_sum(f2);
     NewtonEval e;
-    const double neff = static_cast<double>(Neff);
-    const double cc = static_cast<double>(c);
-    if (U > 0.0) {
-        e.g = D1 - neff * (cc * E1 + E2) / (cc * U + E1);
+    const float neff = static_cast<float>(Neff);
+    if (U > 0.0f) {
+        e.g = D1 - neff * (c * E1 + E2) / (c * U + E1);
         // dg/dx = delta (-T2 + Neff (2 S3 / S1 - (S2 / S1)^2)) in the same centred sums: with F2 = sum d^2,
         // E3 = sum u^2 d^3, a = E1 / (c U), b = E2 / (c^2 U), t3 = E3 / (c^3 U) one has T2 = Neff c^2 + 2 c D1 + F2,
         // S1 = c U (1 + a), S2 = c^2 U (1 + 2a + b), S3 = c^3 U (1 + 3a + 3b + t3), and the O(1) terms cancel exactly
-        const double a = E1 / (cc * U), b = E2 / (cc * cc * U), t3 = E3 / (cc * cc * cc * U);
-        const double br = -2.0 * D1 / (cc * neff) - F2 / (cc * cc * neff) + (2.0 * a + 4.0 * b + 2.0 * t3) / (1.0 + a) -
-                          (a + b) * (a + b) / ((1.0 + a) * (1.0 + a));
-        e.gp = delta_d * neff * cc * cc * br;
+        const float a = E1 / (c * U), b = E2 / (c * c * U), t3 = E3 / (c * c * c * U);
+        const float br = -2.0f * D1 / (c * neff) - F2 / (c * c * neff) + (2.0f * a + 4.0f * b + 2.0f * t3) / (1.0f + a) -
+                         (a + b) * (a + b) / ((1.0f + a) * (1.0f + a));
+        e.gp = static_cast<double>(delta) * neff * c * c * br;
     } else {  // all-zero rotated column: the loss only grows with delta
         e.g = 1.0;
         e.gp = 1.0;
     }
     e.loss = 0.0;
-    if (want_loss) e.loss = neff * log(fmax(cc * U + E1, 1e-300)) + warp_sum(static_cast<double>(sl));
+    if (want_loss) e.loss = neff * logf(fmaxf(c * U + E1, 1e-30f)) + warp_sum(sl);
     return e;
 }
 
@@ -202,12 +226,33 @@ __global__ void k_newton_refine(const double* __restrict__ s, int Neff, const fl
     double out = grid[i];
     if (refine && G > 1) {
         const float* u = UYt + p * ldu;
-        // the FP32 grid can misplace the argmin by a node on flat losses: walk it with exact derivative signs
-        // until the loss rises on both sides of the bracket centre (bounded walk)
-        for (int step = 0; step < 8; ++step) {
-            if (i < G - 1 && newton_eval(s32, sbar, u, Neff, grid[i + 1], false).g < 0.0) { ++i; continue; }
-            if (i > 0 && newton_eval(s32, sbar, u, Neff, grid[i - 1], false).g > 0.0) { --i; continue; }
-            break;
+        // The FP32 grid argmin is only as good as the FP32 loss (~1e-4 absolute); on flat losses it can sit several
+        // nodes from the minimum.  The exact derivative sign at that node says which side the minimum is on, and a
+        // binary search over the grid nodes on that side finds where d loss / d log delta changes sign, so the
+        // bracket [grid[i-1], grid[i+1]] always contains the minimum (for losses with one minimum on that side).
+        const double gi = newton_eval(s32, sbar, u, Neff, grid[i], false).g;
+        if (gi < 0.0) {
+            if (newton_eval(s32, sbar, u, Neff, grid[G - 1], false).g < 0.0) {
+                i = G - 1;  // still falling at the top of the grid
+            } else {
+                int lo = i, hi = G - 1;  // g(lo) < 0 <= g(hi)
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (newton_eval(s32, sbar, u, Neff, grid[mid], false).g < 0.0) lo = mid; else hi = mid;
+                }
+                i = hi;
+            }
+        } else if (gi > 0.0) {
+            if (newton_eval(s32, sbar, u, Neff, grid[0], false).g > 0.0) {
+                i = 0;  // already rising at the bottom of the grid
+            } else {
+                int lo = 0, hi = i;  // g(lo) <= 0 < g(hi)
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (newton_eval(s32, sbar, u, Neff, grid[mid], false).g > 0.0) hi = mid; else lo = mid;
+                }
+                i = lo;
+            }
         }
         const double a = grid[max(i - 1, 0)], b = grid[min(i + 1, G - 1)];
         const NewtonEval ea = newton_eval(s32, sbar, u, Neff, a, false);

@@ -36,7 +36,7 @@ constexpr int kThreads = 192;
 template <int NG, int BK>
 struct Cfg {
     static constexpr int kTileBytes = 128 * BK * 2;
-    static constexpr int kStageBytes = NG * 4 * kTileBytes;  // A hi, A lo, B hi, B lo per product
+    static constexpr int kStageBytes = 4 * kTileBytes;  // A hi, A lo, B hi, B lo of one product
     static constexpr int kStages = 3;
     static constexpr uint32_t kSwizzle = (BK == 64) ? 2u : 4u;  // 128-byte / 64-byte swizzle
     static constexpr uint32_t kSBO = 8u * BK * 2u;             // bytes between 8-row groups
@@ -51,7 +51,8 @@ struct TcMaps {
 };
 
 struct TcArgs {
-    int Mr, Nr, K;  // A rows, B rows, reduction length
+    int Mr, Nr, K;  // A rows, B rows, reduction length of product 0
+    int K2;         // reduction length of product 1 (NG == 2)
     int* err;       // device error flag (bounded waits)
     // NG == 1 epilogue
     const float* sa;
@@ -90,7 +91,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
     const int n_tiles = ((args.Mr + kBM - 1) / kBM) * tiles_b;
-    const int n_kb = (args.K + BK - 1) / BK;
+    // the NG products of a tile run one after the other, product g over its own K: k-blocks [0, n_kb0) feed
+    // accumulator 0, [n_kb0, n_kb) accumulator 1
+    const int n_kb0 = (args.K + BK - 1) / BK;
+    const int n_kb = n_kb0 + (NG == 2 ? (args.K2 + BK - 1) / BK : 0);
     constexpr uint32_t idesc = idesc_f16_f32(kBM, kBN);
 
     if (threadIdx.x == 0) {
@@ -133,13 +137,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                     armed[stage] = true;
                     armed_phase[stage] = phase;
                     uint8_t* base = smem + stage * C::kStageBytes;
-#pragma unroll
-                    for (int g = 0; g < NG; ++g) {
-                        tma_load_2d(base + (g * 4 + 0) * C::kTileBytes, &maps.m[g * 4 + 0], kb * BK, ta * kBM, &full[stage]);
-                        tma_load_2d(base + (g * 4 + 1) * C::kTileBytes, &maps.m[g * 4 + 1], kb * BK, ta * kBM, &full[stage]);
-                        tma_load_2d(base + (g * 4 + 2) * C::kTileBytes, &maps.m[g * 4 + 2], kb * BK, tb * kBN, &full[stage]);
-                        tma_load_2d(base + (g * 4 + 3) * C::kTileBytes, &maps.m[g * 4 + 3], kb * BK, tb * kBN, &full[stage]);
-                    }
+                    const int g = kb < n_kb0 ? 0 : 1;
+                    const int kx = (kb - g * n_kb0) * BK;
+                    tma_load_2d(base + 0 * C::kTileBytes, &maps.m[g * 4 + 0], kx, ta * kBM, &full[stage]);
+                    tma_load_2d(base + 1 * C::kTileBytes, &maps.m[g * 4 + 1], kx, ta * kBM, &full[stage]);
+                    tma_load_2d(base + 2 * C::kTileBytes, &maps.m[g * 4 + 2], kx, tb * kBN, &full[stage]);
+                    tma_load_2d(base + 3 * C::kTileBytes, &maps.m[g * 4 + 3], kx, tb * kBN, &full[stage]);
                     if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
                 }
             }
@@ -163,20 +166,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                     if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
                     fence_after_sync();
                     const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
+                    const int g = kb < n_kb0 ? 0 : 1;
+                    const int kb_g = kb - g * n_kb0;
+                    const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
 #pragma unroll
                     for (int kk = 0; kk < BK / 16; ++kk) {
-#pragma unroll
-                        for (int g = 0; g < NG; ++g) {
-                            const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
-                            const uint32_t tg = sbase + static_cast<uint32_t>(g * 4 * C::kTileBytes);
-                            const uint64_t ah = smem_desc(tg + 0 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                            const uint64_t al = smem_desc(tg + 1 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                            const uint64_t bh = smem_desc(tg + 2 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                            const uint64_t bl = smem_desc(tg + 3 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                            mma_f16(d, ah, bh, idesc, (kb | kk) ? 1u : 0u);
-                            mma_f16(d, ah, bl, idesc, 1u);
-                            mma_f16(d, al, bh, idesc, 1u);
-                        }
+                        const uint64_t ah = smem_desc(sbase + 0 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t al = smem_desc(sbase + 1 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t bh = smem_desc(sbase + 2 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t bl = smem_desc(sbase + 3 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        mma_f16(d, ah, bh, idesc, (kb_g | kk) ? 1u : 0u);
+                        mma_f16(d, ah, bl, idesc, 1u);
+                        mma_f16(d, al, bh, idesc, 1u);
                     }
                     mma_commit(&empty[stage]);
                     if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
@@ -236,7 +237,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                         const int m = tb * kBN + c0 + j;
                         if (m >= args.Nr) continue;
                         const float swy = vy[j] * sa1 * args.sb[m];
-                        const float denom = fmaxf(vs[j] * sa2 * args.sb2[m], 1e-30f);
+                        const float sws = vs[j] * sa2 * args.sb2[m];
+                        if (!(sws > 0.0f)) {
+                            // a variant with no variance left (e.g. monomorphic): the reference clamps sWs to 1e-300
+                            // in FP64, which gives beta = F = SFVE = 0 and SE = sqrt(rWr / df / 1e-300)
+                            colmax = fmaxf(colmax, 0.0f);
+                            if (real) {
+                                const int64_t o = args.rows[m] * args.ldo + p;
+                                args.f[o] = 0.0;
+                                args.beta[o] = 0.0;
+                                args.se[o] = sqrt(fmax(static_cast<double>(rwr), 1e-300) / args.var_df / 1e-300);
+                                args.sfve[o] = 0.0;
+                            }
+                            continue;
+                        }
+                        const float denom = fmaxf(sws, 1e-30f);
                         const float inv_d = 1.0f / denom;
                         const float b = swy * inv_d;
                         const float qq = swy * swy;
@@ -323,45 +338,96 @@ __global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int
     if (threadIdx.x == 0) scale[r] = ldexpf(1.0f, -e);
 }
 
-// Wald column side (fasterlmm/core.py:639-643): w = 1 / (s + delta_p), A1 = w UY, A2 = w, rWr = sum w UY^2 (FP64
-// accumulation), each row split with its own exponent.  One warp per column p.
+// sWs by interpolation.  sWs(delta) = sum_n US_n^2 / (s_n + delta) depends on the column only through delta.  All
+// Wald outputs are unchanged when a column's weights w = 1 / (s + delta) are multiplied by a constant, so the scan
+// uses w~ = (shat + delta) / (s + delta) (shat = mean eigenvalue), whose sums vary by a bounded factor over the whole
+// delta range even when some s are 0.  f~(x) = sum_n US_n^2 w~_n(e^x) is smooth in x = log delta (poles at distance
+// pi from the real axis), so it is evaluated at R equispaced nodes x_r = x0 + r h (h = 1/4) and interpolated at each
+// column's x by the 10-point Lagrange polynomial on the nodes around it (interpolation error < 1e-9 relative).  The
+// second product of the Wald kernel then has K = R (~90) instead of K = Neff.
+constexpr int kInterpPoints = 10;
+
+// Wald column side (fasterlmm/core.py:639-643): w~ = (shat + delta_p) / (s + delta_p), A1 = w~ o UY split,
+// rWr = sum w~ UY^2 (FP64 accumulation), and the column's Lagrange weights L (R entries, 10 non-zero) split.  One
+// warp per column p.
 __global__ void k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __restrict__ UYt,
-                                    int64_t ldu, const double* __restrict__ ld, int P, __half* __restrict__ A1h,
-                                    __half* __restrict__ A1l, __half* __restrict__ A2h, __half* __restrict__ A2l,
-                                    int64_t lda, float* __restrict__ sa1, float* __restrict__ sa2,
-                                    float* __restrict__ rWr) {
+                                    int64_t ldu, const double* __restrict__ ld, int P, const float* __restrict__ shat_p,
+                                    double x0, double h, int R, __half* __restrict__ A1h, __half* __restrict__ A1l,
+                                    int64_t lda, __half* __restrict__ Lh, __half* __restrict__ Ll, int64_t ldl,
+                                    float* __restrict__ sa1, float* __restrict__ sl, float* __restrict__ rWr) {
     const int lane = threadIdx.x & 31;
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
-    const float delta = static_cast<float>(exp(ld[p]));
+    const double x = ld[p];
+    const float delta = static_cast<float>(exp(x));
+    const float num = *shat_p + delta;
     const float* u = UYt + p * ldu;
-    float m1 = 0.0f, m2 = 0.0f;
+    float m1 = 0.0f;
     double acc = 0.0;
     for (int n = lane; n < Neff; n += 32) {
-        const float w = 1.0f / (s32[n] + delta);
+        const float w = num / (s32[n] + delta);
         const float a = w * u[n];
         m1 = fmaxf(m1, fabsf(a));
-        m2 = fmaxf(m2, w);
         acc += static_cast<double>(a) * static_cast<double>(u[n]);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-        m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-    }
+    for (int o = 16; o > 0; o >>= 1) m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
     acc = warp_sum(acc);
-    int e1, e2;
-    const float mul1 = row_scale_exp(m1, &e1), mul2 = row_scale_exp(m2, &e2);
-    for (int n = lane; n < Neff; n += 32) {
-        const float w = 1.0f / (s32[n] + delta);
-        split_store(w * u[n], mul1, A1h, A1l, p * lda + n);
-        split_store(w, mul2, A2h, A2l, p * lda + n);
+    int e1;
+    const float mul1 = row_scale_exp(m1, &e1);
+    for (int n = lane; n < Neff; n += 32) split_store((num / (s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
+    // Lagrange weights on nodes base .. base + 9 around x; lane k < 10 owns weight k
+    int base = static_cast<int>(floor((x - x0) / h)) - (kInterpPoints / 2 - 1);
+    base = max(0, min(base, R - kInterpPoints));
+    const double t = (x - (x0 + base * h)) / h;
+    double wk = 0.0;
+    if (lane < kInterpPoints) {
+        wk = 1.0;
+        for (int m = 0; m < kInterpPoints; ++m)
+            if (m != lane) wk *= (t - m) / static_cast<double>(lane - m);
+    }
+    float lm = fabsf(static_cast<float>(wk));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lm = fmaxf(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    int el;
+    const float mull = row_scale_exp(lm, &el);
+    // every lane writes its own entries of the row; the ten weights come from lanes 0..9 by shuffle
+    double wv[kInterpPoints];
+#pragma unroll
+    for (int k = 0; k < kInterpPoints; ++k) wv[k] = __shfl_sync(0xffffffffu, wk, k);
+    for (int r = lane; r < R; r += 32) {
+        const int k = r - base;
+        double v = 0.0;
+#pragma unroll
+        for (int kk = 0; kk < kInterpPoints; ++kk)
+            if (kk == k) v = wv[kk];
+        const double vs = v * static_cast<double>(mull);
+        const __half hh = __double2half(vs);
+        Lh[p * ldl + r] = hh;
+        Ll[p * ldl + r] = __double2half(vs - static_cast<double>(__half2float(hh)));
     }
     if (lane == 0) {
         sa1[p] = ldexpf(1.0f, -e1);
-        sa2[p] = ldexpf(1.0f, -e2);
+        sl[p] = ldexpf(1.0f, -el);
         rWr[p] = static_cast<float>(fmax(acc, 1e-300));
     }
+}
+
+// normalised weights at the interpolation nodes: W~[r, n] = (shat + e^{x_r}) / (s_n + e^{x_r}), FP64
+__global__ void k_interp_nodes(const double* __restrict__ s, int Neff, const float* __restrict__ shat_p, double x0,
+                               double h, int R, double* __restrict__ W) {
+    const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t >= static_cast<int64_t>(R) * Neff) return;
+    const int r = static_cast<int>(t / Neff), n = static_cast<int>(t % Neff);
+    const double delta = exp(x0 + r * h);
+    W[t] = (static_cast<double>(*shat_p) + delta) / (s[n] + delta);
+}
+
+__global__ void k_mean(const double* __restrict__ x, int n, float* __restrict__ out) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) acc += x[i];
+    acc = warp_sum(acc);
+    if (threadIdx.x == 0) *out = static_cast<float>(acc / n);
 }
 
 // Wald variant side: B1 = US, B2 = US o US, each row split.  One warp per variant m.
@@ -489,17 +555,31 @@ extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void
     return launch_tc<1, 64>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }
 
+extern "C" int flmm_mean_f32(const double* x, int n, float* out, void* stream) {
+    FLMM_REQUIRE(x && out && n > 0, "flmm_mean_f32: bad arguments");
+    k_mean<<<1, 32, 0, as_stream(stream)>>>(x, n, out);
+    return check_launch("k_mean");
+}
+
+extern "C" int flmm_wald_interp_nodes(const double* s, int Neff, const float* shat, double x0, double h, int R,
+                                      double* W, void* stream) {
+    FLMM_REQUIRE(s && shat && W && Neff > 0 && R >= kInterpPoints && h > 0, "flmm_wald_interp_nodes: bad arguments");
+    k_interp_nodes<<<ceil_div(static_cast<int64_t>(R) * Neff, 256), 256, 0, as_stream(stream)>>>(s, Neff, shat, x0, h,
+                                                                                               R, W);
+    return check_launch("k_interp_nodes");
+}
+
 extern "C" int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu,
-                                            const double* log_delta, int P, void* A1h, void* A1l, void* A2h,
-                                            void* A2l, int64_t lda, float* sa1, float* sa2, float* rWr,
-                                            void* stream) {
-    FLMM_REQUIRE(s32 && UYt && log_delta && A1h && A1l && A2h && A2l && sa1 && sa2 && rWr && Neff > 0 &&
-                     ldu >= Neff && lda >= Neff && P >= 0,
+                                            const double* log_delta, int P, const float* shat, double x0, double h,
+                                            int R, void* A1h, void* A1l, int64_t lda, void* Lh, void* Ll, int64_t ldl,
+                                            float* sa1, float* sl, float* rWr, void* stream) {
+    FLMM_REQUIRE(s32 && UYt && log_delta && shat && A1h && A1l && Lh && Ll && sa1 && sl && rWr && Neff > 0 &&
+                     ldu >= Neff && lda >= Neff && ldl >= R && R >= kInterpPoints && h > 0 && P >= 0,
                  "flmm_wald_split_prep_columns: bad arguments");
     if (P == 0) return FLMM_OK;
     k_wald_prep_columns<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, as_stream(stream)>>>(
-        s32, Neff, UYt, ldu, log_delta, P, static_cast<__half*>(A1h), static_cast<__half*>(A1l),
-        static_cast<__half*>(A2h), static_cast<__half*>(A2l), lda, sa1, sa2, rWr);
+        s32, Neff, UYt, ldu, log_delta, P, shat, x0, h, R, static_cast<__half*>(A1h), static_cast<__half*>(A1l), lda,
+        static_cast<__half*>(Lh), static_cast<__half*>(Ll), ldl, sa1, sl, rWr);
     return check_launch("k_wald_prep_columns");
 }
 
@@ -515,37 +595,42 @@ extern "C" int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int
     return check_launch("k_wald_prep_variants");
 }
 
-extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, const void* A2h,
-                                   const void* A2l, int64_t lda, const float* sa1, const float* sa2, const float* rWr,
-                                   int P, int n_real, const void* B1h, const void* B1l, const void* B2h,
-                                   const void* B2l, int64_t ldb, const float* sb1, const float* sb2, int Mc, int Neff,
-                                   const int64_t* rows, double* f, double* beta, double* se, double* sfve, int64_t ldo,
-                                   double* max_F, void* stream) {
-    FLMM_REQUIRE(ctx && A1h && A1l && A2h && A2l && sa1 && sa2 && rWr && B1h && B1l && B2h && B2l && sb1 && sb2 &&
-                     max_F && Neff > 1 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
-                     ldb >= Neff,
+extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda, const float* sa1,
+                                   const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr,
+                                   int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1,
+                                   const void* Fh, const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff,
+                                   int R, const int64_t* rows, double* f, double* beta, double* se, double* sfve,
+                                   int64_t ldo, double* max_F, void* stream) {
+    FLMM_REQUIRE(ctx && A1h && A1l && sa1 && Lh && Ll && sl && rWr && B1h && B1l && sb1 && Fh && Fl && sf && max_F &&
+                     Neff > 1 && R > 0 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
+                     ldb >= Neff && ldl >= R && ldf >= R,
                  "flmm_wald_split_f16: bad arguments");
     FLMM_REQUIRE(n_real == 0 || Mc == 0 || (rows && f && beta && se && sfve && ldo >= n_real),
                  "flmm_wald_split_f16: real-column outputs missing");
     if (P == 0 || Mc == 0) return FLMM_OK;
     TcMaps maps;
     std::memset(&maps, 0, sizeof(maps));
-    const void* srcs[8] = {A1h, A1l, B1h, B1l, A2h, A2l, B2h, B2l};
-    for (int i = 0; i < 8; ++i) {
-        const bool a_side = (i % 4) < 2;
-        int rc = make_map(&maps.m[i], srcs[i], a_side ? P : Mc, Neff, a_side ? lda : ldb, 32);
-        if (rc) return rc;
-    }
+    int rc;
+    // product 0: sWy = (w~ o UY) US^T over K = Neff; product 1: sWs~ = L F^T over K = R
+    if ((rc = make_map(&maps.m[0], A1h, P, Neff, lda, 64))) return rc;
+    if ((rc = make_map(&maps.m[1], A1l, P, Neff, lda, 64))) return rc;
+    if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, 64))) return rc;
+    if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, 64))) return rc;
+    if ((rc = make_map(&maps.m[4], Lh, P, R, ldl, 64))) return rc;
+    if ((rc = make_map(&maps.m[5], Ll, P, R, ldl, 64))) return rc;
+    if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, 64))) return rc;
+    if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, 64))) return rc;
     TcArgs a;
     std::memset(&a, 0, sizeof(a));
     a.Mr = P;
     a.Nr = Mc;
     a.K = Neff;
+    a.K2 = R;
     a.err = flmm_ctx_err_flag(ctx);
     a.sa = sa1;
     a.sb = sb1;
-    a.sa2 = sa2;
-    a.sb2 = sb2;
+    a.sa2 = sl;
+    a.sb2 = sf;
     a.rWr = rWr;
     a.n_real = n_real;
     a.var_df = static_cast<float>(Neff - 1);
@@ -556,5 +641,5 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sfve = sfve;
     a.ldo = ldo;
     a.max_F = max_F;
-    return launch_tc<2, 32>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+    return launch_tc<2, 64>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }

@@ -37,6 +37,8 @@ SIGNATURES: dict[str, list] = {
     "flmm_project_kinship": [_p, _i64, _p, _i, _i, _p, _i64, _p, _sz, _p],
     "flmm_eigh_workspace_bytes": [_p, _i, _psz],
     "flmm_eigh": [_p, _p, _i, _p, _p, _sz, _p],
+    "flmm_eigh_batched_workspace_bytes": [_p, _i, _i, _i, _psz],
+    "flmm_eigh_batched": [_p, _p, _i, _i, _p, _i, _p, _sz, _p],
     "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
     "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],
     "flmm_gemm_nt_f64": [_p, _i64, _p, _i64, _p, _i64, _i, _i, _i, _d, _p],
@@ -56,10 +58,13 @@ SIGNATURES: dict[str, list] = {
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],
     "flmm_fit_delta_fast_workspace_bytes": [_i, _i, _psz],
     "flmm_fit_delta_fast": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
-    "flmm_wald_split_prep_columns": [_p, _i, _p, _i64, _p, _i, _p, _p, _p, _p, _i64, _p, _p, _p, _p],
+    "flmm_mean_f32": [_p, _i, _p, _p],
+    "flmm_wald_interp_nodes": [_p, _i, _p, _d, _d, _i, _p, _p],
+    "flmm_wald_split_prep_columns": [_p, _i, _p, _i64, _p, _i, _p, _d, _d, _i, _p, _p, _i64, _p, _p, _i64, _p, _p,
+                                     _p, _p],
     "flmm_wald_split_prep_variants": [_p, _i64, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _p],
-    "flmm_wald_split_f16": [_p, _p, _p, _p, _p, _i64, _p, _p, _p, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _i, _i, _p,
-                            _p, _p, _p, _p, _i64, _p, _p],
+    "flmm_wald_split_f16": [_p, _p, _p, _i64, _p, _p, _p, _i64, _p, _p, _i, _i, _p, _p, _i64, _p, _p, _p, _i64, _p,
+                            _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, _p],
     "flmm_convert_f64_f32": [_i64, _p, _p, _p],
     "flmm_accumulate_f32_f64": [_i64, _p, _p, _p],
     "flmm_loco_kinship_f32": [_p, _p, _i, _d, _p, _p],

@@ -202,6 +202,34 @@ class CovariateBasis:
         return R
 
 
+def project_kinship(K: Tensor, basis: CovariateBasis, out: Tensor) -> Tensor:
+    """out (N, N) = (I - PX)(K + I)(I - PX) (fasterlmm/core.py:499-506)."""
+    dev = K.device
+    N = K.shape[0]
+    D = basis.X.shape[1]
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_project_kinship_workspace_bytes", N, D))
+    _lib.call("flmm_project_kinship", _ptr(K), K.stride(0), _ptr(basis.Qx), N, D, _ptr(out), N, w, wb, _stream(dev))
+    return out
+
+
+def eigh_batched(A: Tensor, mode: int = 2) -> Tensor:
+    """In-place FP64 eigendecomposition of a (batch, N, N) stack: eigenvector rows overwrite A; returns evals."""
+    dev = A.device
+    batch, N, _ = A.shape
+    ctx = _lib.context(dev.index)
+    evals = torch.empty((batch, N), dtype=F64, device=dev)
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_eigh_batched_workspace_bytes", ctx, N, batch, mode))
+    _lib.call("flmm_eigh_batched", ctx, _ptr(A), N, batch, _ptr(evals), mode, w, wb, _stream(dev))
+    return evals
+
+
+def compat_spectrum(evals: Tensor, D: int) -> Tensor:
+    N = evals.shape[0]
+    s = torch.empty(N - D, dtype=F64, device=evals.device)
+    _lib.call("flmm_compat_spectrum", _ptr(evals), N, D, _ptr(s), _stream(evals.device))
+    return s
+
+
 def compat_eigh(K: Tensor, basis: CovariateBasis) -> tuple[Tensor, Tensor]:
     """Projected kinship eigendecomposition: s (Neff,) and Ut (Neff, N) (fasterlmm/core.py:498-515)."""
     dev = K.device

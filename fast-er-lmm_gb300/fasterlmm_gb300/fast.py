@@ -21,10 +21,15 @@ import torch
 from torch import Tensor
 
 from . import _lib
-from .core import F64, CovariateBasis, ScanResult, _alloc_outputs, _ptr, _stream, _work, compat_eigh
+from .core import F64, CovariateBasis, ScanResult, _alloc_outputs, _ptr, _stream, _work, compat_spectrum, \
+    eigh_batched, project_kinship
 
 F16 = torch.float16
 F32 = torch.float32
+
+# how the per-chromosome FP64 eigendecompositions run: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on
+# worker streams (see flmm_eigh_batched)
+EIGH_MODE = 1
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -142,6 +147,18 @@ class KinshipPanel:
         return K
 
 
+# sWs interpolation nodes in log delta: spacing and points of the local Lagrange rule (see csrc/flmm_fast.cu)
+INTERP_H = 0.25
+INTERP_Q = 10
+
+
+def interp_nodes(lo: float, hi: float) -> tuple[float, int]:
+    """(x0, R): R nodes x0 + r h covering [lo, hi] with the margins the 10-point stencil needs at both ends."""
+    x0 = lo - (INTERP_Q // 2) * INTERP_H
+    R = int(np.ceil((hi - lo) / INTERP_H - 1e-9)) + INTERP_Q + 1
+    return x0, R
+
+
 class WaldOperands:
     """Split operand buffers of the fused Wald kernel, reused across chromosomes (grow-only)."""
 
@@ -150,40 +167,60 @@ class WaldOperands:
         self.cols = None
         self.vars = None
 
-    def _cols(self, P: int, ld: int):
-        if self.cols is None or self.cols[0].shape[0] < P or self.cols[0].shape[1] != ld:
-            self.cols = [torch.empty((P, ld), dtype=F16, device=self.dev) for _ in range(4)] + \
+    def _cols(self, P: int, ldk: int, ldr: int):
+        c = self.cols
+        if c is None or c[0].shape[0] < P or c[0].shape[1] != ldk or c[2].shape[1] != ldr:
+            self.cols = [torch.empty((P, ldk), dtype=F16, device=self.dev) for _ in range(2)] + \
+                        [torch.empty((P, ldr), dtype=F16, device=self.dev) for _ in range(2)] + \
                         [torch.empty(P, dtype=F32, device=self.dev) for _ in range(3)]
         return self.cols
 
-    def _vars(self, Mc: int, ld: int):
-        if self.vars is None or self.vars[0].shape[0] < Mc or self.vars[0].shape[1] != ld:
-            self.vars = [torch.empty((Mc, ld), dtype=F16, device=self.dev) for _ in range(4)] + \
+    def _vars(self, Mc: int, ldk: int):
+        if self.vars is None or self.vars[0].shape[0] < Mc or self.vars[0].shape[1] != ldk:
+            self.vars = [torch.empty((Mc, ldk), dtype=F16, device=self.dev) for _ in range(4)] + \
                         [torch.empty(Mc, dtype=F32, device=self.dev) for _ in range(2)]
         return self.vars
 
 
 def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: Tensor, n_real: int, rows: Tensor,
-              out: dict, max_F: Tensor, mark=None, done=None) -> None:
+              out: dict, max_F: Tensor, log_delta_min: float = -10.0, log_delta_max: float = 10.0, mark=None,
+              done=None) -> None:
+    """
+    Fused split-precision Wald of one chromosome (fasterlmm/core.py:601-671).  sWs is interpolated from R nodes in
+    log delta covering [log_delta_min, log_delta_max], which must contain every log delta in ``ld``.
+    """
     dev = s.device
     st = _stream(dev)
     Neff = s.shape[0]
     P = UYt.shape[0]
     Mc = USt.shape[0]
     ldk = _pad(Neff)
+    x0, R = interp_nodes(log_delta_min, log_delta_max)
+    ldr = _pad(R)
     s32 = torch.empty(Neff, dtype=F32, device=dev)
+    shat = torch.empty(1, dtype=F32, device=dev)
     _lib.call("flmm_convert_f64_f32", Neff, _ptr(s), _ptr(s32), st)
-    A1h, A1l, A2h, A2l, sa1, sa2, rWr = ops._cols(P, ldk)
-    _lib.call("flmm_wald_split_prep_columns", _ptr(s32), Neff, _ptr(UYt), UYt.stride(0), _ptr(ld), P, _ptr(A1h),
-              _ptr(A1l), _ptr(A2h), _ptr(A2l), ldk, _ptr(sa1), _ptr(sa2), _ptr(rWr), st)
+    _lib.call("flmm_mean_f32", _ptr(s), Neff, _ptr(shat), st)
+    A1h, A1l, Lh, Ll, sa1, sl, rWr = ops._cols(P, ldk, ldr)
+    _lib.call("flmm_wald_split_prep_columns", _ptr(s32), Neff, _ptr(UYt), UYt.stride(0), _ptr(ld), P, _ptr(shat),
+              float(x0), INTERP_H, R, _ptr(A1h), _ptr(A1l), ldk, _ptr(Lh), _ptr(Ll), ldr, _ptr(sa1), _ptr(sl),
+              _ptr(rWr), st)
     B1h, B1l, B2h, B2l, sb1, sb2 = ops._vars(Mc, ldk)
     _lib.call("flmm_wald_split_prep_variants", _ptr(USt), USt.stride(0), Mc, Neff, _ptr(B1h), _ptr(B1l), _ptr(B2h),
               _ptr(B2l), ldk, _ptr(sb1), _ptr(sb2), st)
+    # node values of sWs~: F (Mc, R) = (US o US) W~^T
+    W = torch.empty((R, Neff), dtype=F64, device=dev)
+    _lib.call("flmm_wald_interp_nodes", _ptr(s), Neff, _ptr(shat), float(x0), INTERP_H, R, _ptr(W), st)
+    Ws = SplitRows.of(W)
+    F = torch.empty((Mc, ldr), dtype=F32, device=dev)
+    us2 = SplitView(ops, (_ptr(B2h), _ptr(B2l), _ptr(sb2), ldk, Mc, Neff))
+    gemm_split(ctx, us2, Ws.view(), F[:, :R])
+    Fs = SplitRows.of(F[:, :R])
     slot = mark("wald") if mark else None
-    _lib.call("flmm_wald_split_f16", ctx, _ptr(A1h), _ptr(A1l), _ptr(A2h), _ptr(A2l), ldk, _ptr(sa1), _ptr(sa2),
-              _ptr(rWr), P, n_real, _ptr(B1h), _ptr(B1l), _ptr(B2h), _ptr(B2l), ldk, _ptr(sb1), _ptr(sb2), Mc, Neff,
-              _ptr(rows), _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]), _ptr(out["sfve"]), n_real,
-              _ptr(max_F), st)
+    _lib.call("flmm_wald_split_f16", ctx, _ptr(A1h), _ptr(A1l), ldk, _ptr(sa1), _ptr(Lh), _ptr(Ll), ldr, _ptr(sl),
+              _ptr(rWr), P, n_real, _ptr(B1h), _ptr(B1l), ldk, _ptr(sb1), _ptr(Fs.hi), _ptr(Fs.lo), Fs.ld,
+              _ptr(Fs.scale), Mc, Neff, R, _ptr(rows), _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]),
+              _ptr(out["sfve"]), n_real, _ptr(max_F), st)
     if done:
         done(slot)
     _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, st)
@@ -230,12 +267,21 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     ops = WaldOperands(dev)
     log_deltas = {}
     D = X.shape[1]
+    if N <= D:
+        raise ValueError(f"need more samples than covariate columns (N={N}, D={D})")
     Neff = N - D
     ldk = _pad(Neff)
+    # all projected LOCO kinships first, so their FP64 eigendecompositions run side by side
+    slot = mark("eigh")
+    Kp = torch.empty((len(units), N, N), dtype=F64, device=dev)
+    for k_idx, (c, _, _) in enumerate(units):
+        project_kinship(kin.kinship(c), basis, Kp[k_idx])
+    evals = eigh_batched(Kp, mode=EIGH_MODE)
+    done(slot)
     UYt = torch.empty((P, ldk), dtype=F32, device=dev)
     for k_idx, (c, a, n) in enumerate(units):
-        K = kin.kinship(c)
-        s, Ut = compat_eigh(K, basis)
+        s = compat_spectrum(evals[k_idx], D)
+        Ut = Kp[k_idx, D:]
         Us = SplitRows.of(Ut)
         gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
         ld, _ = fit_delta_fast(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
@@ -243,7 +289,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         USt = torch.empty((n, ldk), dtype=F32, device=dev)
         gemm_split(ctx, Zs.view(a, n), Us.view(), USt[:, :Neff])
         wald_fast(ctx, ops, s, UYt[:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,
-                  mark=mark, done=done)
+                  log_delta_min=log_delta_min, log_delta_max=log_delta_max, mark=mark, done=done)
         log_deltas[c if c is not None else 0] = ld
         if on_chrom is not None:
             on_chrom(k_idx + 1, len(units))

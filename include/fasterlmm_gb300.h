@@ -99,6 +99,13 @@ int flmm_project_kinship(const double* K, int64_t ldk, const double* Qx, int N, 
 int flmm_eigh_workspace_bytes(flmm_context* ctx, int N, size_t* bytes);
 int flmm_eigh(flmm_context* ctx, double* A, int N, double* evals, void* work, size_t work_bytes, void* stream);
 
+/* The same for `batch` independent matrices A (batch, N, N) contiguous, evals (batch, N): every LOCO kinship of a
+ * scan at once.  mode 1 = cusolverDnXsyevBatched, mode 2 = syevd calls run side by side on the context's worker
+ * streams, forked from and joined back into `stream`.  Workspace per mode from the query. */
+int flmm_eigh_batched_workspace_bytes(flmm_context* ctx, int N, int batch, int mode, size_t* bytes);
+int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, void* work,
+                      size_t work_bytes, void* stream);
+
 /* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514). */
 int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream);
 
@@ -194,23 +201,32 @@ int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu
                         double hi, int refine, double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
                         void* stream);
 
-/* Wald operands (fasterlmm/core.py:639-650).  Column side: w = 1 / (s + exp(log_delta[p])) from s32 (FP32 copy of
- * s), A1 = w o UY and A2 = w split per column, rWr[p] = max(sum w UY^2, 1e-300).  Variant side: B1 = US and
- * B2 = US o US split per variant. */
+/* Wald operands (fasterlmm/core.py:639-650).  All Wald outputs are unchanged when a column's weights w = 1/(s + delta)
+ * are scaled by a constant; the fast form uses w~ = (shat + delta) / (s + delta) with shat the mean eigenvalue
+ * (flmm_mean_f32).  Column side: A1 = w~ o UY split per column, rWr[p] = max(sum w~ UY^2, 1e-300), and the 10-point
+ * Lagrange weights L (R entries per column, split) of x = log_delta[p] on the nodes x0 + r h (r < R).  Node side:
+ * W~ (R, Neff) FP64 = (shat + e^{x_r}) / (s + e^{x_r}), to be split and multiplied into F = (US o US) W~^T, the node
+ * values of sWs~.  Variant side: B1 = US and B2 = US o US split per variant.  Column log deltas must lie in
+ * [x0 + 4h, x0 + (R - 6) h]. */
+int flmm_mean_f32(const double* x, int n, float* out, void* stream);
+int flmm_wald_interp_nodes(const double* s, int Neff, const float* shat, double x0, double h, int R, double* W,
+                           void* stream);
 int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu, const double* log_delta,
-                                 int P, void* A1h, void* A1l, void* A2h, void* A2l, int64_t lda, float* sa1,
-                                 float* sa2, float* rWr, void* stream);
+                                 int P, const float* shat, double x0, double h, int R, void* A1h, void* A1l,
+                                 int64_t lda, void* Lh, void* Ll, int64_t ldl, float* sa1, float* sl, float* rWr,
+                                 void* stream);
 int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Neff, void* B1h, void* B1l, void* B2h,
                                   void* B2l, int64_t ldb, float* sb1, float* sb2, void* stream);
 
-/* Fused split-precision Wald scan (fasterlmm/core.py:601-671): sWy = A1 B1^T and sWs = A2 B2^T on the tensor cores,
- * then in the epilogue beta, var_beta (df Neff - 1), F, SE, SFVE with the reference's clamps; real columns p < n_real
- * write out[rows[m] * ldo + p]; max_F[p] is raised to the column max. */
-int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, const void* A2h, const void* A2l,
-                        int64_t lda, const float* sa1, const float* sa2, const float* rWr, int P, int n_real,
-                        const void* B1h, const void* B1l, const void* B2h, const void* B2l, int64_t ldb,
-                        const float* sb1, const float* sb2, int Mc, int Neff, const int64_t* rows, double* f,
-                        double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
+/* Fused split-precision Wald scan (fasterlmm/core.py:601-671): sWy = A1 B1^T (K = Neff) and sWs~ = L F^T (K = R) on
+ * the tensor cores, then in the epilogue beta, var_beta (df Neff - 1), F, SE, SFVE with the reference's clamps (a
+ * variant with sWs = 0 gets the FP64 1e-300 clamp); real columns p < n_real write out[rows[m] * ldo + p]; max_F[p]
+ * is raised to the column max. */
+int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda, const float* sa1,
+                        const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr, int P,
+                        int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1, const void* Fh,
+                        const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff, int R, const int64_t* rows,
+                        double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
 
 /* Small conversions of the fast form: y[i] = (float)x[i]; y[i] += x[i] (FP32 into FP64); the LOCO kinship from an FP64
  * total and an FP32 chromosome Gram, K = (Gtot - Gc) / m_loco. */

@@ -91,7 +91,7 @@ def test_fast_wald_matches_plain_wald():
     core.wald_t(spec.s, spec.UYt, ld, USt, n_real, rows, out64, mF64)
     out32, mF32 = core._alloc_outputs(M, n_real, P, spec.s.device)
     wald_fast(_lib.context(0), WaldOperands(spec.s.device), spec.s, spec.UYt.float(), ld, USt.float(), n_real, rows,
-              out32, mF32)
+              out32, mF32, log_delta_min=-10.0, log_delta_max=10.0)
     _lib.call("flmm_context_check", _lib.context(0), None)
     for k in DETAIL:
         a, b = out32[k].cpu().numpy(), out64[k].cpu().numpy()
