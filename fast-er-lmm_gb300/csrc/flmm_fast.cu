@@ -64,6 +64,7 @@ struct TcArgs {
     const float* sa2;
     const float* sb2;
     const float* rWr;
+    const float* rWr0;  // rWr with the unscaled weights w = 1 / (s + delta), for the sWs = 0 clamp
     int n_real;
     float var_df;
     const int64_t* rows;
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                                 const int64_t o = args.rows[m] * args.ldo + p;
                                 args.f[o] = 0.0;
                                 args.beta[o] = 0.0;
-                                args.se[o] = sqrt(fmax(static_cast<double>(rwr), 1e-300) / args.var_df / 1e-300);
+                                args.se[o] = sqrt(fmax(static_cast<double>(args.rWr0[p]), 1e-300) / args.var_df / 1e-300);
                                 args.sfve[o] = 0.0;
                             }
                             continue;
@@ -354,7 +355,8 @@ __global__ void k_wald_prep_columns(const float* __restrict__ s32, int Neff, con
                                     int64_t ldu, const double* __restrict__ ld, int P, const float* __restrict__ shat_p,
                                     double x0, double h, int R, __half* __restrict__ A1h, __half* __restrict__ A1l,
                                     int64_t lda, __half* __restrict__ Lh, __half* __restrict__ Ll, int64_t ldl,
-                                    float* __restrict__ sa1, float* __restrict__ sl, float* __restrict__ rWr) {
+                                    float* __restrict__ sa1, float* __restrict__ sl, float* __restrict__ rWr,
+                                    float* __restrict__ rWr0) {
     const int lane = threadIdx.x & 31;
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
@@ -410,6 +412,7 @@ __global__ void k_wald_prep_columns(const float* __restrict__ s32, int Neff, con
         sa1[p] = ldexpf(1.0f, -e1);
         sl[p] = ldexpf(1.0f, -el);
         rWr[p] = static_cast<float>(fmax(acc, 1e-300));
+        rWr0[p] = static_cast<float>(fmax(acc / static_cast<double>(num), 1e-300));
     }
 }
 
@@ -572,14 +575,14 @@ extern "C" int flmm_wald_interp_nodes(const double* s, int Neff, const float* sh
 extern "C" int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu,
                                             const double* log_delta, int P, const float* shat, double x0, double h,
                                             int R, void* A1h, void* A1l, int64_t lda, void* Lh, void* Ll, int64_t ldl,
-                                            float* sa1, float* sl, float* rWr, void* stream) {
-    FLMM_REQUIRE(s32 && UYt && log_delta && shat && A1h && A1l && Lh && Ll && sa1 && sl && rWr && Neff > 0 &&
+                                            float* sa1, float* sl, float* rWr, float* rWr0, void* stream) {
+    FLMM_REQUIRE(s32 && UYt && log_delta && shat && A1h && A1l && Lh && Ll && sa1 && sl && rWr && rWr0 && Neff > 0 &&
                      ldu >= Neff && lda >= Neff && ldl >= R && R >= kInterpPoints && h > 0 && P >= 0,
                  "flmm_wald_split_prep_columns: bad arguments");
     if (P == 0) return FLMM_OK;
     k_wald_prep_columns<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, as_stream(stream)>>>(
         s32, Neff, UYt, ldu, log_delta, P, shat, x0, h, R, static_cast<__half*>(A1h), static_cast<__half*>(A1l), lda,
-        static_cast<__half*>(Lh), static_cast<__half*>(Ll), ldl, sa1, sl, rWr);
+        static_cast<__half*>(Lh), static_cast<__half*>(Ll), ldl, sa1, sl, rWr, rWr0);
     return check_launch("k_wald_prep_columns");
 }
 
@@ -597,11 +600,11 @@ extern "C" int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int
 
 extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda, const float* sa1,
                                    const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr,
-                                   int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1,
+                                   const float* rWr0, int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1,
                                    const void* Fh, const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff,
                                    int R, const int64_t* rows, double* f, double* beta, double* se, double* sfve,
                                    int64_t ldo, double* max_F, void* stream) {
-    FLMM_REQUIRE(ctx && A1h && A1l && sa1 && Lh && Ll && sl && rWr && B1h && B1l && sb1 && Fh && Fl && sf && max_F &&
+    FLMM_REQUIRE(ctx && A1h && A1l && sa1 && Lh && Ll && sl && rWr && rWr0 && B1h && B1l && sb1 && Fh && Fl && sf && max_F &&
                      Neff > 1 && R > 0 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
                      ldb >= Neff && ldl >= R && ldf >= R,
                  "flmm_wald_split_f16: bad arguments");
@@ -632,6 +635,7 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sa2 = sl;
     a.sb2 = sf;
     a.rWr = rWr;
+    a.rWr0 = rWr0;
     a.n_real = n_real;
     a.var_df = static_cast<float>(Neff - 1);
     a.rows = rows;

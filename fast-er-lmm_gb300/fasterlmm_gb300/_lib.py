@@ -61,9 +61,9 @@ SIGNATURES: dict[str, list] = {
     "flmm_mean_f32": [_p, _i, _p, _p],
     "flmm_wald_interp_nodes": [_p, _i, _p, _d, _d, _i, _p, _p],
     "flmm_wald_split_prep_columns": [_p, _i, _p, _i64, _p, _i, _p, _d, _d, _i, _p, _p, _i64, _p, _p, _i64, _p, _p,
-                                     _p, _p],
+                                     _p, _p, _p],
     "flmm_wald_split_prep_variants": [_p, _i64, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _p],
-    "flmm_wald_split_f16": [_p, _p, _p, _i64, _p, _p, _p, _i64, _p, _p, _i, _i, _p, _p, _i64, _p, _p, _p, _i64, _p,
+    "flmm_wald_split_f16": [_p, _p, _p, _i64, _p, _p, _p, _i64, _p, _p, _p, _i, _i, _p, _p, _i64, _p, _p, _p, _i64, _p,
                             _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, _p],
     "flmm_convert_f64_f32": [_i64, _p, _p, _p],
     "flmm_accumulate_f32_f64": [_i64, _p, _p, _p],

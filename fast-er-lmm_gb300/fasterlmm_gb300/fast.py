@@ -172,7 +172,7 @@ class WaldOperands:
         if c is None or c[0].shape[0] < P or c[0].shape[1] != ldk or c[2].shape[1] != ldr:
             self.cols = [torch.empty((P, ldk), dtype=F16, device=self.dev) for _ in range(2)] + \
                         [torch.empty((P, ldr), dtype=F16, device=self.dev) for _ in range(2)] + \
-                        [torch.empty(P, dtype=F32, device=self.dev) for _ in range(3)]
+                        [torch.empty(P, dtype=F32, device=self.dev) for _ in range(4)]
         return self.cols
 
     def _vars(self, Mc: int, ldk: int):
@@ -201,10 +201,10 @@ def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: T
     shat = torch.empty(1, dtype=F32, device=dev)
     _lib.call("flmm_convert_f64_f32", Neff, _ptr(s), _ptr(s32), st)
     _lib.call("flmm_mean_f32", _ptr(s), Neff, _ptr(shat), st)
-    A1h, A1l, Lh, Ll, sa1, sl, rWr = ops._cols(P, ldk, ldr)
+    A1h, A1l, Lh, Ll, sa1, sl, rWr, rWr0 = ops._cols(P, ldk, ldr)
     _lib.call("flmm_wald_split_prep_columns", _ptr(s32), Neff, _ptr(UYt), UYt.stride(0), _ptr(ld), P, _ptr(shat),
               float(x0), INTERP_H, R, _ptr(A1h), _ptr(A1l), ldk, _ptr(Lh), _ptr(Ll), ldr, _ptr(sa1), _ptr(sl),
-              _ptr(rWr), st)
+              _ptr(rWr), _ptr(rWr0), st)
     B1h, B1l, B2h, B2l, sb1, sb2 = ops._vars(Mc, ldk)
     _lib.call("flmm_wald_split_prep_variants", _ptr(USt), USt.stride(0), Mc, Neff, _ptr(B1h), _ptr(B1l), _ptr(B2h),
               _ptr(B2l), ldk, _ptr(sb1), _ptr(sb2), st)
@@ -218,7 +218,7 @@ def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: T
     Fs = SplitRows.of(F[:, :R])
     slot = mark("wald") if mark else None
     _lib.call("flmm_wald_split_f16", ctx, _ptr(A1h), _ptr(A1l), ldk, _ptr(sa1), _ptr(Lh), _ptr(Ll), ldr, _ptr(sl),
-              _ptr(rWr), P, n_real, _ptr(B1h), _ptr(B1l), ldk, _ptr(sb1), _ptr(Fs.hi), _ptr(Fs.lo), Fs.ld,
+              _ptr(rWr), _ptr(rWr0), P, n_real, _ptr(B1h), _ptr(B1l), ldk, _ptr(sb1), _ptr(Fs.hi), _ptr(Fs.lo), Fs.ld,
               _ptr(Fs.scale), Mc, Neff, R, _ptr(rows), _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]),
               _ptr(out["sfve"]), n_real, _ptr(max_F), st)
     if done:

@@ -206,7 +206,8 @@ int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu
  * (flmm_mean_f32).  Column side: A1 = w~ o UY split per column, rWr[p] = max(sum w~ UY^2, 1e-300), and the 10-point
  * Lagrange weights L (R entries per column, split) of x = log_delta[p] on the nodes x0 + r h (r < R).  Node side:
  * W~ (R, Neff) FP64 = (shat + e^{x_r}) / (s + e^{x_r}), to be split and multiplied into F = (US o US) W~^T, the node
- * values of sWs~.  Variant side: B1 = US and B2 = US o US split per variant.  Column log deltas must lie in
+ * values of sWs~; rWr0 receives the same sum with the unscaled weights.  Variant side: B1 = US and B2 = US o US split
+ * per variant.  Column log deltas must lie in
  * [x0 + 4h, x0 + (R - 6) h]. */
 int flmm_mean_f32(const double* x, int n, float* out, void* stream);
 int flmm_wald_interp_nodes(const double* s, int Neff, const float* shat, double x0, double h, int R, double* W,
@@ -214,7 +215,7 @@ int flmm_wald_interp_nodes(const double* s, int Neff, const float* shat, double 
 int flmm_wald_split_prep_columns(const float* s32, int Neff, const float* UYt, int64_t ldu, const double* log_delta,
                                  int P, const float* shat, double x0, double h, int R, void* A1h, void* A1l,
                                  int64_t lda, void* Lh, void* Ll, int64_t ldl, float* sa1, float* sl, float* rWr,
-                                 void* stream);
+                                 float* rWr0, void* stream);
 int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Neff, void* B1h, void* B1l, void* B2h,
                                   void* B2l, int64_t ldb, float* sb1, float* sb2, void* stream);
 
@@ -223,8 +224,8 @@ int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Ne
  * variant with sWs = 0 gets the FP64 1e-300 clamp); real columns p < n_real write out[rows[m] * ldo + p]; max_F[p]
  * is raised to the column max. */
 int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda, const float* sa1,
-                        const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr, int P,
-                        int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1, const void* Fh,
+                        const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr,
+                        const float* rWr0, int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1, const void* Fh,
                         const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff, int R, const int64_t* rows,
                         double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
 
