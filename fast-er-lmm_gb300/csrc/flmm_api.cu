@@ -223,9 +223,10 @@ extern "C" int flmm_eigh_batched_workspace_bytes(flmm_context* ctx, int N, int b
     return FLMM_OK;
 }
 
-extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, void* work,
-                                 size_t work_bytes, void* stream) {
-    FLMM_REQUIRE(ctx && A && evals && work && N > 0 && batch > 0, "flmm_eigh_batched: bad arguments");
+extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, int slot,
+                                 void* work, size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(ctx && A && evals && work && N > 0 && batch > 0 && slot >= -1 && slot < kEighWorkers,
+                 "flmm_eigh_batched: bad arguments");
     size_t need = 0;
     int rc = flmm_eigh_batched_workspace_bytes(ctx, N, batch, mode, &need);
     if (rc) return rc;
@@ -237,8 +238,9 @@ extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch,
         BatchedLayout L;
         if ((rc = batched_api_sizes(ctx, N, batch, &L))) return rc;
         int* info = reinterpret_cast<int*>(static_cast<char*>(work) + (L.dev_bytes - align_up(sizeof(int) * batch, 256)));
-        cusolverDnSetStream(ctx->solver, st);
-        cusolverStatus_t cs = cusolverDnXsyevBatched(ctx->solver, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
+        cusolverDnHandle_t hdl = slot < 0 ? ctx->solver : ctx->wsolver[slot];
+        cusolverDnSetStream(hdl, st);
+        cusolverStatus_t cs = cusolverDnXsyevBatched(hdl, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
                                                      CUBLAS_FILL_MODE_LOWER, N, CUDA_R_64F, A, N, CUDA_R_64F, evals,
                                                      CUDA_R_64F, work, L.dev_bytes, nullptr, 0, info, batch);
         if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail(cs, "cusolverDnXsyevBatched");
@@ -251,6 +253,7 @@ extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch,
     const int lwork = static_cast<int>((one - 256) / sizeof(double));
     FLMM_CUDA(cudaEventRecord(ctx->fork, st));
     for (int w = 0; w < slots; ++w) FLMM_CUDA(cudaStreamWaitEvent(ctx->workers[w], ctx->fork, 0));
+    for (int w = 0; w < slots; ++w) cusolverDnSetStream(ctx->wsolver[w], ctx->workers[w]);
     for (int b = 0; b < batch; ++b) {
         const int w = b % slots;
         char* wbase = static_cast<char*>(work) + one * static_cast<size_t>(w);

@@ -16,7 +16,66 @@ __global__ void k_neglog10p_f64(const double* __restrict__ F, int64_t n, double 
         out[i] = neglog10_fsf<double>(F[i], df2, lbeta);
 }
 
+// Genome-wide threshold per phenotype (fasterlmm/cli.py:128): p = P(F(1, df2) > perm_max_F) for the row's n_perm
+// permutation maxima, then numpy.quantile(p, q) with linear interpolation between order statistics.  p is
+// decreasing in F, so the ascending p order is the descending F order: the row is sorted once (bitonic, shared
+// memory) and only the two straddling order statistics are converted to p.  One block per phenotype.
+__global__ void k_perm_threshold(const double* __restrict__ pmax, int B, int n_perm, int npow2, double df2,
+                                 double lbeta, double q, double* __restrict__ thresh) {
+    extern __shared__ double v[];
+    const int b = blockIdx.x;
+    const double* row = pmax + static_cast<int64_t>(b) * n_perm;
+    for (int i = threadIdx.x; i < npow2; i += blockDim.x) v[i] = (i < n_perm) ? -row[i] : INFINITY;  // -F ascending
+    __syncthreads();
+    for (int size = 2; size <= npow2; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < npow2 / 2; i += blockDim.x) {
+                const int lo = 2 * i - (i & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const double a = v[lo], c = v[hi];
+                if ((a > c) == up) {
+                    v[lo] = c;
+                    v[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        // numpy's default ("linear"): position h = (n - 1) q, value = x[floor h] + (h - floor h)(x[floor h + 1] - x[floor h])
+        const double h = (n_perm - 1) * q;
+        const int j = static_cast<int>(floor(h));
+        const double frac = h - j;
+        const double p0 = exp(-neglog10_fsf<double>(-v[j], df2, lbeta) * 2.302585092994045684);
+        double out = p0;
+        if (frac > 0.0 && j + 1 < n_perm) {
+            const double p1 = exp(-neglog10_fsf<double>(-v[j + 1], df2, lbeta) * 2.302585092994045684);
+            out = p0 + frac * (p1 - p0);
+        }
+        thresh[b] = out;
+    }
+}
+
 }  // namespace
+
+extern "C" int flmm_perm_threshold_p(const double* perm_max_F, int B, int n_perm, int df2, double q, double* thresh,
+                                     void* stream) {
+    FLMM_REQUIRE((perm_max_F && thresh) || B == 0, "flmm_perm_threshold_p: NULL argument");
+    FLMM_REQUIRE(n_perm >= 1 && n_perm <= 16384 && df2 >= 1 && q >= 0.0 && q <= 1.0,
+                 "flmm_perm_threshold_p: need 1 <= n_perm <= 16384, df2 >= 1, 0 <= q <= 1");
+    if (B == 0) return FLMM_OK;
+    int npow2 = 1;
+    while (npow2 < n_perm) npow2 <<= 1;
+    const size_t smem = sizeof(double) * npow2;
+    if (smem > 48 * 1024)
+        FLMM_CUDA(cudaFuncSetAttribute(k_perm_threshold, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    const double a = 0.5 * df2;
+    const double lbeta = lgamma(a) + lgamma(0.5) - lgamma(a + 0.5);
+    k_perm_threshold<<<B, 256, smem, as_stream(stream)>>>(perm_max_F, B, n_perm, npow2, static_cast<double>(df2),
+                                                          lbeta, q, thresh);
+    return check_launch("k_perm_threshold");
+}
 
 extern "C" int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double* out, void* stream) {
     FLMM_REQUIRE((F && out) || n == 0, "flmm_neglog10_pvalue: NULL argument");

@@ -38,7 +38,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_eigh_workspace_bytes": [_p, _i, _psz],
     "flmm_eigh": [_p, _p, _i, _p, _p, _sz, _p],
     "flmm_eigh_batched_workspace_bytes": [_p, _i, _i, _i, _psz],
-    "flmm_eigh_batched": [_p, _p, _i, _i, _p, _i, _p, _sz, _p],
+    "flmm_eigh_batched": [_p, _p, _i, _i, _p, _i, _i, _p, _sz, _p],
     "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
     "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],
     "flmm_gemm_nt_f64": [_p, _i64, _p, _i64, _p, _i64, _i, _i, _i, _d, _p],
@@ -53,6 +53,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_perm_threshold_p": [_p, _i, _i, _i, _d, _p, _p],
     "flmm_context_check": [_p, _p],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],

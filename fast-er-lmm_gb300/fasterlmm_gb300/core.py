@@ -212,14 +212,25 @@ def project_kinship(K: Tensor, basis: CovariateBasis, out: Tensor) -> Tensor:
     return out
 
 
-def eigh_batched(A: Tensor, mode: int = 2) -> Tensor:
-    """In-place FP64 eigendecomposition of a (batch, N, N) stack: eigenvector rows overwrite A; returns evals."""
+def eigh_batched(A: Tensor, mode: int = 1, slot: int = -1, evals: Tensor | None = None,
+                 work: Tensor | None = None) -> Tensor:
+    """
+    In-place FP64 eigendecomposition of a (batch, N, N) stack on the current stream: eigenvector rows overwrite A;
+    returns evals (batch, N).  ``slot`` >= 0 uses a worker cuSOLVER handle and ``work`` a private workspace, for
+    batches that run on another stream next to work that uses the shared scratch buffer.
+    """
     dev = A.device
     batch, N, _ = A.shape
     ctx = _lib.context(dev.index)
-    evals = torch.empty((batch, N), dtype=F64, device=dev)
-    w, wb = _work.get(dev, _lib.query_bytes("flmm_eigh_batched_workspace_bytes", ctx, N, batch, mode))
-    _lib.call("flmm_eigh_batched", ctx, _ptr(A), N, batch, _ptr(evals), mode, w, wb, _stream(dev))
+    if evals is None:
+        evals = torch.empty((batch, N), dtype=F64, device=dev)
+    nbytes = _lib.query_bytes("flmm_eigh_batched_workspace_bytes", ctx, N, batch, mode)
+    if work is None:
+        w, wb = _work.get(dev, nbytes)
+    else:
+        assert work.numel() >= nbytes
+        w, wb = C.c_void_p(work.data_ptr()), work.numel()
+    _lib.call("flmm_eigh_batched", ctx, _ptr(A), N, batch, _ptr(evals), mode, slot, w, wb, _stream(dev))
     return evals
 
 

@@ -21,3 +21,22 @@ def neg_log10_pvalue(F: Tensor, df2: int) -> Tensor:
     out = torch.empty_like(Fd)
     _lib.call("flmm_neglog10_pvalue", _ptr(Fd), Fd.numel(), int(df2), _ptr(out), _stream(dev))
     return out if not isinstance(F, Tensor) or F.is_cuda else out.to(F.device)
+
+
+def perm_threshold_p(perm_max_F: Tensor, df2: int, q: float = 0.05) -> Tensor:
+    """
+    (B,) genome-wide p threshold per phenotype: the linear-interpolated q-quantile of P(F(1, df2) > perm_max_F[b])
+    over the row's permutations (fasterlmm/cli.py:128), as numpy.quantile(perm_min_p, q).
+    """
+    dev = _cuda_device(perm_max_F)
+    Fm = _f64(perm_max_F, dev)
+    B, n_perm = Fm.shape
+    out = torch.empty(B, dtype=F64, device=dev)
+    _lib.call("flmm_perm_threshold_p", _ptr(Fm), B, n_perm, int(df2), float(q), _ptr(out), _stream(dev))
+    return out if not isinstance(perm_max_F, Tensor) or perm_max_F.is_cuda else out.to(perm_max_F.device)
+
+
+def effect_size(beta: Tensor, g_var: Tensor, p_var: Tensor) -> Tensor:
+    """EffectSize = beta^2 var(g) / var(y) per (variant, phenotype) (fasterlmm/cli.py:131-132): elementwise on the
+    (M, B) beta with (M,) genotype and (B,) phenotype variances."""
+    return beta * beta * g_var[:, None] / p_var[None, :]

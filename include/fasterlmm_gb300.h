@@ -100,10 +100,11 @@ int flmm_eigh_workspace_bytes(flmm_context* ctx, int N, size_t* bytes);
 int flmm_eigh(flmm_context* ctx, double* A, int N, double* evals, void* work, size_t work_bytes, void* stream);
 
 /* The same for `batch` independent matrices A (batch, N, N) contiguous, evals (batch, N): every LOCO kinship of a
- * scan at once.  mode 1 = cusolverDnXsyevBatched, mode 2 = syevd calls run side by side on the context's worker
- * streams, forked from and joined back into `stream`.  Workspace per mode from the query. */
+ * scan at once.  mode 1 = cusolverDnXsyevBatched on the context's main solver handle (slot = -1) or on worker handle
+ * `slot` (0..7, so that batches on different streams never share a handle); mode 2 = syevd calls run side by side on
+ * the context's worker streams, forked from and joined back into `stream`.  Workspace per mode from the query. */
 int flmm_eigh_batched_workspace_bytes(flmm_context* ctx, int N, int batch, int mode, size_t* bytes);
-int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, void* work,
+int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, int slot, void* work,
                       size_t work_bytes, void* stream);
 
 /* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514). */
@@ -234,6 +235,11 @@ int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int
 int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
+
+/* Genome-wide permutation threshold per phenotype (fasterlmm/cli.py:128, :406): thresh[b] = numpy.quantile(p, q) with
+ * linear interpolation, p = P(F(1, df2) > perm_max_F[b, :]) over the row's n_perm permutation maxima (B, n_perm). */
+int flmm_perm_threshold_p(const double* perm_max_F, int B, int n_perm, int df2, double q, double* thresh,
+                          void* stream);
 
 #ifdef __cplusplus
 }

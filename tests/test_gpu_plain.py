@@ -203,3 +203,29 @@ def test_device_permutation_orders_are_bit_identical():
         dev_o = perms.perm_orders_device(N, cols, n_perm, seed, torch.device(DEV)).cpu().numpy()
         host_o = perms.perm_orders(N, cols, n_perm, seed)
         assert np.array_equal(dev_o, host_o), (N, list(cols)[:3], seed)
+
+
+def test_permutation_threshold_matches_numpy_quantile(golden):
+    """Device threshold = numpy.quantile(f.sf(perm_max_F, 1, df2), 0.05) per phenotype (the CLI's rule)."""
+    from fasterlmm_gb300 import post
+    g = golden("loco_n150_m1500")
+    N, D = g["X"].shape
+    thr = post.perm_threshold_p(torch.from_numpy(g["perm_max_F"]).to(DEV), N - D - 1).cpu().numpy()
+    np.testing.assert_allclose(thr, g["threshold"], rtol=1e-10, atol=0)
+    for q in (0.0, 0.5, 1.0, 0.123):
+        ref = [np.quantile(orc.f_sf(g["perm_max_F"][b], N - D - 1), q) for b in range(g["perm_max_F"].shape[0])]
+        got = post.perm_threshold_p(torch.from_numpy(g["perm_max_F"]).to(DEV), N - D - 1, q).cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=1e-10, atol=0)
+
+
+def test_grouped_driver_matches_golden(golden):
+    """The CLI-style grouped scan (one perm_threshold per NaN pattern, full-table seeds) on the reference's fixture."""
+    from fasterlmm_gb300.groups import perm_threshold_grouped
+    g = golden("na_groups")
+    data = _data(g["G"], g["X"], g["Y"], g["chrom"])
+    out = perm_threshold_grouped(data, list(range(g["Y"].shape[1])), n_perm=int(g["n_perm"]))
+    assert len(out) == int(g["n_groups"])
+    for gi, gr in enumerate(out):
+        assert gr.cols == g[f"g{gi}_cols"].tolist() and gr.df2 == len(gr.keep) - g["X"].shape[1] - 1
+        assert_scan_close(_np(gr.res), g, prefix=f"g{gi}_")
+        assert_scan_close({"perm_max_F": gr.perm_max_F.cpu().numpy()}, g, keys=("perm_max_F",), prefix=f"g{gi}_")

@@ -112,3 +112,16 @@ def test_oracle_na_groups(golden):
                                       n_perm=int(g["n_perm"]), seed_idx=cols)
         assert_scan_close(res, g, prefix=f"g{gi}_")
         assert_scan_close({"perm_max_F": pmf}, g, keys=("perm_max_F",), prefix=f"g{gi}_")
+
+
+def test_group_by_na_host_logic_matches_reference_groups(golden):
+    """The package's host grouping (no GPU needed) reproduces the reference's groups on its NA fixture."""
+    from fasterlmm_gb300.groups import group_by_na
+    g = golden("na_groups")
+    groups = group_by_na(g["Y"], list(range(g["Y"].shape[1])))
+    assert len(groups) == int(g["n_groups"])
+    for gi, (keep, cols) in enumerate(groups):
+        assert keep == g[f"g{gi}_keep"].tolist() and cols == g[f"g{gi}_cols"].tolist()
+    # all-NaN column -> empty keep rows; a column without NaN -> every row
+    Y = np.array([[1.0, np.nan], [2.0, np.nan], [3.0, np.nan]])
+    assert group_by_na(Y, [0, 1]) == [([0, 1, 2], [0]), ([], [1])]
