@@ -14,6 +14,8 @@
 // stationary point, well inside the FP64 noise of the reference's own search on flat likelihoods.
 #include <math.h>
 
+#include <mutex>
+
 #include "flmm_common.cuh"
 
 using namespace flmm;
@@ -318,6 +320,79 @@ extern "C" int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, 
     if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
     const size_t smem = sizeof(float) * static_cast<size_t>(Neff);
     if (smem > 48 * 1024) FLMM_CUDA(cudaFuncSetAttribute(k_newton_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, st>>>(s, Neff, UYt, ldu, P, grid,
+                                                                                    n_grid, grid_idx, refine, log_delta);
+    return check_launch("k_newton_refine");
+}
+
+// ---- allocation-free variant ------------------------------------------------------------------------------------
+//
+// Some callers cannot hand this library any device memory: a host whose device memory is entirely owned by another
+// memory pool (a framework that reserved all of it up front), or a call site in a latency-critical loop that may not
+// call cudaMalloc, which can synchronise the device and has no bounded latency.  flmm_fit_delta_fast_noalloc serves
+// them: its scratch (grid nodes, the (n_grid, Neff) weight table and the per-node log determinants) lives in the
+// fixed array below, which every GPU that loads this library holds until the process exits.
+//
+// The array is shared by every call of this entry point on a device and keeps the previous call's contents; each
+// call overwrites every byte it reads before reading it, so nothing has to start at zero.  Calls whose kernels
+// overlap on the GPU (other streams, other host threads) race on the array: serialise them.
+
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;  // 4 MiB: n_grid * Neff up to ~1.04 million
+static __device__ __align__(256) unsigned char g_fit_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_fit_scratch on the current device, looked up once per device.  In host code the array's name
+// is only a host-side stand-in, so the address must come from the runtime.
+int scratch_address(void** out) {
+    int dev = 0;
+    FLMM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(FLMM_ERR_DEVICE, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_fit_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(FLMM_ERR_CUDA, "cudaGetSymbolAddress(g_fit_scratch) on device %d: %s", dev,
+                        cudaGetErrorString(e));
+        g_scratch_addr[dev] = ptr;
+    }
+    *out = g_scratch_addr[dev];
+    return FLMM_OK;
+}
+
+}  // namespace
+
+extern "C" int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
+                                           double lo, double hi, int refine, double* log_delta, int32_t* grid_idx,
+                                           void* stream) {
+    FLMM_REQUIRE(s && UYt && log_delta && grid_idx && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
+                 "flmm_fit_delta_fast_noalloc: bad arguments");
+    FLMM_REQUIRE(Neff <= 12288, "flmm_fit_delta_fast_noalloc: Neff must be <= 12288 (shared-memory spectrum)");
+    const size_t need = fast_ws(Neff, n_grid);
+    if (need > kNoAllocScratchBytes)
+        return fail(FLMM_ERR_WORKSPACE,
+                    "flmm_fit_delta_fast_noalloc: n_grid * Neff = %lld needs %zu bytes of scratch, more than the fixed "
+                    "%zu; use flmm_fit_delta_fast with caller-provided workspace",
+                    static_cast<long long>(n_grid) * Neff, need, kNoAllocScratchBytes);
+    void* scratch = nullptr;
+    int rc = scratch_address(&scratch);
+    if (rc) return rc;
+    if (P == 0) return FLMM_OK;
+    cudaStream_t st = as_stream(stream);
+    double* grid = static_cast<double*>(scratch);
+    float* Wg = reinterpret_cast<float*>(grid + n_grid);
+    float* sum_log = Wg + static_cast<size_t>(n_grid) * Neff;
+    if ((rc = flmm_delta_grid_nodes(lo, hi, n_grid, grid, stream))) return rc;
+    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, grid, Wg, sum_log);
+    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
+    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
+    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
+    const size_t smem = sizeof(float) * static_cast<size_t>(Neff);
     k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, st>>>(s, Neff, UYt, ldu, P, grid,
                                                                                     n_grid, grid_idx, refine, log_delta);
     return check_launch("k_newton_refine");

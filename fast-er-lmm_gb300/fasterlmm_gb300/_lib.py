@@ -59,6 +59,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],
     "flmm_fit_delta_fast_workspace_bytes": [_i, _i, _psz],
     "flmm_fit_delta_fast": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
+    "flmm_fit_delta_fast_noalloc": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p],
     "flmm_mean_f32": [_p, _i, _p, _p],
     "flmm_wald_interp_nodes": [_p, _i, _p, _d, _d, _i, _p, _p],
     "flmm_wald_split_prep_columns": [_p, _i, _p, _i64, _p, _i, _p, _d, _d, _i, _p, _p, _i64, _p, _p, _i64, _p, _p,

@@ -202,6 +202,16 @@ int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu
                         double hi, int refine, double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
                         void* stream);
 
+/* flmm_fit_delta_fast without caller workspace.  No counterpart in the reference: it exists for callers that cannot
+ * give this library device memory -- a host whose device memory is all owned by another pool, or a latency-critical
+ * loop that may not call cudaMalloc (it can synchronise the device).  The scratch is a fixed 4 MiB device array in
+ * the library (held by every GPU that loads it until exit), so n_grid * Neff is limited to ~1.04 million; larger
+ * requests fail with FLMM_ERR_WORKSPACE.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream capture.  All calls share
+ * the array: calls whose kernels overlap on the GPU race and must be serialised by the caller.  Allocates nothing. */
+int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
+                                double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* stream);
+
 /* Wald operands (fasterlmm/core.py:639-650).  All Wald outputs are unchanged when a column's weights w = 1/(s + delta)
  * are scaled by a constant; the fast form uses w~ = (shat + delta) / (s + delta) with shat the mean eigenvalue
  * (flmm_mean_f32).  Column side: A1 = w~ o UY split per column, rWr[p] = max(sum w~ UY^2, 1e-300), and the 10-point
