@@ -30,9 +30,6 @@ F32 = torch.float32
 # how the per-chromosome FP64 eigendecompositions run: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on
 # worker streams (see flmm_eigh_batched)
 EIGH_MODE = 1
-# > 0: the eigendecompositions run in this many batches on a side stream, so that the tensor-core work of the
-# chromosomes already decomposed overlaps the FP64 work of the next batch
-EIGH_OVERLAP_CHUNKS = 0
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -279,37 +276,10 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     Kp = torch.empty((len(units), N, N), dtype=F64, device=dev)
     for k_idx, (c, _, _) in enumerate(units):
         project_kinship(kin.kinship(c), basis, Kp[k_idx])
-    n_chunks = min(EIGH_OVERLAP_CHUNKS, len(units)) if EIGH_MODE == 1 else 0
-    ready = None
-    if n_chunks > 1:
-        # fork: the side stream decomposes chunk after chunk; the main stream waits per chunk (join events)
-        evals = torch.empty((len(units), N), dtype=F64, device=dev)
-        main = torch.cuda.current_stream(dev)
-        side = torch.cuda.Stream(device=dev)
-        fork = torch.cuda.Event()
-        fork.record(main)
-        bounds = np.linspace(0, len(units), n_chunks + 1).astype(int)
-        ready = [None] * len(units)
-        with torch.cuda.stream(side):
-            side.wait_event(fork)
-            nbytes = _lib.query_bytes("flmm_eigh_batched_workspace_bytes", ctx, N, int(np.diff(bounds).max()), 1)
-            ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
-            for b0, b1 in zip(bounds[:-1], bounds[1:]):
-                eigh_batched(Kp[b0:b1], mode=1, slot=0, evals=evals[b0:b1], work=ws)
-                ev = torch.cuda.Event()
-                ev.record(side)
-                for u in range(b0, b1):
-                    ready[u] = ev
-        Kp.record_stream(side)
-        evals.record_stream(side)
-        ws.record_stream(side)
-    else:
-        evals = eigh_batched(Kp, mode=EIGH_MODE)
+    evals = eigh_batched(Kp, mode=EIGH_MODE)
     done(slot)
     UYt = torch.empty((P, ldk), dtype=F32, device=dev)
     for k_idx, (c, a, n) in enumerate(units):
-        if ready is not None:
-            torch.cuda.current_stream(dev).wait_event(ready[k_idx])
         s = compat_spectrum(evals[k_idx], D)
         Ut = Kp[k_idx, D:]
         Us = SplitRows.of(Ut)
