@@ -270,6 +270,56 @@ extern "C" int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch,
     return check_cuda("flmm_eigh_batched");
 }
 
+// ---- single-precision batched eigendecomposition (fast form) -----------------------------------------------------
+//
+// The fast form carries the eigenbasis as split-FP16 operands (~2^-22 relative) and its spectrum in FP32, so an FP32
+// eigendecomposition (backward error ~1e-7 of the projected kinship) is below the precision it is used at.
+
+namespace {
+
+int batched_api_sizes_f32(flmm_context* ctx, int N, int batch, BatchedLayout* L) {
+    size_t dbytes = 0, hbytes = 0;
+    cusolverStatus_t st = cusolverDnXsyevBatched_bufferSize(ctx->solver, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
+                                                            CUBLAS_FILL_MODE_LOWER, N, CUDA_R_32F, nullptr, N,
+                                                            CUDA_R_32F, nullptr, CUDA_R_32F, &dbytes, &hbytes, batch);
+    if (st != CUSOLVER_STATUS_SUCCESS) return solver_fail(st, "cusolverDnXsyevBatched_bufferSize (FP32)");
+    L->dev_bytes = align_up(dbytes, 256) + align_up(sizeof(int) * batch, 256);
+    L->host_bytes = hbytes;
+    return FLMM_OK;
+}
+
+}  // namespace
+
+extern "C" int flmm_eigh_batched_f32_workspace_bytes(flmm_context* ctx, int N, int batch, size_t* bytes) {
+    FLMM_REQUIRE(ctx && bytes && N > 0 && batch > 0, "flmm_eigh_batched_f32_workspace_bytes: bad arguments");
+    BatchedLayout L;
+    int rc = batched_api_sizes_f32(ctx, N, batch, &L);
+    if (rc) return rc;
+    if (L.host_bytes != 0)
+        return fail(FLMM_ERR_SOLVER, "cusolverDnXsyevBatched (FP32) needs %zu bytes of host workspace", L.host_bytes);
+    *bytes = L.dev_bytes;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* evals, void* work,
+                                     size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(ctx && A && evals && work && N > 0 && batch > 0, "flmm_eigh_batched_f32: bad arguments");
+    size_t need = 0;
+    int rc = flmm_eigh_batched_f32_workspace_bytes(ctx, N, batch, &need);
+    if (rc) return rc;
+    if (work_bytes < need)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_eigh_batched_f32: need %zu bytes, got %zu", need, work_bytes);
+    BatchedLayout L;
+    if ((rc = batched_api_sizes_f32(ctx, N, batch, &L))) return rc;
+    int* info = reinterpret_cast<int*>(static_cast<char*>(work) + (L.dev_bytes - align_up(sizeof(int) * batch, 256)));
+    cusolverDnSetStream(ctx->solver, as_stream(stream));
+    cusolverStatus_t cs = cusolverDnXsyevBatched(ctx->solver, ctx->params, CUSOLVER_EIG_MODE_VECTOR,
+                                                 CUBLAS_FILL_MODE_LOWER, N, CUDA_R_32F, A, N, CUDA_R_32F, evals,
+                                                 CUDA_R_32F, work, L.dev_bytes, nullptr, 0, info, batch);
+    if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail(cs, "cusolverDnXsyevBatched (FP32)");
+    return check_cuda("cusolverDnXsyevBatched (FP32)");
+}
+
 // ---- covariate basis (thin SVD of X) --------------------------------------------------------------------------
 
 namespace {

@@ -47,6 +47,35 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// Neumaier-compensated running sum: comp collects the rounding error of every addition, so sum + comp is the sum of
+// the added terms without the accumulated FP32 rounding
+__device__ __forceinline__ void neumaier(float& sum, float& comp, float x) {
+    const float t = sum + x;
+    comp += (fabsf(sum) >= fabsf(x)) ? ((sum - t) + x) : ((x - t) + sum);
+    sum = t;
+}
+
+// exact sum and error of a + b (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// warp-wide sum of a compensated pair (hi + lo), TwoSum at every level of the butterfly
+__device__ __forceinline__ float warp_sum_pair(float hi, float lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        float sum, err;
+        two_sum(hi, oh, sum, err);
+        hi = sum;
+        lo = lo + ol + err;
+    }
+    return hi + lo;
+}
+
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

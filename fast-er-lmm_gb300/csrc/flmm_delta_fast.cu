@@ -8,10 +8,10 @@
 //     dL/dx = delta (T1 - Neff S2 / S1),  d/dx (T1 - Neff S2 / S1) = delta (-T2 + Neff (2 S3 / S1 - S2^2 / S1^2)),
 // and a sign-safeguarded Newton iteration on g = T1 - Neff S2 / S1 keeps g(lo) < 0 < g(hi), so it always converges
 // to a local minimum of the loss in the bracket (never a maximum).  When g does not change sign the minimum is a
-// bracket edge, which is where the golden-section search converges as well.  S1, S2, T1 are accumulated with
-// Neumaier-compensated FP32 sums and combined across lanes in FP64, so g is accurate to the rounding of the
-// individual terms (~1e-7 relative each, averaging out over Neff); log delta comes out within ~1e-7 of the exact
-// stationary point, well inside the FP64 noise of the reference's own search on flat likelihoods.
+// bracket edge, which is where the golden-section search converges as well.  The sums are accumulated in FP32 in a
+// centred form (newton_eval) with Neumaier compensation and combined across lanes with TwoSum, so g is accurate to
+// the rounding of the individual terms (~1e-7 relative each, averaging out over Neff); log delta comes out within
+// ~1e-7 of the exact stationary point, well inside the FP64 noise of the reference's own search on flat likelihoods.
 #include <math.h>
 
 #include <mutex>
@@ -123,33 +123,6 @@ struct NewtonEval {
     double loss;   // Neff log S1 + sum log (s + delta), up to constants
 };
 
-__device__ __forceinline__ void neumaier(float& sum, float& comp, float x) {
-    const float t = sum + x;
-    comp += (fabsf(sum) >= fabsf(x)) ? ((sum - t) + x) : ((x - t) + sum);
-    sum = t;
-}
-
-// exact sum and error of a + b (Knuth's TwoSum)
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-// warp-wide sum of a compensated pair (hi + lo), TwoSum at every level of the butterfly
-__device__ __forceinline__ float warp_sum_pair(float hi, float lo) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
-        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
-        float sum, err;
-        two_sum(hi, oh, sum, err);
-        hi = sum;
-        lo = lo + ol + err;
-    }
-    return hi + lo;
-}
-
 // One evaluation by a warp at x = log delta (x is warp-uniform), all in FP32.
 //
 // g is formed around the centre c = 1 / (sbar + delta), sbar the mean eigenvalue: with d_n = r_n - c =
@@ -169,7 +142,7 @@ __device__ NewtonEval newton_eval(const float* __restrict__ s32, float sbar, con
     float d1 = 0.f, cd1 = 0.f, e1 = 0.f, ce1 = 0.f, e2 = 0.f, e3 = 0.f, f2 = 0.f, uu_s = 0.f, cu = 0.f, sl = 0.f;
     for (int n = lane; n < Neff; n += 32) {
         const float sd = s32[n] + delta;
-        const float r = 1.0f / sd;
+        const float r = __frcp_rn(sd);  // correctly rounded, cheaper than the IEEE division
         const float d = (sbar - s32[n]) * r * c;
         const float uu = u[n] * u[n];
         neumaier(d1, cd1, d);
@@ -207,6 +180,25 @@ __device__ NewtonEval newton_eval(const float* __restrict__ s32, float sbar, con
     return e;
 }
 
+// Safeguarded Newton on g in a bracket with g(lo) < 0 < g(hi), starting at x0 (the bracket's midpoint if x0 is not
+// inside).  The FP32 sums put a noise floor of ~1e-7 on x: near the root the Newton steps stop shrinking and jump
+// around the root by that much, so the iteration ends once a step or the bracket is below 1e-7.
+__device__ double newton_in_bracket(const float* __restrict__ s32, float sbar, const float* __restrict__ u, int Neff,
+                                   double lo, double hi, double x0) {
+    double x = (x0 > lo && x0 < hi) ? x0 : 0.5 * (lo + hi);
+    for (int it = 0; it < 60; ++it) {
+        const NewtonEval e = newton_eval(s32, sbar, u, Neff, x, false);
+        if (e.g == 0.0) break;
+        if (e.g < 0.0) lo = x; else hi = x;
+        double xn = x - e.g / e.gp;
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const double stepx = fabs(xn - x);
+        x = xn;
+        if (stepx < 1e-7 || hi - lo < 1e-7) break;
+    }
+    return x;
+}
+
 __global__ void k_newton_refine(const double* __restrict__ s, int Neff, const float* __restrict__ UYt, int64_t ldu,
                                 int P, const double* __restrict__ grid, int G, const int32_t* __restrict__ idx,
                                 int refine, double* __restrict__ log_delta) {
@@ -226,8 +218,17 @@ __global__ void k_newton_refine(const double* __restrict__ s, int Neff, const fl
     if (p >= P) return;
     int i = idx[p];
     double out = grid[i];
-    if (refine && G > 1) {
-        const float* u = UYt + p * ldu;
+    const float* u = UYt + p * ldu;
+    bool refined = false;
+    if (refine && i > 0 && i < G - 1) {
+        // the usual case: d loss / d log delta changes sign between the argmin's neighbours
+        const double a = grid[i - 1], b = grid[i + 1];
+        if (newton_eval(s32, sbar, u, Neff, a, false).g < 0.0 && newton_eval(s32, sbar, u, Neff, b, false).g > 0.0) {
+            out = newton_in_bracket(s32, sbar, u, Neff, a, b, grid[i]);
+            refined = true;
+        }
+    }
+    if (refine && G > 1 && !refined) {
         // The FP32 grid argmin is only as good as the FP32 loss (~1e-4 absolute); on flat losses it can sit several
         // nodes from the minimum.  The exact derivative sign at that node says which side the minimum is on, and a
         // binary search over the grid nodes on that side finds where d loss / d log delta changes sign, so the
@@ -269,19 +270,7 @@ __global__ void k_newton_refine(const double* __restrict__ s, int Neff, const fl
         } else if (eb.g <= 0.0) {
             out = b;
         } else {
-            double lo = a, hi = b;
-            double x = (grid[i] > lo && grid[i] < hi) ? grid[i] : 0.5 * (lo + hi);
-            for (int it = 0; it < 60; ++it) {
-                const NewtonEval e = newton_eval(s32, sbar, u, Neff, x, false);
-                if (e.g == 0.0) break;
-                if (e.g < 0.0) lo = x; else hi = x;
-                double xn = x - e.g / e.gp;
-                if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
-                const double stepx = fabs(xn - x);
-                x = xn;
-                if (stepx < 1e-10 || hi - lo < 1e-10) break;
-            }
-            out = x;
+            out = newton_in_bracket(s32, sbar, u, Neff, a, b, grid[i]);
         }
     }
     if (lane == 0) log_delta[p] = out;

@@ -11,9 +11,9 @@
 //           and the per-chromosome Gram (fasterlmm/io.py:264);
 //   NG = 2: the Wald scan (fasterlmm/core.py:649-667): sWy = (w o UY) US^T and sWs = w (US o US)^T accumulated
 //           side by side, with beta, var_beta, F, SE, SFVE and the per-column genome max computed in the epilogue.
-// Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, warps 2-5 run the epilogue
-// (warp w reads TMEM lanes 32 (w % 4) .. +31).  Shared memory holds 3 stages of operand tiles; tensor memory holds
-// two accumulator sets so the epilogue of one tile overlaps the MMAs of the next.
+// Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, warps 2-9 run the epilogue
+// (warp w reads TMEM lanes 32 (w % 4) .. +31, half of the tile's columns).  Shared memory holds 192 KB of operand
+// stages; tensor memory holds two accumulator sets so the epilogue of one tile overlaps the MMAs of the next.
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 #include <math.h>
@@ -31,13 +31,15 @@ namespace {
 
 constexpr int kBM = 128;  // A rows per tile (TMEM lanes)
 constexpr int kBN = 128;  // B rows per tile (accumulator columns)
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;        // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int kEpilogueThreads = 256;
+constexpr int kBK = 64;  // reduction depth of one pipeline stage: 64 gives 3 stages of 64 KB, 32 gives 6 of 32 KB
 
 template <int NG, int BK>
 struct Cfg {
     static constexpr int kTileBytes = 128 * BK * 2;
     static constexpr int kStageBytes = 4 * kTileBytes;  // A hi, A lo, B hi, B lo of one product
-    static constexpr int kStages = 3;
+    static constexpr int kStages = (BK == 32) ? 6 : 3;   // 192 KB of operand stages either way
     static constexpr uint32_t kSwizzle = (BK == 64) ? 2u : 4u;  // 128-byte / 64-byte swizzle
     static constexpr uint32_t kSBO = 8u * BK * 2u;             // bytes between 8-row groups
     static constexpr int kTmemCols = NG * kBN * 2;
@@ -76,6 +78,31 @@ struct TcArgs {
     double* max_F;
 };
 
+// 16 consecutive row scales (fewer than 16 valid: the rest read as 0); all lanes of a warp read the same addresses
+__device__ __forceinline__ void load16(const float* __restrict__ p, int n, float (&v)[16]) {
+    if (n >= 16 && (reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+        const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 x = __ldg(p4 + k);
+            v[4 * k] = x.x;
+            v[4 * k + 1] = x.y;
+            v[4 * k + 2] = x.z;
+            v[4 * k + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = k < n ? __ldg(p + k) : 0.0f;
+    }
+}
+
+// hardware reciprocal (relative error ~2^-23); arguments here are clamped to normal numbers
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 template <int NG, int BK>
 __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMaps maps, const TcArgs args) {
     using C = Cfg<NG, BK>;
@@ -105,7 +132,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 128);
+            mbar_init(&acc_empty[b], kEpilogueThreads);
         }
         mbar_init(final_bar, 1);
         fence_barrier_init();
@@ -192,8 +219,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             mbar_drain(final_bar, 0);
         }
     } else {
-        // ---- epilogue: warps 2..5, thread = one accumulator row ----
+        // ---- epilogue: warps 2..9.  Warp w reads TMEM lanes 32 (w % 4) .. +31 (thread = one accumulator row) and
+        // half (w - 2) / 4 of the tile's columns, so two warps share each lane quarter.
         const int q = warp & 3;
+        const int cbeg = ((warp - 2) >> 2) * (kBN / 2);
         const int r = q * 32 + lane;
         int ab = 0;
         uint32_t aphase = 0;
@@ -204,69 +233,86 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
             const int i = ta * kBM + r;  // A row
             const bool row_ok = i < args.Mr;
+            const int nvalid = min(kBN, args.Nr - tb * kBN);  // columns of this tile inside B
             if constexpr (NG == 1) {
                 const float sa = row_ok ? args.sa[i] : 0.0f;
-                for (int c0 = 0; c0 < kBN; c0 += 16) {
-                    float v[16];
+                float* crow = args.C + static_cast<int64_t>(i) * args.ldc + tb * kBN;
+                for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
+                    float v[16], sbv[16];
+                    load16(args.sb + tb * kBN + c0, nvalid - c0, sbv);
                     tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
                     if (!row_ok) continue;
-                    float* crow = args.C + static_cast<int64_t>(i) * args.ldc;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int col = tb * kBN + c0 + j;
-                        if (col < args.Nr) {
-                            const float x = v[j] * sa * args.sb[col];
-                            crow[col] = args.accumulate ? crow[col] + x : x;
+                        if (c0 + j < nvalid) {
+                            const float x = v[j] * sa * sbv[j];
+                            crow[c0 + j] = args.accumulate ? crow[c0 + j] + x : x;
                         }
                     }
                 }
             } else {
-                // Wald statistics, the reference's formulas (fasterlmm/core.py:651-667) in FP32 on unscaled sums
+                // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each
+                // test needs two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
+                //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
                 const int p = i;
                 const float sa1 = row_ok ? args.sa[p] : 0.0f;
                 const float sa2 = row_ok ? args.sa2[p] : 0.0f;
                 const float rwr = row_ok ? args.rWr[p] : 1.0f;
+                const float df = args.var_df;
+                const bool real_tile = ta * kBM < args.n_real;  // uniform over the CTA
                 const bool real = row_ok && p < args.n_real;
                 float colmax = -INFINITY;
                 bool col_nan = false;
-                for (int c0 = 0; c0 < kBN; c0 += 16) {
-                    float vy[16], vs[16];
+                for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
+                    float vy[16], vs[16], sbv[16], sb2v[16];
+                    load16(args.sb + tb * kBN + c0, nvalid - c0, sbv);
+                    load16(args.sb2 + tb * kBN + c0, nvalid - c0, sb2v);
                     tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
                     if (!row_ok) continue;
+                    if (!real_tile) {
+                        // permutation columns: F and the column maximum only
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float swy = vy[j] * sa1 * sbv[j];
+                            const float sws = vs[j] * sa2 * sb2v[j];
+                            const float qv = swy * swy * rcp_approx(fmaxf(sws, 1e-30f));
+                            float F = qv * df * rcp_approx(fmaxf(rwr - qv, 1e-30f));
+                            F = (sws > 0.0f) ? F : 0.0f;  // no variance left: the reference's clamp gives F = 0
+                            F = (c0 + j < nvalid) ? F : -INFINITY;
+                            colmax = fmaxf(colmax, F);
+                            col_nan |= (F != F);
+                        }
+                        continue;
+                    }
+                    const float inv_df = 1.0f / df;
+                    const float inv_rwr = 1.0f / rwr;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int m = tb * kBN + c0 + j;
-                        if (m >= args.Nr) continue;
-                        const float swy = vy[j] * sa1 * args.sb[m];
-                        const float sws = vs[j] * sa2 * args.sb2[m];
-                        if (!(sws > 0.0f)) {
+                        if (c0 + j >= nvalid) continue;
+                        const float swy = vy[j] * sa1 * sbv[j];
+                        const float sws = vs[j] * sa2 * sb2v[j];
+                        const float inv_d = rcp_approx(fmaxf(sws, 1e-30f));
+                        const float qv = swy * swy * inv_d;
+                        const float rss = fmaxf(rwr - qv, 1e-30f);
+                        const bool var_ok = sws > 0.0f;
+                        const float F = var_ok ? qv * df * rcp_approx(rss) : 0.0f;
+                        colmax = fmaxf(colmax, F);
+                        col_nan |= (F != F);
+                        if (!real) continue;
+                        const int64_t o = args.rows[m] * args.ldo + p;
+                        if (var_ok) {
+                            args.f[o] = F;
+                            args.beta[o] = swy * inv_d;
+                            args.se[o] = sqrtf(rss * inv_d * inv_df);
+                            args.sfve[o] = sqrtf(fmaxf(qv * inv_rwr, 0.0f));
+                        } else {
                             // a variant with no variance left (e.g. monomorphic): the reference clamps sWs to 1e-300
                             // in FP64, which gives beta = F = SFVE = 0 and SE = sqrt(rWr / df / 1e-300)
-                            colmax = fmaxf(colmax, 0.0f);
-                            if (real) {
-                                const int64_t o = args.rows[m] * args.ldo + p;
-                                args.f[o] = 0.0;
-                                args.beta[o] = 0.0;
-                                args.se[o] = sqrt(fmax(static_cast<double>(args.rWr0[p]), 1e-300) / args.var_df / 1e-300);
-                                args.sfve[o] = 0.0;
-                            }
-                            continue;
-                        }
-                        const float denom = fmaxf(sws, 1e-30f);
-                        const float inv_d = 1.0f / denom;
-                        const float b = swy * inv_d;
-                        const float qq = swy * swy;
-                        const float rss = fmaxf(rwr - qq * inv_d, 1e-30f);
-                        const float var_b = rss / args.var_df * inv_d;
-                        const float F = b * b / var_b;
-                        colmax = fmaxf(colmax, F);
-                        col_nan |= isnan(F);
-                        if (real) {
-                            const int64_t o = args.rows[m] * args.ldo + p;
-                            args.f[o] = F;
-                            args.beta[o] = b;
-                            args.se[o] = sqrtf(var_b);
-                            args.sfve[o] = sqrtf(fmaxf(qq * inv_d / rwr, 0.0f));
+                            args.f[o] = 0.0;
+                            args.beta[o] = 0.0;
+                            args.se[o] = sqrt(fmax(static_cast<double>(args.rWr0[p]), 1e-300) / args.var_df / 1e-300);
+                            args.sfve[o] = 0.0;
                         }
                     }
                 }
@@ -349,70 +395,80 @@ __global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int
 constexpr int kInterpPoints = 10;
 
 // Wald column side (fasterlmm/core.py:639-643): w~ = (shat + delta_p) / (s + delta_p), A1 = w~ o UY split,
-// rWr = sum w~ UY^2 (FP64 accumulation), and the column's Lagrange weights L (R entries, 10 non-zero) split.  One
-// warp per column p.
-__global__ void k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __restrict__ UYt,
-                                    int64_t ldu, const double* __restrict__ ld, int P, const float* __restrict__ shat_p,
-                                    double x0, double h, int R, __half* __restrict__ A1h, __half* __restrict__ A1l,
-                                    int64_t lda, __half* __restrict__ Lh, __half* __restrict__ Ll, int64_t ldl,
-                                    float* __restrict__ sa1, float* __restrict__ sl, float* __restrict__ rWr,
-                                    float* __restrict__ rWr0) {
-    const int lane = threadIdx.x & 31;
-    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+// rWr = sum w~ UY^2, and the column's Lagrange weights L (R entries, 10 non-zero) split.  A block of kPrepCols warps
+// handles kPrepCols columns.  GB300's FP64 rate is ~1/60 of its FP32 rate, so FP64 is kept off the per-element
+// path: the Lagrange weights (FP64 products, one division each) are formed by ten threads per column before the
+// warps start, delta = exp(x) comes from a hi / lo split of x in FP32, and rWr is a compensated FP32 sum.
+constexpr int kPrepCols = 8;
+
+__global__ void __launch_bounds__(32 * kPrepCols)
+k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __restrict__ UYt, int64_t ldu,
+                    const double* __restrict__ ld, int P, const float* __restrict__ shat_p, double x0, double h,
+                    double inv_h, int R, __half* __restrict__ A1h, __half* __restrict__ A1l, int64_t lda,
+                    __half* __restrict__ Lh, __half* __restrict__ Ll, int64_t ldl, float* __restrict__ sa1,
+                    float* __restrict__ sl, float* __restrict__ rWr, float* __restrict__ rWr0) {
+    __shared__ float lw[kPrepCols][kInterpPoints];
+    __shared__ int lbase[kPrepCols];
+    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * kPrepCols;
+    // Lagrange weights on nodes base .. base + 9 around x: w_k = prod_{m != k} (t - m) / prod_{m != k} (k - m)
+    if (threadIdx.x < kPrepCols * kInterpPoints) {
+        const int j = threadIdx.x / kInterpPoints, k = threadIdx.x % kInterpPoints;
+        const int64_t p = p0 + j;
+        if (p < P) {
+            const double x = ld[p];
+            int base = static_cast<int>(floor((x - x0) * inv_h)) - (kInterpPoints / 2 - 1);
+            base = max(0, min(base, R - kInterpPoints));
+            const double t = (x - (x0 + base * h)) * inv_h;
+            double num = 1.0, den = 1.0;
+#pragma unroll
+            for (int m = 0; m < kInterpPoints; ++m) {
+                if (m == k) continue;
+                num *= t - m;
+                den *= static_cast<double>(k - m);  // integer products up to 9!, exact
+            }
+            lw[j][k] = static_cast<float>(num / den);
+            if (k == 0) lbase[j] = base;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+    const int64_t p = p0 + j;
     if (p >= P) return;
     const double x = ld[p];
-    const float delta = static_cast<float>(exp(x));
+    const float xh = static_cast<float>(x);
+    const float xl = static_cast<float>(x - static_cast<double>(xh));
+    const float delta = expf(xh) * (1.0f + xl);
     const float num = *shat_p + delta;
     const float* u = UYt + p * ldu;
-    float m1 = 0.0f;
-    double acc = 0.0;
+    float m1 = 0.0f, acc = 0.0f, comp = 0.0f;
     for (int n = lane; n < Neff; n += 32) {
-        const float w = num / (s32[n] + delta);
-        const float a = w * u[n];
+        const float un = u[n];
+        const float a = (num / (s32[n] + delta)) * un;
         m1 = fmaxf(m1, fabsf(a));
-        acc += static_cast<double>(a) * static_cast<double>(u[n]);
+        neumaier(acc, comp, a * un);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-    acc = warp_sum(acc);
+    const float rwr = warp_sum_pair(acc, comp);
     int e1;
     const float mul1 = row_scale_exp(m1, &e1);
     for (int n = lane; n < Neff; n += 32) split_store((num / (s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
-    // Lagrange weights on nodes base .. base + 9 around x; lane k < 10 owns weight k
-    int base = static_cast<int>(floor((x - x0) / h)) - (kInterpPoints / 2 - 1);
-    base = max(0, min(base, R - kInterpPoints));
-    const double t = (x - (x0 + base * h)) / h;
-    double wk = 0.0;
-    if (lane < kInterpPoints) {
-        wk = 1.0;
-        for (int m = 0; m < kInterpPoints; ++m)
-            if (m != lane) wk *= (t - m) / static_cast<double>(lane - m);
-    }
-    float lm = fabsf(static_cast<float>(wk));
+    const int base = lbase[j];
+    float lm = 0.0f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lm = fmaxf(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    for (int k = 0; k < kInterpPoints; ++k) lm = fmaxf(lm, fabsf(lw[j][k]));
     int el;
     const float mull = row_scale_exp(lm, &el);
-    // every lane writes its own entries of the row; the ten weights come from lanes 0..9 by shuffle
-    double wv[kInterpPoints];
-#pragma unroll
-    for (int k = 0; k < kInterpPoints; ++k) wv[k] = __shfl_sync(0xffffffffu, wk, k);
     for (int r = lane; r < R; r += 32) {
         const int k = r - base;
-        double v = 0.0;
-#pragma unroll
-        for (int kk = 0; kk < kInterpPoints; ++kk)
-            if (kk == k) v = wv[kk];
-        const double vs = v * static_cast<double>(mull);
-        const __half hh = __double2half(vs);
-        Lh[p * ldl + r] = hh;
-        Ll[p * ldl + r] = __double2half(vs - static_cast<double>(__half2float(hh)));
+        const float v = (k >= 0 && k < kInterpPoints) ? lw[j][k] : 0.0f;
+        split_store(v, mull, Lh, Ll, p * ldl + r);
     }
     if (lane == 0) {
         sa1[p] = ldexpf(1.0f, -e1);
         sl[p] = ldexpf(1.0f, -el);
-        rWr[p] = static_cast<float>(fmax(acc, 1e-300));
-        rWr0[p] = static_cast<float>(fmax(acc / static_cast<double>(num), 1e-300));
+        rWr[p] = fmaxf(rwr, 0.0f);
+        rWr0[p] = fmaxf(rwr, 0.0f) / num;  // 0 for an all-zero column: the epilogue applies the reference's floor
     }
 }
 
@@ -540,10 +596,10 @@ extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void
     TcMaps maps;
     std::memset(&maps, 0, sizeof(maps));
     int rc;
-    if ((rc = make_map(&maps.m[0], Ah, Mr, K, lda, 64))) return rc;
-    if ((rc = make_map(&maps.m[1], Al, Mr, K, lda, 64))) return rc;
-    if ((rc = make_map(&maps.m[2], Bh, Nr, K, ldb, 64))) return rc;
-    if ((rc = make_map(&maps.m[3], Bl, Nr, K, ldb, 64))) return rc;
+    if ((rc = make_map(&maps.m[0], Ah, Mr, K, lda, kBK))) return rc;
+    if ((rc = make_map(&maps.m[1], Al, Mr, K, lda, kBK))) return rc;
+    if ((rc = make_map(&maps.m[2], Bh, Nr, K, ldb, kBK))) return rc;
+    if ((rc = make_map(&maps.m[3], Bl, Nr, K, ldb, kBK))) return rc;
     TcArgs a;
     std::memset(&a, 0, sizeof(a));
     a.Mr = Mr;
@@ -555,7 +611,7 @@ extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void
     a.C = Cout;
     a.ldc = ldc;
     a.accumulate = accumulate;
-    return launch_tc<1, 64>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+    return launch_tc<1, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }
 
 extern "C" int flmm_mean_f32(const double* x, int n, float* out, void* stream) {
@@ -580,8 +636,8 @@ extern "C" int flmm_wald_split_prep_columns(const float* s32, int Neff, const fl
                      ldu >= Neff && lda >= Neff && ldl >= R && R >= kInterpPoints && h > 0 && P >= 0,
                  "flmm_wald_split_prep_columns: bad arguments");
     if (P == 0) return FLMM_OK;
-    k_wald_prep_columns<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, as_stream(stream)>>>(
-        s32, Neff, UYt, ldu, log_delta, P, shat, x0, h, R, static_cast<__half*>(A1h), static_cast<__half*>(A1l), lda,
+    k_wald_prep_columns<<<ceil_div(P, kPrepCols), 32 * kPrepCols, 0, as_stream(stream)>>>(
+        s32, Neff, UYt, ldu, log_delta, P, shat, x0, h, 1.0 / h, R, static_cast<__half*>(A1h), static_cast<__half*>(A1l), lda,
         static_cast<__half*>(Lh), static_cast<__half*>(Ll), ldl, sa1, sl, rWr, rWr0);
     return check_launch("k_wald_prep_columns");
 }
@@ -615,14 +671,14 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     std::memset(&maps, 0, sizeof(maps));
     int rc;
     // product 0: sWy = (w~ o UY) US^T over K = Neff; product 1: sWs~ = L F^T over K = R
-    if ((rc = make_map(&maps.m[0], A1h, P, Neff, lda, 64))) return rc;
-    if ((rc = make_map(&maps.m[1], A1l, P, Neff, lda, 64))) return rc;
-    if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, 64))) return rc;
-    if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, 64))) return rc;
-    if ((rc = make_map(&maps.m[4], Lh, P, R, ldl, 64))) return rc;
-    if ((rc = make_map(&maps.m[5], Ll, P, R, ldl, 64))) return rc;
-    if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, 64))) return rc;
-    if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, 64))) return rc;
+    if ((rc = make_map(&maps.m[0], A1h, P, Neff, lda, kBK))) return rc;
+    if ((rc = make_map(&maps.m[1], A1l, P, Neff, lda, kBK))) return rc;
+    if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, kBK))) return rc;
+    if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, kBK))) return rc;
+    if ((rc = make_map(&maps.m[4], Lh, P, R, ldl, kBK))) return rc;
+    if ((rc = make_map(&maps.m[5], Ll, P, R, ldl, kBK))) return rc;
+    if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, kBK))) return rc;
+    if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, kBK))) return rc;
     TcArgs a;
     std::memset(&a, 0, sizeof(a));
     a.Mr = P;
@@ -645,5 +701,5 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sfve = sfve;
     a.ldo = ldo;
     a.max_F = max_F;
-    return launch_tc<2, 64>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+    return launch_tc<2, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }

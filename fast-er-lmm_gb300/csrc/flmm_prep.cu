@@ -190,10 +190,11 @@ __global__ void k_proj_apply(const double* __restrict__ K, int64_t ldk, const do
     Kp[static_cast<int64_t>(i) * ldkp + j] = a + acc;
 }
 
-__global__ void k_compat_spectrum(const double* __restrict__ evals, int N, int D, double* __restrict__ s) {
+template <typename T>
+__global__ void k_compat_spectrum(const T* __restrict__ evals, int N, int D, double* __restrict__ s) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N - D) return;
-    s[i] = fmax(evals[D + i] - 1.0, 0.0);
+    s[i] = fmax(static_cast<double>(evals[D + i]) - 1.0, 0.0);
 }
 
 // R[r] = A[r] - X (Xpinv A[r]^T); one warp per row, D <= 64 coefficients held in shared memory per warp
@@ -231,12 +232,21 @@ __global__ void k_grid_nodes(double lo, double hi, int n, double* __restrict__ g
     grid[i] = (i < half) ? fma(step, static_cast<double>(i), lo) : fma(-step, static_cast<double>(n - 1 - i), hi);
 }
 
+// nullh2 = 1 / (1 + exp(log delta)) broadcast over a chromosome's variant rows.  The FP64 exp is evaluated once per
+// column and thread (GB300's FP64 rate is low); each thread then writes its column in kNullh2Rows rows, so the
+// stores of a warp are contiguous.
+constexpr int kNullh2Rows = 64;
+
 __global__ void k_fill_nullh2(const double* __restrict__ ld, int n_real, const int64_t* __restrict__ rows, int Mc,
                               double* __restrict__ out, int64_t ldo) {
-    int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-    if (t >= static_cast<int64_t>(Mc) * n_real) return;
-    int m = static_cast<int>(t / n_real), p = static_cast<int>(t % n_real);
-    out[rows[m] * ldo + p] = 1.0 / (1.0 + exp(ld[p]));
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_real) return;
+    const double h2 = 1.0 / (1.0 + exp(ld[p]));
+    for (int64_t m0 = static_cast<int64_t>(blockIdx.y) * kNullh2Rows; m0 < Mc;
+         m0 += static_cast<int64_t>(gridDim.y) * kNullh2Rows) {
+        const int64_t m1 = m0 + kNullh2Rows < Mc ? m0 + kNullh2Rows : Mc;
+        for (int64_t m = m0; m < m1; ++m) out[rows[m] * ldo + p] = h2;
+    }
 }
 
 __global__ void k_axpy(int64_t n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
@@ -337,7 +347,13 @@ extern "C" int flmm_project_kinship(const double* K, int64_t ldk, const double* 
 
 extern "C" int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream) {
     FLMM_REQUIRE(evals && s && N > D && D >= 0, "flmm_compat_spectrum: need N > D");
-    k_compat_spectrum<<<ceil_div(N - D, 256), 256, 0, as_stream(stream)>>>(evals, N, D, s);
+    k_compat_spectrum<double><<<ceil_div(N - D, 256), 256, 0, as_stream(stream)>>>(evals, N, D, s);
+    return check_launch("k_compat_spectrum");
+}
+
+extern "C" int flmm_compat_spectrum_f32(const float* evals, int N, int D, double* s, void* stream) {
+    FLMM_REQUIRE(evals && s && N > D && D >= 0, "flmm_compat_spectrum_f32: need N > D");
+    k_compat_spectrum<float><<<ceil_div(N - D, 256), 256, 0, as_stream(stream)>>>(evals, N, D, s);
     return check_launch("k_compat_spectrum");
 }
 
@@ -360,8 +376,10 @@ extern "C" int flmm_fill_nullh2(const double* log_delta, int n_real, const int64
                                 int64_t ldo, void* stream) {
     FLMM_REQUIRE(log_delta && rows && nullh2 && ldo >= n_real, "flmm_fill_nullh2: bad arguments");
     if (n_real <= 0 || Mc <= 0) return FLMM_OK;
-    k_fill_nullh2<<<ceil_div(static_cast<int64_t>(Mc) * n_real, 256), 256, 0, as_stream(stream)>>>(
-        log_delta, n_real, rows, Mc, nullh2, ldo);
+    const int64_t row_blocks = ceil_div(static_cast<int64_t>(Mc), kNullh2Rows);
+    const dim3 grid(static_cast<unsigned>(ceil_div(n_real, 128)),
+                    static_cast<unsigned>(row_blocks < 65535 ? row_blocks : 65535));
+    k_fill_nullh2<<<grid, 128, 0, as_stream(stream)>>>(log_delta, n_real, rows, Mc, nullh2, ldo);
     return check_launch("k_fill_nullh2");
 }
 

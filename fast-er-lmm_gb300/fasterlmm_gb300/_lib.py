@@ -39,7 +39,10 @@ SIGNATURES: dict[str, list] = {
     "flmm_eigh": [_p, _p, _i, _p, _p, _sz, _p],
     "flmm_eigh_batched_workspace_bytes": [_p, _i, _i, _i, _psz],
     "flmm_eigh_batched": [_p, _p, _i, _i, _p, _i, _i, _p, _sz, _p],
+    "flmm_eigh_batched_f32_workspace_bytes": [_p, _i, _i, _psz],
+    "flmm_eigh_batched_f32": [_p, _p, _i, _i, _p, _p, _sz, _p],
     "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
+    "flmm_compat_spectrum_f32": [_p, _i, _i, _p, _p],
     "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],
     "flmm_gemm_nt_f64": [_p, _i64, _p, _i64, _p, _i64, _i, _i, _i, _d, _p],
     "flmm_delta_grid_nodes": [_d, _d, _i, _p, _p],
@@ -53,6 +56,15 @@ SIGNATURES: dict[str, list] = {
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_shift_diagonal_f64": [_p, _i, _i64, _d, _p],
+    "flmm_clamp_nonneg_f64": [_p, _i64, _p, _p],
+    "flmm_gls_loss_workspace_bytes": [_i, _i, _i, _i, _psz],
+    "flmm_gls_loss_f64": [_p, _i, _p, _i64, _i, _p, _i64, _i, _p, _i, _i, _i, _p, _p, _sz, _p],
+    "flmm_fit_delta_gls_workspace_bytes": [_i, _i, _i, _i, _psz],
+    "flmm_fit_delta_gls_f64": [_p, _i, _p, _i64, _i, _p, _i64, _i, _i, _d, _d, _i, _i, _p, _p, _p, _sz, _p],
+    "flmm_wald_gls_workspace_bytes": [_i, _i, _i, _psz],
+    "flmm_wald_gls_f64": [_p, _i, _p, _i64, _i, _p, _i64, _p, _i, _i, _p, _i64, _i, _p, _p, _p, _p, _p, _i64, _p,
+                          _p, _sz, _p],
     "flmm_perm_threshold_p": [_p, _i, _i, _i, _d, _p, _p],
     "flmm_context_check": [_p, _p],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],

@@ -395,17 +395,20 @@ def _take_rows(Zt: Tensor, blk) -> Tensor:
 def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int, on_chrom=None,
            Zt_kin: Tensor | None = None, chrom_kin: np.ndarray | None = None, loco: bool = True, n_grid: int = 64,
            log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
-           form: str = "plain", timers: dict | None = None) -> ScanResult:
+           form: str = "plain", timers: dict | None = None, host_out: dict | None = None) -> ScanResult:
     """
     Core engine on device tensors: Zt (M, N) standardised tested variants, X (N, D), Yt (P, N) columns, chromosome
     labels (M,).  The kinship Gram of every chromosome is computed once and each LOCO kinship is the total minus
     the chromosome's own block; the covariate basis and the OLS regress-out of the phenotypes are computed once.
+    ``host_out`` (fast form only) streams the results into caller tensors while the scan runs (fast.scan_t).
     """
     if form == "fast":
         from . import fast
         return fast.scan_t(Zt, X, Yt, chrom, n_real=n_real, on_chrom=on_chrom, Zt_kin=Zt_kin, chrom_kin=chrom_kin,
                            loco=loco, n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max,
-                           refine=refine, timers=timers)
+                           refine=refine, timers=timers, host_out=host_out)
+    if host_out is not None:
+        raise ValueError("host_out is only supported by the fast form")
     if form != "plain":
         raise ValueError(f"unknown form {form!r} (expected 'plain' or 'fast')")
     dev = Zt.device

@@ -27,8 +27,12 @@ from .core import F64, CovariateBasis, ScanResult, _alloc_outputs, _ptr, _stream
 F16 = torch.float16
 F32 = torch.float32
 
-# how the per-chromosome FP64 eigendecompositions run: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on
-# worker streams (see flmm_eigh_batched)
+# Precision of the per-chromosome eigendecompositions.  "f64" (default): the FP64 batched call (EIGH_MODE: 1 =
+# cusolverDnXsyevBatched, 2 = syevd side by side on worker streams; see flmm_eigh_batched).  "f32": one FP32
+# cusolverDnXsyevBatched call for all LOCO kinships.  The FP32 decomposition keeps F, beta, SE, SFVE and -log10 p
+# inside the parity tolerance, but on phenotypes with a flat likelihood (h2 near 0) its ~1e-7 backward error moves
+# the fitted delta, and with it nullh2 = 1 / (1 + delta), by more than 1e-5 relative.
+EIGH_PRECISION = "f64"
 EIGH_MODE = 1
 
 
@@ -229,10 +233,13 @@ def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: T
 def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int, on_chrom=None,
            Zt_kin: Tensor | None = None, chrom_kin: np.ndarray | None = None, loco: bool = True, n_grid: int = 64,
            log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
-           timers: dict | None = None) -> ScanResult:
+           timers: dict | None = None, host_out: dict | None = None) -> ScanResult:
     """
     Fast-form engine on device tensors (same contract as fasterlmm_gb300.core.scan_t).  ``timers``, if given, maps
-    a stage name to a list that receives (start, end) CUDA event pairs recorded around that stage.
+    a stage name to a list that receives (start, end) CUDA event pairs recorded around that stage.  ``host_out``, if
+    given, holds result tensors (keys of ScanResult, e.g. pinned host memory) that are filled while the scan runs:
+    each chromosome's result rows are copied on a side stream as soon as its Wald scan is done, so the copies overlap
+    the next chromosome's work; the returned ScanResult then holds those tensors.
     """
     dev = Zt.device
     ctx = _lib.context(dev.index)
@@ -255,6 +262,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
             slot[1] = ev
 
     out, max_F = _alloc_outputs(M, n_real, P, dev)
+    sink = _RowSink(out, host_out, dev) if host_out is not None else None
     basis = CovariateBasis(X)
     Ys = SplitRows.of(basis.regress_out(Yt))
     order, blocks = _chrom_order(chrom)
@@ -276,11 +284,14 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     Kp = torch.empty((len(units), N, N), dtype=F64, device=dev)
     for k_idx, (c, _, _) in enumerate(units):
         project_kinship(kin.kinship(c), basis, Kp[k_idx])
-    evals = eigh_batched(Kp, mode=EIGH_MODE)
+    if EIGH_PRECISION == "f32":
+        Kp, evals = _eigh_batched_f32(ctx, Kp)
+    else:
+        evals = eigh_batched(Kp, mode=EIGH_MODE)
     done(slot)
     UYt = torch.empty((P, ldk), dtype=F32, device=dev)
     for k_idx, (c, a, n) in enumerate(units):
-        s = compat_spectrum(evals[k_idx], D)
+        s = _spectrum(evals[k_idx], D)
         Ut = Kp[k_idx, D:]
         Us = SplitRows.of(Ut)
         gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
@@ -291,7 +302,78 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         wald_fast(ctx, ops, s, UYt[:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,
                   log_delta_min=log_delta_min, log_delta_max=log_delta_max, mark=mark, done=done)
         log_deltas[c if c is not None else 0] = ld
+        if sink is not None:
+            sink.push(order, a, n)
         if on_chrom is not None:
             on_chrom(k_idx + 1, len(units))
     _lib.call("flmm_context_check", ctx, st)
+    if sink is not None:
+        return sink.finish(max_F, log_deltas)
     return ScanResult(max_F=max_F, log_delta=log_deltas, **out)
+
+
+def _eigh_batched_f32(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
+    """FP32 eigendecomposition of a (batch, N, N) FP64 stack: (eigenvector rows (batch, N, N) FP32, evals FP32)."""
+    dev = Kp.device
+    batch, N, _ = Kp.shape
+    st = _stream(dev)
+    A = torch.empty((batch, N, N), dtype=F32, device=dev)
+    _lib.call("flmm_convert_f64_f32", A.numel(), _ptr(Kp), _ptr(A), st)
+    evals = torch.empty((batch, N), dtype=F32, device=dev)
+    nbytes = _lib.query_bytes("flmm_eigh_batched_f32_workspace_bytes", ctx, N, batch)
+    w, wb = _work.get(dev, nbytes)
+    _lib.call("flmm_eigh_batched_f32", ctx, _ptr(A), N, batch, _ptr(evals), w, wb, st)
+    return A, evals
+
+
+def _spectrum(evals: Tensor, D: int) -> Tensor:
+    if evals.dtype == F64:
+        return compat_spectrum(evals, D)
+    N = evals.shape[0]
+    s = torch.empty(N - D, dtype=F64, device=evals.device)
+    _lib.call("flmm_compat_spectrum_f32", _ptr(evals), N, D, _ptr(s), _stream(evals.device))
+    return s
+
+
+class _RowSink:
+    """
+    Copies finished result rows into caller tensors on a side stream.  A chromosome whose rows are contiguous in
+    the caller's variant order is copied as soon as its scan is queued; other rows (unsorted chromosome labels)
+    and max_F are copied at the end.
+    """
+
+    KEYS = ("f", "beta", "se", "sfve", "nullh2")
+
+    def __init__(self, out: dict, host_out: dict, dev: torch.device):
+        self.out, self.host, self.dev = out, host_out, dev
+        self.stream = torch.cuda.Stream(device=dev)
+        self.pending = []  # row ranges not copied early
+
+    def push(self, order, a: int, n: int) -> None:
+        if n == 0:
+            return
+        r0 = a if order is None else int(order[a])
+        if order is not None and not np.array_equal(order[a:a + n], np.arange(r0, r0 + n)):
+            self.pending.append(None)
+            return
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.dev))
+        self.stream.wait_event(ev)
+        with torch.cuda.stream(self.stream):
+            for k in self.KEYS:
+                if k in self.host:
+                    self.host[k][r0:r0 + n].copy_(self.out[k][r0:r0 + n], non_blocking=True)
+
+    def finish(self, max_F: Tensor, log_deltas: dict) -> ScanResult:
+        main = torch.cuda.current_stream(self.dev)
+        if self.pending:  # at least one chromosome was not contiguous: copy everything once more at the end
+            for k in self.KEYS:
+                if k in self.host:
+                    self.host[k].copy_(self.out[k], non_blocking=True)
+        if "max_F" in self.host:
+            self.host["max_F"].copy_(max_F, non_blocking=True)
+        main.synchronize()
+        self.stream.synchronize()
+        pick = lambda k, t: self.host[k] if k in self.host else t
+        return ScanResult(max_F=pick("max_F", max_F), log_delta=log_deltas,
+                          **{k: pick(k, v) for k, v in self.out.items()})

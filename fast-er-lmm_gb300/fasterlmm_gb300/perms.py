@@ -92,12 +92,13 @@ def perm_threshold(data, pheno_idx: list[int], *, n_perm: int = 100, seed: int =
     else:
         orders = torch.from_numpy(perm_orders(N, seed_cols, n_perm, seed)).to(dev)
     Yt_all = pack_perm_columns(Yt_real, orders)
+    stream_out = out if (out is not None and form == "fast") else None
     res = scan_t(Zt, X, Yt_all, np.asarray(data.chrom), n_real=B, on_chrom=on_chrom if loco else None,
                  Zt_kin=Zt_kin, chrom_kin=chrom_kin, loco=loco, n_grid=n_grid, log_delta_min=log_delta_min,
-                 log_delta_max=log_delta_max, form=form, timers=timers)
-    if out is not None:
+                 log_delta_max=log_delta_max, form=form, timers=timers, host_out=stream_out)
+    if out is not None and stream_out is None:
         res = copy_into(res, out)
-    else:
+    elif out is None:
         out_dev = data.Z.device if isinstance(data.Z, torch.Tensor) else dev
         res = _to_device(res, out_dev)
     perm_max_F = res.max_F[B:].reshape(B, n_perm)

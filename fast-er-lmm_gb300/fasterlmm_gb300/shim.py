@@ -5,24 +5,29 @@ Install this package's GPU scan under an existing ``fasterlmm`` (FaST-ER-LMM) in
 ``fasterlmm.core.{loco_scan_compat, single_k_scan_compat, fastlmm_compat_rotate, fit_delta_grid_compat,
 snp_wald_scan_compat}``, the copies ``fasterlmm.perms`` imported by name (fasterlmm/perms.py:17), and
 ``perm_threshold`` in ``fasterlmm.perms`` and in ``fasterlmm.cli`` when that module is loaded (it imports the
-function by name).  The CLI and any user code that goes through those names then runs on the GPU unchanged.
-``uninstall()`` restores the originals.
+function by name).  The plain GLS names of ``fasterlmm.core`` (rotate, eigendecompose, nLLeval, _profile_loss,
+_profile_loss_per_pheno, fit_delta_grid, snp_wald_scan, loco_scan, single_k_scan; fasterlmm/core.py:89-451) and
+the copies ``fasterlmm.extreme`` imported by name (fasterlmm/extreme.py:19) are rebound to the GLS kernels.  The
+CLI and any user code that goes through those names then runs on the GPU unchanged.  ``uninstall()`` restores
+the originals.
 """
 from __future__ import annotations
 
 import functools
 import sys
 
-_saved: dict = {}
+_saved: dict = {}  # (module name, attribute) -> (module, original value)
 
 _CORE_NAMES = ("loco_scan_compat", "single_k_scan_compat", "fastlmm_compat_rotate", "fit_delta_grid_compat",
                "snp_wald_scan_compat")
+_GLS_NAMES = ("eigendecompose", "rotate", "nLLeval", "_profile_loss", "_profile_loss_per_pheno", "fit_delta_grid",
+              "snp_wald_scan", "loco_scan", "single_k_scan", "Spectrum")
 
 
 def _set(mod, name, value):
     key = (mod.__name__, name)
     if key not in _saved:
-        _saved[key] = getattr(mod, name)
+        _saved[key] = (mod, getattr(mod, name))
     setattr(mod, name, value)
 
 
@@ -31,14 +36,15 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
     Patch the reference's modules (imported from sys.modules, or given as ``modules`` = {"core": ..., "perms":
     ..., "cli": ...}).  ``form`` picks the numeric form of the scan drivers.  Returns the patched qualified names.
     """
-    from . import core, perms
+    from . import core, gls, perms
     mods = dict(modules or {})
     if not mods:
         import importlib
         mods["core"] = importlib.import_module("fasterlmm.core")
         mods["perms"] = importlib.import_module("fasterlmm.perms")
-        if "fasterlmm.cli" in sys.modules:
-            mods["cli"] = sys.modules["fasterlmm.cli"]
+        for key in ("cli", "extreme"):
+            if f"fasterlmm.{key}" in sys.modules:
+                mods[key] = sys.modules[f"fasterlmm.{key}"]
     ours = {
         "loco_scan_compat": functools.partial(core.loco_scan_compat, form=form),
         "single_k_scan_compat": functools.partial(core.single_k_scan_compat, form=form),
@@ -51,6 +57,12 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
         if hasattr(mods.get("core"), name):
             _set(mods["core"], name, ours[name])
             patched.append(f"{mods['core'].__name__}.{name}")
+    for name in _GLS_NAMES:
+        for key in ("core", "extreme"):
+            m = mods.get(key)
+            if m is not None and hasattr(m, name):
+                _set(m, name, getattr(gls, name))
+                patched.append(f"{m.__name__}.{name}")
     pt = functools.partial(perms.perm_threshold, form=form)
     for key in ("perms", "cli"):
         m = mods.get(key)
@@ -67,8 +79,6 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
 
 
 def uninstall() -> None:
-    for (modname, name), value in list(_saved.items()):
-        mod = sys.modules.get(modname)
-        if mod is not None:
-            setattr(mod, name, value)
+    for (_, name), (mod, value) in list(_saved.items()):
+        setattr(mod, name, value)
     _saved.clear()

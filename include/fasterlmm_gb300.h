@@ -107,8 +107,16 @@ int flmm_eigh_batched_workspace_bytes(flmm_context* ctx, int N, int batch, int m
 int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* evals, int mode, int slot, void* work,
                       size_t work_bytes, void* stream);
 
-/* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514). */
+/* FP32 twin of flmm_eigh_batched (mode 1, main handle) for the split-precision form, whose eigenbasis is used at
+ * ~2^-22 relative precision: an FP32 eigendecomposition's backward error (~1e-7 of the projected kinship) is below
+ * that.  Same layout: eigenvectors one per row of each A[b], evals ascending. */
+int flmm_eigh_batched_f32_workspace_bytes(flmm_context* ctx, int N, int batch, size_t* bytes);
+int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* evals, void* work, size_t work_bytes,
+                          void* stream);
+
+/* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514); the _f32 form reads FP32 evals. */
 int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream);
+int flmm_compat_spectrum_f32(const float* evals, int N, int D, double* s, void* stream);
 
 /* OLS regress-out of the covariates, row-wise: R[i] = A[i] - X (Xpinv A[i]^T) for rows of A (rows, N)
  * (fasterlmm/core.py:517 for phenotypes, :628 for variants).  R may alias A. */
@@ -245,6 +253,37 @@ int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int
 int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
+
+/* ---- plain GLS path (fasterlmm/core.py:89-451): covariates kept in the model ------------------------------------
+ *
+ * Layouts as in the compat path: Xrt (C, N) the rotated covariates U^T X one column per row, Yrt (P, N) the rotated
+ * phenotype columns, Srt (M, N) rotated variants, s (N,) the spectrum.  1 <= C <= 30. */
+
+/* eigendecompose's jitter and clamp (fasterlmm/core.py:89-102): A[i, i] += value; y = max(x, 0). */
+int flmm_shift_diagonal_f64(double* A, int N, int64_t lda, double value, void* stream);
+int flmm_clamp_nonneg_f64(const double* x, int64_t n, double* y, void* stream);
+
+/* GLS -2 log L (fasterlmm/core.py:148-224): per_column = 0 evaluates the (n_ld, P) grid loss[g, p] at the n_ld
+ * values log_delta (workspace from the query); per_column = 1 evaluates loss[p] at log_delta[p] (n_ld == P, no
+ * workspace).  reml = 1 divides by N - C and adds log det(X~^T W X~).  A failed Cholesky gives +inf. */
+int flmm_gls_loss_workspace_bytes(int N, int C, int P, int n_ld, size_t* bytes);
+int flmm_gls_loss_f64(const double* s, int N, const double* Xrt, int64_t ldx, int C, const double* Yrt, int64_t ldy,
+                      int P, const double* log_delta, int n_ld, int per_column, int reml, double* loss, void* work,
+                      size_t work_bytes, void* stream);
+
+/* fit_delta_grid (fasterlmm/core.py:227-264): grid argmin then 50 golden-section steps per column, ML or REML. */
+int flmm_fit_delta_gls_workspace_bytes(int N, int C, int P, int n_grid, size_t* bytes);
+int flmm_fit_delta_gls_f64(const double* s, int N, const double* Xrt, int64_t ldx, int C, const double* Yrt,
+                           int64_t ldy, int P, int n_grid, double lo, double hi, int refine, int reml,
+                           double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes, void* stream);
+
+/* snp_wald_scan (fasterlmm/core.py:295-375): GLS Wald of every (variant, column) with the covariates in the model;
+ * detail rows[m] * ldo + p for p < n_real, running max into max_F (P,) (initialise to -inf). */
+int flmm_wald_gls_workspace_bytes(int N, int C, int P, size_t* bytes);
+int flmm_wald_gls_f64(const double* s, int N, const double* Xrt, int64_t ldx, int C, const double* Yrt, int64_t ldy,
+                      const double* log_delta, int P, int n_real, const double* Srt, int64_t lds, int M,
+                      const int64_t* rows, double* f, double* beta, double* se, double* sfve, int64_t ldo,
+                      double* max_F, void* work, size_t work_bytes, void* stream);
 
 /* Genome-wide permutation threshold per phenotype (fasterlmm/cli.py:128, :406): thresh[b] = numpy.quantile(p, q) with
  * linear interpolation, p = P(F(1, df2) > perm_max_F[b, :]) over the row's n_perm permutation maxima (B, n_perm). */

@@ -234,6 +234,193 @@ def single_k_scan_compat(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, *, n_real:
 
 
 # --------------------------------------------------------------------------------------------------------------
+# plain GLS path: rotation with covariates kept, ML / REML delta fit with a per-delta Cholesky, GLS Wald scan
+# --------------------------------------------------------------------------------------------------------------
+
+def eigendecompose(K: np.ndarray, jitter: float = 1e-6) -> tuple[np.ndarray, np.ndarray]:
+    """eigh(K + jitter I), eigenvalues clamped at 0 (fasterlmm/core.py:89-102)."""
+    s, U = np.linalg.eigh(K + jitter * np.eye(K.shape[0]))
+    return np.maximum(s, 0.0), U
+
+
+def rotate(K: np.ndarray, X: np.ndarray, Y: np.ndarray) -> dict:
+    """Spectrum with U^T X and U^T Y (fasterlmm/core.py:105-116)."""
+    s, U = eigendecompose(K)
+    return {"s": s, "U": U, "X_rot": U.T @ X, "Y_rot": U.T @ Y}
+
+
+def _gls_terms(w: np.ndarray, X_rot: np.ndarray, Y_rot: np.ndarray):
+    """A = X~^T W X~ per row of w, its Cholesky (identity where it fails), u = X~^T W Y~, uAu, yWy."""
+    A = np.einsum("gn,nc,nd->gcd", w, X_rot, X_rot)
+    C = X_rot.shape[1]
+    L = np.empty_like(A)
+    bad = np.zeros(A.shape[0], dtype=bool)
+    for g in range(A.shape[0]):
+        try:
+            L[g] = np.linalg.cholesky(A[g])
+        except np.linalg.LinAlgError:
+            L[g] = np.eye(C)
+            bad[g] = True
+    return A, L, bad
+
+
+def profile_loss(log_delta: np.ndarray, s: np.ndarray, X_rot: np.ndarray, Y_rot: np.ndarray, *,
+                 reml: bool = False) -> np.ndarray:
+    """
+    (G, P) -2 log likelihood with beta profiled out by GLS (fasterlmm/core.py:148-187): A = X~^T W X~ per grid
+    point, uAu = u^T A^-1 u, rWr = max(yWy - uAu, floor); ML divides by N, REML by N - C and adds log det A.
+    Grid points whose A has no Cholesky get +inf.
+    """
+    N, C = X_rot.shape
+    delta = np.exp(log_delta)
+    Sd = s[None, :] + delta[:, None]
+    w = 1.0 / Sd
+    A, L, bad = _gls_terms(w, X_rot, Y_rot)
+    logdet_A = 2.0 * np.log(np.diagonal(L, axis1=1, axis2=2)).sum(axis=1)
+    u = np.einsum("gn,nc,np->gcp", w, X_rot, Y_rot)
+    beta_x = np.stack([np.linalg.solve(L[g].T, np.linalg.solve(L[g], u[g])) for g in range(len(delta))])
+    uAu = (u * beta_x).sum(axis=1)
+    yWy = w @ (Y_rot * Y_rot)
+    rWr = np.maximum(yWy - uAu, pos_floor())
+    sum_log_Sd = np.log(Sd).sum(axis=1)
+    if reml:
+        loss = (N - C) * (LOG2PI + np.log(rWr / (N - C)) + 1.0) + sum_log_Sd[:, None] + logdet_A[:, None]
+    else:
+        loss = N * (LOG2PI + np.log(rWr / N) + 1.0) + sum_log_Sd[:, None]
+    loss[bad, :] = np.inf
+    return loss
+
+
+def profile_loss_per_pheno(log_delta: np.ndarray, s: np.ndarray, X_rot: np.ndarray, Y_rot: np.ndarray, *,
+                           reml: bool = False) -> np.ndarray:
+    """Column p's loss at its own log_delta[p] (fasterlmm/core.py:190-224)."""
+    P = Y_rot.shape[1]
+    return np.array([profile_loss(log_delta[p:p + 1], s, X_rot, Y_rot[:, p:p + 1], reml=reml)[0, 0]
+                     for p in range(P)])
+
+
+def nll_eval(delta: float, s: np.ndarray, X_rot: np.ndarray, y_rot: np.ndarray) -> float:
+    """ML -2 log likelihood of one phenotype at one delta (fasterlmm/core.py:122-145)."""
+    N = X_rot.shape[0]
+    w = 1.0 / (s + delta)
+    WX = w[:, None] * X_rot
+    A = WX.T @ X_rot
+    Xy = WX.T @ y_rot
+    beta = np.linalg.solve(A, Xy)
+    rWr = (y_rot * w * y_rot).sum() - (Xy * beta).sum()
+    return float(N * (LOG2PI + np.log(rWr / N) + 1.0) + np.log(s + delta).sum())
+
+
+def fit_delta_grid(s: np.ndarray, X_rot: np.ndarray, Y_rot: np.ndarray, *, n_grid: int = 64,
+                   log_delta_min: float = -10.0, log_delta_max: float = 10.0, refine: bool = True,
+                   reml: bool = False, return_idx: bool = False):
+    """Grid argmin then 50 golden-section steps on the GLS loss (fasterlmm/core.py:227-264)."""
+    grid = delta_grid(n_grid, log_delta_min, log_delta_max)
+    loss = profile_loss(grid, s, X_rot, Y_rot, reml=reml)
+    idx = loss.argmin(axis=0)
+    if not refine:
+        out = grid[idx]
+        return (out, idx) if return_idx else out
+    a = grid[np.clip(idx - 1, 0, n_grid - 1)].copy()
+    b = grid[np.clip(idx + 1, 0, n_grid - 1)].copy()
+    inv_phi = 2.0 / (1.0 + 5.0 ** 0.5)
+    inv_phi2 = inv_phi * inv_phi
+    c = a + inv_phi2 * (b - a)
+    d = a + inv_phi * (b - a)
+    fc = profile_loss_per_pheno(c, s, X_rot, Y_rot, reml=reml)
+    fd = profile_loss_per_pheno(d, s, X_rot, Y_rot, reml=reml)
+    for _ in range(50):
+        cond = fc < fd
+        b = np.where(cond, d, b)
+        a = np.where(cond, a, c)
+        c = a + inv_phi2 * (b - a)
+        d = a + inv_phi * (b - a)
+        fc = profile_loss_per_pheno(c, s, X_rot, Y_rot, reml=reml)
+        fd = profile_loss_per_pheno(d, s, X_rot, Y_rot, reml=reml)
+    out = np.clip(0.5 * (a + b), log_delta_min, log_delta_max)
+    return (out, idx) if return_idx else out
+
+
+def snp_wald_scan(spec: dict, log_delta: np.ndarray, S_rot: np.ndarray, *, n_real: int | None = None) -> dict:
+    """
+    GLS Wald test per (variant, column) with the covariates in the model (fasterlmm/core.py:295-375): per column
+    the null fit (A, beta_x, r, rWr), per test B = X~^T W S, quad = B^T A^-1 B, denom = max(sWs - quad, floor),
+    num = (W r)^T S, beta = num / denom, var_beta = max(rWr - num^2 / denom, floor) / (N - C - 1) / denom.
+    """
+    s, X_rot, Y_rot = spec["s"], spec["X_rot"], spec["Y_rot"]
+    N, C = X_rot.shape
+    P = Y_rot.shape[1]
+    M = S_rot.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    floor = pos_floor()
+    delta = np.exp(log_delta)
+    w = 1.0 / (s[None, :] + delta[:, None])
+    A, L, _ = _gls_terms(w, X_rot, Y_rot)
+    u = np.einsum("pn,nc,np->pc", w, X_rot, Y_rot)
+    beta_x = np.stack([np.linalg.solve(L[p].T, np.linalg.solve(L[p], u[p])) for p in range(P)])
+    r = Y_rot - X_rot @ beta_x.T
+    rWr = (w * r.T * r.T).sum(axis=1)
+    wr = w * r.T
+    B = np.einsum("pn,nc,nm->pcm", w, X_rot, S_rot)
+    AinvB = np.stack([np.linalg.solve(L[p].T, np.linalg.solve(L[p], B[p])) for p in range(P)])
+    sWs = w @ (S_rot * S_rot)
+    quad = (B * AinvB).sum(axis=1)
+    denom = np.maximum(sWs - quad, floor)
+    num = wr @ S_rot
+    beta = num / denom
+    rss = np.maximum(rWr[:, None] - num * num / denom, floor)
+    var_beta = rss / (N - C - 1) / denom
+    F = beta * beta / var_beta
+    max_F = F.max(axis=1) if M > 0 else np.full(P, -np.inf)
+    rr = slice(0, n_real)
+    sfve = np.sqrt(np.maximum((num[rr] * num[rr]) / (denom[rr] * rWr[rr, None]), 0.0))
+    h2 = 1.0 / (1.0 + np.exp(log_delta[:n_real]))
+    return {"f": F[rr].T.copy(), "beta": beta[rr].T.copy(), "se": np.sqrt(var_beta[rr]).T.copy(),
+            "sfve": sfve.T.copy(), "nullh2": np.broadcast_to(h2[None, :], (M, n_real)).copy(), "max_F": max_F}
+
+
+def loco_scan(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, chrom: np.ndarray, *, n_real: int | None = None,
+              Z_kin: np.ndarray | None = None, chrom_kin: np.ndarray | None = None, on_chrom=None) -> dict:
+    """Plain LOCO driver (fasterlmm/core.py:381-436): per chromosome K_loco, rotate, ML fit, GLS Wald."""
+    if (Z_kin is None) != (chrom_kin is None):
+        raise ValueError("Z_kin and chrom_kin go together")
+    chrom = np.asarray(chrom)
+    M = Z.shape[1]
+    P = Y.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    out = {k: np.zeros((M, n_real)) for k in ("f", "beta", "se", "sfve", "nullh2")}
+    max_F = np.full(P, -np.inf)
+    chroms = sorted(np.unique(chrom).tolist())
+    log_deltas = {}
+    for k_idx, c in enumerate(chroms):
+        test_mask = chrom == c
+        K = grm(Z[:, chrom != c]) if Z_kin is None else grm(Z_kin[:, np.asarray(chrom_kin) != c])
+        spec = rotate(K, X, Y)
+        ld = fit_delta_grid(spec["s"], spec["X_rot"], spec["Y_rot"])
+        log_deltas[c] = ld
+        res = snp_wald_scan(spec, ld, spec["U"].T @ Z[:, test_mask], n_real=n_real)
+        if n_real > 0:
+            for key in out:
+                out[key][test_mask, :] = res[key]
+        max_F = np.maximum(max_F, res["max_F"])
+        if on_chrom is not None:
+            on_chrom(k_idx + 1, len(chroms))
+    out["max_F"] = max_F
+    out["log_delta"] = log_deltas
+    return out
+
+
+def single_k_scan(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, *, n_real: int | None = None,
+                  Z_kin: np.ndarray | None = None) -> dict:
+    """Plain whole-genome scan (fasterlmm/core.py:439-451)."""
+    spec = rotate(grm(Z if Z_kin is None else Z_kin), X, Y)
+    ld = fit_delta_grid(spec["s"], spec["X_rot"], spec["Y_rot"])
+    res = snp_wald_scan(spec, ld, spec["U"].T @ Z, n_real=n_real)
+    res["log_delta"] = ld
+    return res
+
+
+# --------------------------------------------------------------------------------------------------------------
 # permutations and the batch driver
 # --------------------------------------------------------------------------------------------------------------
 

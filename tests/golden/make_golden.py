@@ -107,13 +107,87 @@ def _inputs(d):
     return {"G": d.G, "X": d.X, "Y": d.Y, "chrom": d.chrom}
 
 
+class _PlainDeltaRecorder:
+    """Wraps core.fit_delta_grid (the plain LOCO loop calls it once per chromosome) to record its outputs."""
+
+    def __init__(self, core):
+        self.core = core
+        self.orig = core.fit_delta_grid
+        self.calls = []
+
+    def __enter__(self):
+        def wrapped(spec, **kw):
+            out = self.orig(spec, **kw)
+            self.calls.append(out.clone())
+            return out
+        self.core.fit_delta_grid = wrapped
+        return self
+
+    def __exit__(self, *exc):
+        self.core.fit_delta_grid = self.orig
+
+
+def _plain_fixtures(core, fio, torch):
+    """The plain GLS path (fasterlmm/core.py:89-451): components, the LOCO driver and the single-K driver."""
+    # components on a toy single-K problem: rotation, ML / REML grid losses, fits, GLS Wald, nLLeval
+    rng = np.random.default_rng(78)
+    Nt, Mt, Pt = 48, 160, 5
+    Zc = fio.standardise_columns(torch.from_numpy(rng.normal(size=(Nt, Mt))))
+    Kc = (Zc @ Zc.T) / Mt
+    Xc = torch.from_numpy(np.concatenate([np.ones((Nt, 1)), rng.normal(size=(Nt, 2))], axis=1))
+    Yc = torch.from_numpy(rng.normal(size=(Nt, Pt)))
+    spec = core.rotate(Kc, Xc, Yc)
+    grid = torch.linspace(-10.0, 10.0, 64, dtype=torch.float64)
+    ld_ml = core.fit_delta_grid(spec)
+    ld_ml_grid = core.fit_delta_grid(spec, refine=False)
+    ld_reml = core.fit_delta_grid(spec, reml=True)
+    ld_reml_grid = core.fit_delta_grid(spec, refine=False, reml=True)
+    S_rot = spec.U.T @ Zc
+    wres = core.snp_wald_scan(spec, ld_ml, S_rot, n_real=3)
+    wres_t = core.snp_wald_scan(spec, ld_ml, S_rot, n_real=3, snp_chunk=23, pheno_chunk=2)
+    nll_d = np.array([0.05, 1.0, 7.5])
+    nll = np.array([[core.nLLeval(float(dl), spec.s, spec.X_rot, spec.Y_rot[:, p]).item() for p in range(Pt)]
+                    for dl in nll_d])
+    np.savez_compressed(HERE / "plain_components.npz", Z_std=Zc.numpy(), K=Kc.numpy(), X=Xc.numpy(), Y=Yc.numpy(),
+                        s=spec.s.numpy(), X_rot=spec.X_rot.numpy(), Y_rot=spec.Y_rot.numpy(), U=spec.U.numpy(),
+                        grid_loss_ml=core._profile_loss(grid, spec.s, spec.X_rot, spec.Y_rot).numpy(),
+                        grid_loss_reml=core._profile_loss(grid, spec.s, spec.X_rot, spec.Y_rot, reml=True).numpy(),
+                        log_delta_ml=ld_ml.numpy(), log_delta_ml_grid=ld_ml_grid.numpy(),
+                        log_delta_reml=ld_reml.numpy(), log_delta_reml_grid=ld_reml_grid.numpy(),
+                        nll_delta=nll_d, nll=nll, **_res_dict(wres), **_res_dict(wres_t, "tiled_"))
+
+    # the LOCO driver on real columns followed by permuted copies (n_real split), and the single-K driver
+    d = make_dataset(120, 900, 6, 3, 6, seed=31337, config_id=8, k_lo=2, k_hi=10)
+    B, n_perm = 6, 3
+    N = d.X.shape[0]
+    orders = np.stack([np.random.default_rng([19930909, b]).random((n_perm, N)).argsort(axis=1) for b in range(B)])
+    y_real = d.Y[:, :B]
+    Y_all = np.concatenate([y_real] + [y_real[orders[b, k], b][:, None] for b in range(B) for k in range(n_perm)],
+                           axis=1)
+    Z_std = fio.standardise_columns(torch.from_numpy(d.Z_float()))
+    X = torch.from_numpy(d.X.copy())
+    seen = []
+    with _PlainDeltaRecorder(core) as rec:
+        res = core.loco_scan(Z_std, X, torch.from_numpy(Y_all), d.chrom, n_real=B, on_chrom=lambda k, n: seen.append(k))
+    res1 = core.single_k_scan(Z_std, X, torch.from_numpy(Y_all), n_real=B)
+    np.savez_compressed(HERE / "plain_loco.npz", **_inputs(d), Y_all=Y_all, n_real=B, **_res_dict(res),
+                        log_delta=np.stack([c.numpy() for c in rec.calls]), n_chrom_seen=len(seen),
+                        **_res_dict(res1, "sk_"))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("FASTERLMM_REFERENCE", ""))
+    ap.add_argument("--only", choices=["compat", "plain"], default=None,
+                    help="write only the compat-path fixtures or only the plain-GLS fixtures")
     args = ap.parse_args()
     if not args.reference:
         sys.exit("pass --reference PATH (or set FASTERLMM_REFERENCE) to the reference checkout")
     core, fio, perms, torch = _import_reference(args.reference)
+    if args.only != "compat":
+        _plain_fixtures(core, fio, torch)
+    if args.only == "plain":
+        return
 
     # 1. the 150 x 1,500 / 16-chromosome workload through perm_threshold, reference defaults (64-pt grid)
     d, w = make_workload("n150_m1500_b20_perm100")

@@ -48,3 +48,33 @@ def assert_log_delta_equivalent(ld: np.ndarray, ld_ref: np.ndarray, s: np.ndarra
     assert not bad.any(), (f"{bad.sum()} log delta values neither close nor loss-equivalent; worst at "
                            f"{np.flatnonzero(bad)[:5]}: got {ld[bad][:5]}, ref {ld_ref[bad][:5]}, "
                            f"dloss {(La - Lb)[bad][:5]}")
+
+
+def gls_loss(ld: np.ndarray, s: np.ndarray, X_rot: np.ndarray, Y_rot: np.ndarray, reml: bool = False) -> np.ndarray:
+    """(P,) -2 log L of the plain GLS model at one log delta per column (the reference's per-pheno plain loss)."""
+    N, C = X_rot.shape
+    out = np.empty(len(ld))
+    for p, l in enumerate(np.asarray(ld, dtype=np.float64)):
+        Sd = s + np.exp(l)
+        w = 1.0 / Sd
+        A = (X_rot * w[:, None]).T @ X_rot
+        u = (X_rot * w[:, None]).T @ Y_rot[:, p]
+        rWr = max((w * Y_rot[:, p] ** 2).sum() - u @ np.linalg.solve(A, u), 1e-300)
+        if reml:
+            out[p] = (N - C) * (np.log(2 * np.pi) + np.log(rWr / (N - C)) + 1.0) + np.log(Sd).sum() + \
+                np.linalg.slogdet(A)[1]
+        else:
+            out[p] = N * (np.log(2 * np.pi) + np.log(rWr / N) + 1.0) + np.log(Sd).sum()
+    return out
+
+
+def assert_log_delta_equivalent_gls(ld, ld_ref, s, X_rot, Y_rot, *, reml: bool = False, ld_atol: float = 1e-6,
+                                    loss_rtol: float = 1e-9):
+    ld = np.asarray(ld, dtype=np.float64)
+    ld_ref = np.asarray(ld_ref, dtype=np.float64)
+    close = np.abs(ld - ld_ref) <= ld_atol
+    La = gls_loss(ld, s, X_rot, Y_rot, reml)
+    Lb = gls_loss(ld_ref, s, X_rot, Y_rot, reml)
+    bad = ~(close | (La <= Lb + loss_rtol * np.abs(Lb)))
+    assert not bad.any(), (f"{bad.sum()} log delta values neither close nor loss-equivalent; got {ld[bad][:5]}, "
+                           f"ref {ld_ref[bad][:5]}, dloss {(La - Lb)[bad][:5]}")

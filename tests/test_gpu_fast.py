@@ -145,3 +145,44 @@ def test_fast_larger_case_matches_oracle():
     ref, rpmf = orc.perm_threshold(z_float(G), d.X, d.Y, chrom, range(61), n_perm=n_perm)
     assert_scan_close(_np(res), ref)
     assert_scan_close({"perm_max_F": pmf.cpu().numpy()}, {"perm_max_F": rpmf}, keys=("perm_max_F",))
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_fast_streamed_host_outputs_match_device(shuffle):
+    """out= with pinned host tensors: rows streamed per chromosome (or copied at the end when labels are unsorted)."""
+    from fasterlmm_gb300 import perms
+    from fasterlmm_gb300.synth import make_dataset
+    d = make_dataset(300, 2000, 3, 3, 20, seed=23, config_id=14, k_lo=1, k_hi=20)
+    G, chrom = d.G, d.chrom
+    if shuffle:
+        perm = np.random.default_rng(1).permutation(G.shape[1])
+        G, chrom = G[:, perm], chrom[perm]
+    data = _data(G, d.X, d.Y, chrom)
+    n_perm = 3
+    ref, ref_pmf = perms.perm_threshold(data, list(range(20)), n_perm=n_perm, form="fast")
+    M = G.shape[1]
+    out = {k: torch.full((M, 20), np.nan, dtype=torch.float64).pin_memory() for k in DETAIL}
+    out["max_F"] = torch.empty(20 * (1 + n_perm), dtype=torch.float64).pin_memory()
+    res, pmf = perms.perm_threshold(data, list(range(20)), n_perm=n_perm, form="fast", out=out)
+    for k in DETAIL + ("max_F",):
+        assert getattr(res, k).data_ptr() == out[k].data_ptr()
+        assert torch.equal(getattr(res, k), getattr(ref, k).cpu()), k
+    assert torch.equal(pmf, ref_pmf.cpu())
+
+
+def test_fast_form_with_fp32_eigendecomposition(golden, monkeypatch):
+    """
+    The FP32 eigendecomposition option: test statistics and -log10 p within the parity tolerance; nullh2 is
+    excluded because a flat likelihood turns the decomposition's ~1e-7 error into a larger shift of delta.
+    """
+    from fasterlmm_gb300 import fast, perms, post
+    monkeypatch.setattr(fast, "EIGH_PRECISION", "f32")
+    g = golden("loco_n150_m1500")
+    B = g["f"].shape[1]
+    res, pmf = perms.perm_threshold(_data(g["G"], g["X"], g["Y"], g["chrom"]), list(range(B)), n_perm=int(g["n_perm"]),
+                                    form="fast")
+    assert_scan_close(_np(res), g, keys=("f", "beta", "se", "sfve", "max_F"))
+    assert_scan_close({"perm_max_F": pmf.cpu().numpy()}, g, keys=("perm_max_F",))
+    N, D = g["X"].shape
+    nl = post.neg_log10_pvalue(res.f, N - D - 1).cpu().numpy()
+    assert np.abs(nl - orc.neg_log10_p(g["f"], N - D - 1)).max() <= 1e-3

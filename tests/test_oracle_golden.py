@@ -125,3 +125,45 @@ def test_group_by_na_host_logic_matches_reference_groups(golden):
     # all-NaN column -> empty keep rows; a column without NaN -> every row
     Y = np.array([[1.0, np.nan], [2.0, np.nan], [3.0, np.nan]])
     assert group_by_na(Y, [0, 1]) == [([0, 1, 2], [0]), ([], [1])]
+
+
+def test_oracle_plain_components(golden):
+    """The plain GLS restatement against the reference's rotate / _profile_loss / fit_delta_grid / snp_wald_scan."""
+    from parity import assert_log_delta_equivalent_gls
+    g = golden("plain_components")
+    spec = orc.rotate(g["K"], g["X"], g["Y"])
+    _close(spec["s"], g["s"], atol=1e-10)
+    # rotated data depend on the basis only through eigenvector signs
+    _close(spec["X_rot"] ** 2, g["X_rot"] ** 2, atol=1e-10)
+    _close(spec["Y_rot"] ** 2, g["Y_rot"] ** 2, atol=1e-10)
+    s, Xr, Yr = g["s"], g["X_rot"], g["Y_rot"]
+    grid = orc.delta_grid(64, -10.0, 10.0)
+    _close(orc.profile_loss(grid, s, Xr, Yr), g["grid_loss_ml"], rtol=1e-10, atol=1e-8)
+    _close(orc.profile_loss(grid, s, Xr, Yr, reml=True), g["grid_loss_reml"], rtol=1e-10, atol=1e-8)
+    for reml, key in ((False, "ml"), (True, "reml")):
+        assert np.array_equal(orc.fit_delta_grid(s, Xr, Yr, refine=False, reml=reml), g[f"log_delta_{key}_grid"])
+        ld = orc.fit_delta_grid(s, Xr, Yr, reml=reml)
+        assert_log_delta_equivalent_gls(ld, g[f"log_delta_{key}"], s, Xr, Yr, reml=reml)
+    for i, dl in enumerate(g["nll_delta"]):
+        for p in range(Yr.shape[1]):
+            np.testing.assert_allclose(orc.nll_eval(float(dl), s, Xr, Yr[:, p]), g["nll"][i, p], rtol=1e-10)
+    S_rot = g["U"].T @ g["Z_std"]
+    res = orc.snp_wald_scan({"s": s, "X_rot": Xr, "Y_rot": Yr}, g["log_delta_ml"], S_rot, n_real=3)
+    for k in DETAIL + ("max_F",):
+        _close(res[k], g[k])
+        _close(res[k], g["tiled_" + k])
+
+
+def test_oracle_plain_loco_and_single_k(golden):
+    g = golden("plain_loco")
+    Zs = orc.standardise_columns(z_float(g["G"]))
+    B = int(g["n_real"])
+    seen = []
+    res = orc.loco_scan(Zs, g["X"], g["Y_all"], g["chrom"], n_real=B, on_chrom=lambda k, n: seen.append(k))
+    assert len(seen) == int(g["n_chrom_seen"])
+    assert_scan_close(res, g)
+    ref_ld = g["log_delta"]
+    for i, c in enumerate(sorted(res["log_delta"])):
+        assert np.abs(res["log_delta"][c] - ref_ld[i]).max() < 1e-3
+    res1 = orc.single_k_scan(Zs, g["X"], g["Y_all"], n_real=B)
+    assert_scan_close(res1, g, prefix="sk_")

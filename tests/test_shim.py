@@ -16,15 +16,22 @@ def _fake(name, attrs):
 
 def test_install_and_uninstall_rebind_reference_names():
     from fasterlmm_gb300 import perms, shim
+    from fasterlmm_gb300 import gls
     core = _fake("fasterlmm.core", ["loco_scan_compat", "single_k_scan_compat", "fastlmm_compat_rotate",
-                                   "fit_delta_grid_compat", "snp_wald_scan_compat", "grm"])
+                                   "fit_delta_grid_compat", "snp_wald_scan_compat", "grm", "rotate", "fit_delta_grid",
+                                   "snp_wald_scan", "loco_scan", "single_k_scan", "nLLeval", "_profile_loss",
+                                   "Spectrum"])
+    extreme = _fake("fasterlmm.extreme", ["Spectrum", "fit_delta_grid", "snp_wald_scan"])
     pmod = _fake("fasterlmm.perms", ["loco_scan_compat", "single_k_scan_compat", "perm_threshold"])
     cli = _fake("fasterlmm.cli", ["perm_threshold"])
     import sys
     sys.modules.update({"fasterlmm.core": core, "fasterlmm.perms": pmod, "fasterlmm.cli": cli})
     try:
         orig = (core.loco_scan_compat, pmod.perm_threshold, cli.perm_threshold, core.grm)
-        patched = shim.install(form="fast", modules={"core": core, "perms": pmod, "cli": cli})
+        orig_ext = extreme.fit_delta_grid
+        patched = shim.install(form="fast", modules={"core": core, "perms": pmod, "cli": cli, "extreme": extreme})
+        assert core.loco_scan is gls.loco_scan and core.nLLeval is gls.nLLeval and core.Spectrum is gls.Spectrum
+        assert extreme.fit_delta_grid is gls.fit_delta_grid and "fasterlmm.extreme.snp_wald_scan" in patched
         assert "fasterlmm.perms.perm_threshold" in patched and "fasterlmm.cli.perm_threshold" in patched
         assert core.loco_scan_compat.keywords == {"form": "fast"}
         assert pmod.perm_threshold.func is perms.perm_threshold
@@ -32,6 +39,7 @@ def test_install_and_uninstall_rebind_reference_names():
         assert core.grm is orig[3]  # names outside the scan path are left alone
         shim.uninstall()
         assert (core.loco_scan_compat, pmod.perm_threshold, cli.perm_threshold) == orig[:3]
+        assert extreme.fit_delta_grid is orig_ext
     finally:
         for k in ("fasterlmm.core", "fasterlmm.perms", "fasterlmm.cli"):
             sys.modules.pop(k, None)
