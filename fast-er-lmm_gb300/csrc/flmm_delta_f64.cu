@@ -15,12 +15,23 @@ namespace {
 
 constexpr double kLog2Pi = 1.8378770664093453;  // log(2 pi) in FP64, the reference's log2pi constant
 
-// ML -2 log L from the weighted sum yWy and log det V (fasterlmm/core.py:538-542)
-__device__ __forceinline__ double ml_loss(double yWy, double sum_log_sd, double neff) {
-    double rWr = fmax(yWy, kPosFloor);
-    double sigma2 = rWr / neff;
+// The low-rank model (fasterlmm/lowrank.py:131-151) adds, per column, the off-rank quadratic form yy_off / delta
+// and (Neff - k) log delta to the log determinant, and its Neff is N - D rather than the spectrum length k.  The
+// compat fit is the special case yy = NULL, n_logd = 0, neff = k.
+struct OffRank {
+    const double* yy;  // (P,) off-rank residual sum of squares, or NULL
+    double neff;       // sample count of the variance estimate
+    double n_logd;     // count of extra log(delta) terms in log det V
+};
+
+// ML -2 log L from the weighted sum yWy and log det V (fasterlmm/core.py:538-542, fasterlmm/lowrank.py:144-151)
+__device__ __forceinline__ double ml_loss(double yWy, double sum_log_sd, double delta, double yy_off,
+                                          const OffRank& o) {
+    double rWr = fmax(o.yy ? add_rn(yWy, yy_off / delta) : yWy, kPosFloor);
+    double sigma2 = rWr / o.neff;
     double t = add_rn(add_rn(kLog2Pi, log(sigma2)), 1.0);
-    return add_rn(mul_rn(neff, t), sum_log_sd);
+    const double logdet = o.n_logd != 0.0 ? add_rn(sum_log_sd, mul_rn(o.n_logd, log(delta))) : sum_log_sd;
+    return add_rn(mul_rn(o.neff, t), logdet);
 }
 
 // Wg[g, n] = 1 / (s[n] + exp(grid[g])), sum_log[g] = sum_n log(s[n] + exp(grid[g])); one block per grid node
@@ -50,15 +61,15 @@ __global__ void k_grid_weights(const double* __restrict__ s, int Neff, const dou
 constexpr int TG = 64, TP = 64, TK = 16, NT = 256;
 
 __global__ void __launch_bounds__(NT)
-k_grid_argmin(const double* __restrict__ Wg, const double* __restrict__ sum_log, const double* __restrict__ UYt,
-              int64_t ldu, int Neff, int P, int G, int32_t* __restrict__ idx_out) {
+k_grid_argmin(const double* __restrict__ Wg, const double* __restrict__ sum_log, const double* __restrict__ grid,
+              const double* __restrict__ UYt, int64_t ldu, int Neff, int P, int G, OffRank off,
+              int32_t* __restrict__ idx_out) {
     __shared__ double Ws[TK][TG + 1];
     __shared__ double Us[TK][TP + 1];
     __shared__ double red_v[16][TP];
     __shared__ int red_i[16][TP];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int p0 = blockIdx.x * TP;
-    const double neff = static_cast<double>(Neff);
     double best = INFINITY;
     int best_g = 0;
     for (int g0 = 0; g0 < G; g0 += TG) {
@@ -97,11 +108,14 @@ k_grid_argmin(const double* __restrict__ Wg, const double* __restrict__ sum_log,
         for (int c = 0; c < 4; ++c) {
             double bv = INFINITY;
             int bi = G;
+            const int pc = p0 + tx + 16 * c;
+            const double yy = (off.yy && pc < P) ? off.yy[pc] : 0.0;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 int g = g0 + ty + 16 * r;
                 if (g < G) {
-                    double v = ml_loss(acc[r][c], sum_log[g], neff);
+                    const double dg = (off.yy || off.n_logd != 0.0) ? exp(grid[g]) : 1.0;  // compat needs no delta
+                    double v = ml_loss(acc[r][c], sum_log[g], dg, yy, off);
                     if (v < bv) { bv = v; bi = g; }
                 }
             }
@@ -122,7 +136,8 @@ k_grid_argmin(const double* __restrict__ Wg, const double* __restrict__ sum_log,
 }
 
 // Per-column loss at its own log delta (fasterlmm/core.py:545-558), by one warp.
-__device__ double pheno_loss(const double* __restrict__ s, const double* __restrict__ u, int Neff, double ld) {
+__device__ double pheno_loss(const double* __restrict__ s, const double* __restrict__ u, int Neff, double ld,
+                             double yy, const OffRank& off) {
     const int lane = threadIdx.x & 31;
     const double delta = exp(ld);
     double ywy = 0.0, sl = 0.0;
@@ -134,13 +149,13 @@ __device__ double pheno_loss(const double* __restrict__ s, const double* __restr
     }
     ywy = warp_sum(ywy);
     sl = warp_sum(sl);
-    return ml_loss(ywy, sl, static_cast<double>(Neff));
+    return ml_loss(ywy, sl, delta, yy, off);
 }
 
 // golden-section search, one warp per column (fasterlmm/core.py:577-595)
 __global__ void k_golden(const double* __restrict__ s, int Neff, const double* __restrict__ UYt, int64_t ldu, int P,
                          const double* __restrict__ grid, int G, const int32_t* __restrict__ idx, int refine,
-                         double lo, double hi, double* __restrict__ log_delta) {
+                         double lo, double hi, OffRank off, double* __restrict__ log_delta) {
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
     const int i = idx[p];
@@ -149,22 +164,23 @@ __global__ void k_golden(const double* __restrict__ s, int Neff, const double* _
         return;
     }
     const double* u = UYt + p * ldu;
+    const double yy = off.yy ? off.yy[p] : 0.0;
     const int lo_i = max(i - 1, 0), hi_i = min(i + 1, G - 1);
     double a = grid[lo_i], b = grid[hi_i];
     const double inv_phi = 2.0 / (1.0 + sqrt(5.0));
     const double inv_phi2 = mul_rn(inv_phi, inv_phi);
     double c = add_rn(a, mul_rn(inv_phi2, add_rn(b, -a)));
     double d = add_rn(a, mul_rn(inv_phi, add_rn(b, -a)));
-    double fc = pheno_loss(s, u, Neff, c);
-    double fd = pheno_loss(s, u, Neff, d);
+    double fc = pheno_loss(s, u, Neff, c, yy, off);
+    double fd = pheno_loss(s, u, Neff, d, yy, off);
     for (int it = 0; it < 50; ++it) {
         const bool cond = fc < fd;
         b = cond ? d : b;
         a = cond ? a : c;
         c = add_rn(a, mul_rn(inv_phi2, add_rn(b, -a)));
         d = add_rn(a, mul_rn(inv_phi, add_rn(b, -a)));
-        fc = pheno_loss(s, u, Neff, c);
-        fd = pheno_loss(s, u, Neff, d);
+        fc = pheno_loss(s, u, Neff, c, yy, off);
+        fd = pheno_loss(s, u, Neff, d, yy, off);
     }
     if ((threadIdx.x & 31) == 0) log_delta[p] = fmin(fmax(mul_rn(0.5, add_rn(a, b)), lo), hi);
 }
@@ -181,13 +197,13 @@ extern "C" int flmm_fit_delta_f64_workspace_bytes(int Neff, int n_grid, size_t* 
     return FLMM_OK;
 }
 
-extern "C" int flmm_fit_delta_f64(const double* s, int Neff, const double* UYt, int64_t ldu, int P, int n_grid,
-                                  double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* work,
-                                  size_t work_bytes, void* stream) {
-    FLMM_REQUIRE(s && UYt && log_delta && grid_idx && work && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
-                 "flmm_fit_delta_f64: bad arguments");
+namespace {
+
+int fit_delta_impl(const double* s, int Neff, const double* UYt, int64_t ldu, int P, int n_grid, double lo, double hi,
+                   int refine, const OffRank& off, double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
+                   void* stream, const char* fn) {
     if (work_bytes < fit_ws(Neff, n_grid))
-        return fail(FLMM_ERR_WORKSPACE, "flmm_fit_delta_f64: need %zu bytes, got %zu", fit_ws(Neff, n_grid), work_bytes);
+        return fail(FLMM_ERR_WORKSPACE, "%s: need %zu bytes, got %zu", fn, fit_ws(Neff, n_grid), work_bytes);
     if (P == 0) return FLMM_OK;
     cudaStream_t st = as_stream(stream);
     double* Wg = static_cast<double*>(work);
@@ -197,9 +213,35 @@ extern "C" int flmm_fit_delta_f64(const double* s, int Neff, const double* UYt, 
     if (rc) return rc;
     k_grid_weights<<<n_grid, 256, 0, st>>>(s, Neff, grid, Wg, sum_log);
     if ((rc = check_launch("k_grid_weights"))) return rc;
-    k_grid_argmin<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
+    k_grid_argmin<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, grid, UYt, ldu, Neff, P, n_grid, off, grid_idx);
     if ((rc = check_launch("k_grid_argmin"))) return rc;
     k_golden<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(s, Neff, UYt, ldu, P, grid, n_grid,
-                                                                          grid_idx, refine, lo, hi, log_delta);
+                                                                          grid_idx, refine, lo, hi, off, log_delta);
     return check_launch("k_golden");
+}
+
+}  // namespace
+
+extern "C" int flmm_fit_delta_f64(const double* s, int Neff, const double* UYt, int64_t ldu, int P, int n_grid,
+                                  double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* work,
+                                  size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(s && UYt && log_delta && grid_idx && work && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
+                 "flmm_fit_delta_f64: bad arguments");
+    const OffRank off{nullptr, static_cast<double>(Neff), 0.0};
+    return fit_delta_impl(s, Neff, UYt, ldu, P, n_grid, lo, hi, refine, off, log_delta, grid_idx, work, work_bytes,
+                          stream, "flmm_fit_delta_f64");
+}
+
+extern "C" int flmm_fit_delta_lowrank_f64(const double* s, int k, const double* UYt, int64_t ldu, const double* yy_off,
+                                          int Neff, int P, int n_grid, double lo, double hi, int refine,
+                                          double* log_delta, int32_t* grid_idx, void* work, size_t work_bytes,
+                                          void* stream) {
+    FLMM_REQUIRE(s && UYt && yy_off && log_delta && grid_idx && work && k > 0 && Neff > 0 && n_grid > 0 && ldu >= k &&
+                     P >= 0,
+                 "flmm_fit_delta_lowrank_f64: bad arguments");
+    // Neff - k may be negative: with k >= N the reference's basis can keep O(1e-17) directions of the projected-out
+    // space, each adding log(s + delta) ~ log(delta), which the negative count cancels (fasterlmm/lowrank.py:88-94)
+    const OffRank off{yy_off, static_cast<double>(Neff), static_cast<double>(Neff - k)};
+    return fit_delta_impl(s, k, UYt, ldu, P, n_grid, lo, hi, refine, off, log_delta, grid_idx, work, work_bytes,
+                          stream, "flmm_fit_delta_lowrank_f64");
 }

@@ -428,6 +428,24 @@ __global__ void k_loco_kinship_f32(const double* __restrict__ Gtot, const float*
 
 }  // namespace
 
+// out[r] = sum_c A[r, c]^2, one warp per row
+__global__ void k_row_sumsq(const double* __restrict__ A, int64_t lda, int rows, int cols, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    if (r >= rows) return;
+    double acc = 0.0;
+    for (int c = lane; c < cols; c += 32) acc = fma(A[r * lda + c], A[r * lda + c], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) out[r] = acc;
+}
+
+extern "C" int flmm_row_sumsq_f64(const double* A, int64_t lda, int rows, int cols, double* out, void* stream) {
+    FLMM_REQUIRE((A && out && lda >= cols && cols >= 0) || rows == 0, "flmm_row_sumsq_f64: bad arguments");
+    if (rows == 0) return FLMM_OK;
+    k_row_sumsq<<<ceil_div(static_cast<int64_t>(rows) * 32, 256), 256, 0, as_stream(stream)>>>(A, lda, rows, cols, out);
+    return check_launch("k_row_sumsq");
+}
+
 extern "C" int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream) {
     FLMM_REQUIRE((x && y) || n == 0, "flmm_convert_f64_f32: NULL argument");
     if (n == 0) return FLMM_OK;

@@ -38,9 +38,9 @@ constexpr int TP = 64, TM = 64, TK = 16, NT = 256;
 // (consecutive columns of one output row) coalesce.
 __global__ void __launch_bounds__(NT)
 k_wald_f64(const double* __restrict__ W, const double* __restrict__ A1, const double* __restrict__ rWr, int Neff,
-           int P, int n_real, const double* __restrict__ USt, int64_t ldus, int Mc, const int64_t* __restrict__ rows,
-           double* __restrict__ f, double* __restrict__ beta, double* __restrict__ se, double* __restrict__ sfve,
-           int64_t ldo, double* __restrict__ max_F) {
+           double var_df, int P, int n_real, const double* __restrict__ USt, int64_t ldus, int Mc,
+           const int64_t* __restrict__ rows, double* __restrict__ f, double* __restrict__ beta, double* __restrict__ se,
+           double* __restrict__ sfve, int64_t ldo, double* __restrict__ max_F) {
     __shared__ double Ws[TK][TP + 1];
     __shared__ double As[TK][TP + 1];
     __shared__ double Us[TK][TM + 1];
@@ -84,7 +84,6 @@ k_wald_f64(const double* __restrict__ W, const double* __restrict__ A1, const do
         }
         __syncthreads();
     }
-    const double var_df = static_cast<double>(Neff - 1);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int p = p0 + tx + 16 * r;
@@ -142,6 +141,46 @@ extern "C" int flmm_wald_f64_workspace_bytes(int P, int Neff, size_t* bytes) {
     return FLMM_OK;
 }
 
+namespace {
+
+// rows of [A | B] (rows, ka + kb) from A (rows, ka) and B (rows, kb)
+__global__ void k_concat_rows(const double* __restrict__ A, int64_t lda, int ka, const double* __restrict__ B,
+                              int64_t ldb, int kb, int rows, double* __restrict__ C) {
+    const int k = ka + kb;
+    const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t >= static_cast<int64_t>(rows) * k) return;
+    const int64_t r = t / k;
+    const int c = static_cast<int>(t % k);
+    C[t] = c < ka ? A[r * lda + c] : B[r * ldb + (c - ka)];
+}
+
+__global__ void k_spectrum_pad(const double* __restrict__ s, int k, int n0, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k + n0) out[i] = i < k ? s[i] : 0.0;
+}
+
+int wald_impl(const double* s, int Neff, const double* UYt, int64_t ldu, const double* log_delta, int P, int n_real,
+              const double* USt, int64_t ldus, int Mc, const int64_t* rows, double* f, double* beta, double* se,
+              double* sfve, int64_t ldo, double* max_F, double var_df, void* work, cudaStream_t st) {
+    double* W = static_cast<double*>(work);
+    double* A1 = W + static_cast<size_t>(P) * Neff;
+    double* rWr = A1 + static_cast<size_t>(P) * Neff;
+    k_wald_prep<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(s, Neff, UYt, ldu, log_delta, P, W, A1,
+                                                                             rWr);
+    int rc = check_launch("k_wald_prep");
+    if (rc) return rc;
+    dim3 grid(ceil_div(Mc, TM), ceil_div(P, TP));
+    k_wald_f64<<<grid, NT, 0, st>>>(W, A1, rWr, Neff, var_df, P, n_real, USt, ldus, Mc, rows, f, beta, se, sfve, ldo,
+                                    max_F);
+    return check_launch("k_wald_f64");
+}
+
+size_t lowrank_cat_doubles(int k, int N, int P, int Mc) {
+    return static_cast<size_t>(k + N) * (1 + static_cast<size_t>(P) + static_cast<size_t>(Mc));
+}
+
+}  // namespace
+
 extern "C" int flmm_wald_f64(const double* s, int Neff, const double* UYt, int64_t ldu, const double* log_delta, int P,
                              int n_real, const double* USt, int64_t ldus, int Mc, const int64_t* rows, double* f,
                              double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* work,
@@ -155,15 +194,49 @@ extern "C" int flmm_wald_f64(const double* s, int Neff, const double* UYt, int64
     if (work_bytes < wald_ws(P, Neff))
         return fail(FLMM_ERR_WORKSPACE, "flmm_wald_f64: need %zu bytes, got %zu", wald_ws(P, Neff), work_bytes);
     if (P == 0 || Mc == 0) return FLMM_OK;
+    return wald_impl(s, Neff, UYt, ldu, log_delta, P, n_real, USt, ldus, Mc, rows, f, beta, se, sfve, ldo, max_F,
+                     static_cast<double>(Neff - 1), work, as_stream(stream));
+}
+
+extern "C" int flmm_wald_lowrank_f64_workspace_bytes(int k, int N, int P, int Mc, size_t* bytes) {
+    FLMM_REQUIRE(bytes && k > 0 && N > 0 && P >= 0 && Mc >= 0, "flmm_wald_lowrank_f64_workspace_bytes: bad arguments");
+    *bytes = sizeof(double) * lowrank_cat_doubles(k, N, P, Mc) + 256 + wald_ws(P, k + N);
+    return FLMM_OK;
+}
+
+extern "C" int flmm_wald_lowrank_f64(const double* s, int k, const double* UYt, int64_t ldu, const double* UUYt,
+                                     int64_t lduu, int N, int Neff, const double* log_delta, int P, int n_real,
+                                     const double* USt, int64_t ldus, const double* UUSt, int64_t lduus, int Mc,
+                                     const int64_t* rows, double* f, double* beta, double* se, double* sfve,
+                                     int64_t ldo, double* max_F, void* work, size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(s && UYt && UUYt && log_delta && max_F && work && k > 0 && N > 0 && Neff > 1 && P >= 0 && Mc >= 0 &&
+                     ldu >= k && lduu >= N && ldus >= k && lduus >= N && n_real >= 0 && n_real <= P,
+                 "flmm_wald_lowrank_f64: bad arguments");
+    FLMM_REQUIRE(n_real == 0 || Mc == 0 || (rows && f && beta && se && sfve && ldo >= n_real),
+                 "flmm_wald_lowrank_f64: real-column outputs missing");
+    FLMM_REQUIRE(Mc == 0 || (USt && UUSt), "flmm_wald_lowrank_f64: variant operands missing");
+    size_t need = 0;
+    flmm_wald_lowrank_f64_workspace_bytes(k, N, P, Mc, &need);
+    if (work_bytes < need)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_wald_lowrank_f64: need %zu bytes, got %zu", need, work_bytes);
+    if (P == 0 || Mc == 0) return FLMM_OK;
+    // The off-rank directions enter every form with weight 1 / delta, i.e. as eigen-directions with s = 0: the scan
+    // is the compat scan over [on-rank | off-rank] = k + N directions with var_df = Neff - 1
+    // (fasterlmm/lowrank.py:274-299).
     cudaStream_t st = as_stream(stream);
-    double* W = static_cast<double*>(work);
-    double* A1 = W + static_cast<size_t>(P) * Neff;
-    double* rWr = A1 + static_cast<size_t>(P) * Neff;
-    k_wald_prep<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(s, Neff, UYt, ldu, log_delta, P, W, A1,
-                                                                             rWr);
-    int rc = check_launch("k_wald_prep");
+    const int kc = k + N;
+    double* s_cat = static_cast<double*>(work);
+    double* UY_cat = s_cat + kc;
+    double* US_cat = UY_cat + static_cast<size_t>(P) * kc;
+    void* rest = reinterpret_cast<char*>(work) + ((sizeof(double) * lowrank_cat_doubles(k, N, P, Mc) + 255) / 256) * 256;
+    k_spectrum_pad<<<ceil_div(kc, 256), 256, 0, st>>>(s, k, N, s_cat);
+    int rc = check_launch("k_spectrum_pad");
     if (rc) return rc;
-    dim3 grid(ceil_div(Mc, TM), ceil_div(P, TP));
-    k_wald_f64<<<grid, NT, 0, st>>>(W, A1, rWr, Neff, P, n_real, USt, ldus, Mc, rows, f, beta, se, sfve, ldo, max_F);
-    return check_launch("k_wald_f64");
+    k_concat_rows<<<ceil_div(static_cast<int64_t>(P) * kc, 256), 256, 0, st>>>(UYt, ldu, k, UUYt, lduu, N, P, UY_cat);
+    if ((rc = check_launch("k_concat_rows"))) return rc;
+    k_concat_rows<<<ceil_div(static_cast<int64_t>(Mc) * kc, 256), 256, 0, st>>>(USt, ldus, k, UUSt, lduus, N, Mc,
+                                                                                 US_cat);
+    if ((rc = check_launch("k_concat_rows"))) return rc;
+    return wald_impl(s_cat, kc, UY_cat, kc, log_delta, P, n_real, US_cat, kc, Mc, rows, f, beta, se, sfve, ldo, max_F,
+                     static_cast<double>(Neff - 1), rest, st);
 }

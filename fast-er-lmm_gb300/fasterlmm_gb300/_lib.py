@@ -41,6 +41,8 @@ SIGNATURES: dict[str, list] = {
     "flmm_eigh_batched": [_p, _p, _i, _i, _p, _i, _i, _p, _sz, _p],
     "flmm_eigh_batched_f32_workspace_bytes": [_p, _i, _i, _psz],
     "flmm_eigh_batched_f32": [_p, _p, _i, _i, _p, _p, _sz, _p],
+    "flmm_eigh_refine_workspace_bytes": [_i, _i, _psz],
+    "flmm_eigh_refine_f32": [_p, _p, _p, _p, _i, _i, _p, _sz, _p],
     "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
     "flmm_compat_spectrum_f32": [_p, _i, _i, _p, _p],
     "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],
@@ -56,6 +58,11 @@ SIGNATURES: dict[str, list] = {
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_fit_delta_lowrank_f64": [_p, _i, _p, _i64, _p, _i, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
+    "flmm_wald_lowrank_f64_workspace_bytes": [_i, _i, _i, _i, _psz],
+    "flmm_wald_lowrank_f64": [_p, _i, _p, _i64, _p, _i64, _i, _i, _p, _i, _i, _p, _i64, _p, _i64, _i, _p, _p, _p, _p,
+                              _p, _i64, _p, _p, _sz, _p],
+    "flmm_row_sumsq_f64": [_p, _i64, _i, _i, _p, _p],
     "flmm_shift_diagonal_f64": [_p, _i, _i64, _d, _p],
     "flmm_clamp_nonneg_f64": [_p, _i64, _p, _p],
     "flmm_gls_loss_workspace_bytes": [_i, _i, _i, _i, _psz],

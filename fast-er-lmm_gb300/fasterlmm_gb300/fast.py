@@ -27,12 +27,14 @@ from .core import F64, CovariateBasis, ScanResult, _alloc_outputs, _ptr, _stream
 F16 = torch.float16
 F32 = torch.float32
 
-# Precision of the per-chromosome eigendecompositions.  "f64" (default): the FP64 batched call (EIGH_MODE: 1 =
-# cusolverDnXsyevBatched, 2 = syevd side by side on worker streams; see flmm_eigh_batched).  "f32": one FP32
-# cusolverDnXsyevBatched call for all LOCO kinships.  The FP32 decomposition keeps F, beta, SE, SFVE and -log10 p
-# inside the parity tolerance, but on phenotypes with a flat likelihood (h2 near 0) its ~1e-7 backward error moves
-# the fitted delta, and with it nullh2 = 1 / (1 + delta), by more than 1e-5 relative.
-EIGH_PRECISION = "f64"
+# Precision of the per-chromosome eigendecompositions.
+#   "f32r" (default): one FP32 cusolverDnXsyevBatched call for all LOCO kinships, then one refinement step of the
+#          eigenvectors against the FP64 kinships (flmm_eigh_refine_f32) and FP64 Rayleigh-quotient eigenvalues.
+#   "f32": the FP32 call alone.  F, beta, SE, SFVE and -log10 p stay inside the parity tolerance, but on phenotypes
+#          with a flat likelihood (h2 near 0) the decomposition's ~1e-7 error moves the fitted delta, and with it
+#          nullh2 = 1 / (1 + delta), by more than 1e-5 relative; the refinement step removes that.
+#   "f64": the FP64 batched call (EIGH_MODE: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on worker streams).
+EIGH_PRECISION = "f32r"
 EIGH_MODE = 1
 
 
@@ -284,7 +286,9 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     Kp = torch.empty((len(units), N, N), dtype=F64, device=dev)
     for k_idx, (c, _, _) in enumerate(units):
         project_kinship(kin.kinship(c), basis, Kp[k_idx])
-    if EIGH_PRECISION == "f32":
+    if EIGH_PRECISION == "f32r":
+        Kp, evals = _eigh_batched_f32_refined(ctx, Kp)
+    elif EIGH_PRECISION == "f32":
         Kp, evals = _eigh_batched_f32(ctx, Kp)
     else:
         evals = eigh_batched(Kp, mode=EIGH_MODE)
@@ -324,6 +328,18 @@ def _eigh_batched_f32(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
     w, wb = _work.get(dev, nbytes)
     _lib.call("flmm_eigh_batched_f32", ctx, _ptr(A), N, batch, _ptr(evals), w, wb, st)
     return A, evals
+
+
+def _eigh_batched_f32_refined(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
+    """FP32 eigendecomposition plus one refinement step: (eigenvector rows FP32, FP64 Rayleigh-quotient evals)."""
+    dev = Kp.device
+    batch, N, _ = Kp.shape
+    U, _ = _eigh_batched_f32(ctx, Kp)
+    U_ref = torch.empty_like(U)
+    evals = torch.empty((batch, N), dtype=F64, device=dev)
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_eigh_refine_workspace_bytes", N, batch))
+    _lib.call("flmm_eigh_refine_f32", _ptr(Kp), _ptr(U), _ptr(U_ref), _ptr(evals), N, batch, w, wb, _stream(dev))
+    return U_ref, evals
 
 
 def _spectrum(evals: Tensor, D: int) -> Tensor:

@@ -7,7 +7,9 @@ snp_wald_scan_compat}``, the copies ``fasterlmm.perms`` imported by name (faster
 ``perm_threshold`` in ``fasterlmm.perms`` and in ``fasterlmm.cli`` when that module is loaded (it imports the
 function by name).  The plain GLS names of ``fasterlmm.core`` (rotate, eigendecompose, nLLeval, _profile_loss,
 _profile_loss_per_pheno, fit_delta_grid, snp_wald_scan, loco_scan, single_k_scan; fasterlmm/core.py:89-451) and
-the copies ``fasterlmm.extreme`` imported by name (fasterlmm/extreme.py:19) are rebound to the GLS kernels.  The
+the copies ``fasterlmm.extreme`` imported by name (fasterlmm/extreme.py:19) are rebound to the GLS kernels, and
+the low-rank names of ``fasterlmm.lowrank`` and the copies ``fasterlmm.extreme_scan`` imported (fasterlmm/
+extreme_scan.py:21-22) to the low-rank kernels, so the streamed engine's block loop runs its math on the GPU.  The
 CLI and any user code that goes through those names then runs on the GPU unchanged.  ``uninstall()`` restores
 the originals.
 """
@@ -22,6 +24,9 @@ _CORE_NAMES = ("loco_scan_compat", "single_k_scan_compat", "fastlmm_compat_rotat
                "snp_wald_scan_compat")
 _GLS_NAMES = ("eigendecompose", "rotate", "nLLeval", "_profile_loss", "_profile_loss_per_pheno", "fit_delta_grid",
               "snp_wald_scan", "loco_scan", "single_k_scan", "Spectrum")
+_LOWRANK_NAMES = ("LowRankBasis", "LowRankSpectrum", "lowrank_basis", "rotate_phenos", "lowrank_rotate",
+                  "fit_delta_grid_lowrank", "snp_wald_scan_lowrank", "loco_scan_lowrank", "single_k_scan_lowrank",
+                  "loco_scan_resident")
 
 
 def _set(mod, name, value):
@@ -36,13 +41,13 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
     Patch the reference's modules (imported from sys.modules, or given as ``modules`` = {"core": ..., "perms":
     ..., "cli": ...}).  ``form`` picks the numeric form of the scan drivers.  Returns the patched qualified names.
     """
-    from . import core, gls, perms
+    from . import core, gls, lowrank, perms
     mods = dict(modules or {})
     if not mods:
         import importlib
         mods["core"] = importlib.import_module("fasterlmm.core")
         mods["perms"] = importlib.import_module("fasterlmm.perms")
-        for key in ("cli", "extreme"):
+        for key in ("cli", "extreme", "lowrank", "extreme_scan"):
             if f"fasterlmm.{key}" in sys.modules:
                 mods[key] = sys.modules[f"fasterlmm.{key}"]
     ours = {
@@ -62,6 +67,12 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
             m = mods.get(key)
             if m is not None and hasattr(m, name):
                 _set(m, name, getattr(gls, name))
+                patched.append(f"{m.__name__}.{name}")
+    for name in _LOWRANK_NAMES:
+        for key in ("lowrank", "extreme_scan"):
+            m = mods.get(key)
+            if m is not None and hasattr(m, name):
+                _set(m, name, getattr(lowrank, name))
                 patched.append(f"{m.__name__}.{name}")
     pt = functools.partial(perms.perm_threshold, form=form)
     for key in ("perms", "cli"):

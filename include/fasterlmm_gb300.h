@@ -114,6 +114,14 @@ int flmm_eigh_batched_f32_workspace_bytes(flmm_context* ctx, int N, int batch, s
 int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* evals, void* work, size_t work_bytes,
                           void* stream);
 
+/* One Ogita-Aishima refinement step for the FP32 decomposition of FP64 symmetric A (batch, N, N): U (batch, N, N)
+ * FP32 eigenvector rows in, U_out refined rows out (U_out != U), evals (batch, N) FP64 Rayleigh quotients out.  A U
+ * is formed in double-FP32 arithmetic; the corrections in FP32.  No counterpart in the reference (its eigh is
+ * FP64, fasterlmm/core.py:54-77); it brings the FP32 eigenbasis to the accuracy the fast form's delta fit needs. */
+int flmm_eigh_refine_workspace_bytes(int N, int batch, size_t* bytes);
+int flmm_eigh_refine_f32(const double* A, float* U, float* U_out, double* evals, int N, int batch, void* work,
+                         size_t work_bytes, void* stream);
+
 /* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514); the _f32 form reads FP32 evals. */
 int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream);
 int flmm_compat_spectrum_f32(const float* evals, int N, int D, double* s, void* stream);
@@ -253,6 +261,30 @@ int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int
 int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
+
+/* ---- low-rank path (fasterlmm/lowrank.py): kinship factor G (N, k), k < N --------------------------------------
+ *
+ * s (k,) kept eigenvalues, UYt (P, k) on-rank rotated columns, UUYt (P, N) off-rank residuals, USt / UUSt the same
+ * for a variant block; Neff = N - D (not k). */
+
+/* fit_delta_grid_lowrank (fasterlmm/lowrank.py:172-208): grid + golden section on the low-rank ML loss, with the
+ * off-rank sum of squares yy_off (P,) (see flmm_row_sumsq_f64) and (Neff - k) log(delta) in log det V.  Workspace
+ * as flmm_fit_delta_f64_workspace_bytes(k, n_grid). */
+int flmm_fit_delta_lowrank_f64(const double* s, int k, const double* UYt, int64_t ldu, const double* yy_off, int Neff,
+                               int P, int n_grid, double lo, double hi, int refine, double* log_delta,
+                               int32_t* grid_idx, void* work, size_t work_bytes, void* stream);
+
+/* snp_wald_scan_lowrank (fasterlmm/lowrank.py:239-316): on-rank forms weighted by 1 / (s + delta), off-rank ones
+ * by 1 / delta, df = Neff - 1; outputs as flmm_wald_f64. */
+int flmm_wald_lowrank_f64_workspace_bytes(int k, int N, int P, int Mc, size_t* bytes);
+int flmm_wald_lowrank_f64(const double* s, int k, const double* UYt, int64_t ldu, const double* UUYt, int64_t lduu,
+                          int N, int Neff, const double* log_delta, int P, int n_real, const double* USt, int64_t ldus,
+                          const double* UUSt, int64_t lduus, int Mc, const int64_t* rows, double* f, double* beta,
+                          double* se, double* sfve, int64_t ldo, double* max_F, void* work, size_t work_bytes,
+                          void* stream);
+
+/* out[r] = sum_c A[r, c]^2 (off-rank residual sums of squares). */
+int flmm_row_sumsq_f64(const double* A, int64_t lda, int rows, int cols, double* out, void* stream);
 
 /* ---- plain GLS path (fasterlmm/core.py:89-451): covariates kept in the model ------------------------------------
  *

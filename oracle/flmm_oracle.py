@@ -421,6 +421,170 @@ def single_k_scan(Z: np.ndarray, X: np.ndarray, Y: np.ndarray, *, n_real: int | 
 
 
 # --------------------------------------------------------------------------------------------------------------
+# low-rank path: kinship factor G (N, k) with k < N, the N - k null directions carried analytically
+# --------------------------------------------------------------------------------------------------------------
+
+def lowrank_basis(G: np.ndarray, X: np.ndarray, *, sv_floor: float = 1e-10) -> dict:
+    """
+    fastlmm's k < N spectral decomposition (fasterlmm/lowrank.py:59-96): G_ = G - X Xpinv G; eigh of G_^T G_
+    (k < N) or of G_ G_^T / M_kin (k >= N); keep singular values above sv_floor; U_eff = G_ V / sv, s = sv^2 / M_kin.
+    """
+    N, k_in = G.shape
+    D = X.shape[1]
+    Xpinv = np.linalg.pinv(X)
+    G_ = G - X @ (Xpinv @ G)
+    if k_in < N:
+        evals, V = np.linalg.eigh(G_.T @ G_)
+        sv = np.sqrt(np.maximum(evals, 0.0))
+        keep = sv > sv_floor
+        sv, V = sv[keep], V[:, keep]
+        U_eff = G_ @ (V / sv)
+        s = sv * sv / k_in
+    else:
+        evals, U = np.linalg.eigh((G_ @ G_.T) / k_in)
+        keep = np.maximum(evals, 0.0) > sv_floor * sv_floor / k_in
+        s = np.maximum(evals[keep], 0.0)
+        U_eff = np.ascontiguousarray(U[:, keep])
+    return {"s": s, "U_eff": U_eff, "X": X, "Xpinv": Xpinv, "Neff": N - D}
+
+
+def rotate_phenos(basis: dict, Y: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """On-rank UY = U_eff^T Y_r and off-rank residual UUY = Y_r - U_eff UY (fasterlmm/lowrank.py:99-111)."""
+    Y_r = Y - basis["X"] @ (basis["Xpinv"] @ Y)
+    UY = basis["U_eff"].T @ Y_r
+    return UY, Y_r - basis["U_eff"] @ UY
+
+
+def lowrank_rotate(G: np.ndarray, X: np.ndarray, Y: np.ndarray, *, sv_floor: float = 1e-10) -> dict:
+    """lowrank_basis + rotate_phenos (fasterlmm/lowrank.py:114-125)."""
+    spec = lowrank_basis(G, X, sv_floor=sv_floor)
+    spec["UY"], spec["UUY"] = rotate_phenos(spec, Y)
+    return spec
+
+
+def profile_loss_lowrank(log_delta: np.ndarray, s: np.ndarray, UY: np.ndarray, yy_off: np.ndarray,
+                         Neff: int) -> np.ndarray:
+    """
+    (G, P) ML -2 log L of the low-rank model (fasterlmm/lowrank.py:131-151): rWr = sum UY^2 / (s + delta) +
+    yy_off / delta, log det = sum log(s + delta) + (Neff - k) log delta.
+    """
+    k = s.shape[0]
+    delta = np.exp(log_delta)
+    Sd = s[None, :] + delta[:, None]
+    rWr = np.maximum((1.0 / Sd) @ (UY * UY) + yy_off[None, :] / delta[:, None], pos_floor())
+    logdet = np.log(Sd).sum(axis=1) + (Neff - k) * np.log(delta)
+    return Neff * (LOG2PI + np.log(rWr / Neff) + 1.0) + logdet[:, None]
+
+
+def profile_loss_lowrank_per_pheno(log_delta: np.ndarray, s: np.ndarray, UY: np.ndarray, yy_off: np.ndarray,
+                                   Neff: int) -> np.ndarray:
+    """One log delta per column (fasterlmm/lowrank.py:154-169)."""
+    k = s.shape[0]
+    delta = np.exp(log_delta)
+    Sd = s[None, :] + delta[:, None]
+    rWr = np.maximum(((1.0 / Sd) * UY.T * UY.T).sum(axis=1) + yy_off / delta, pos_floor())
+    logdet = np.log(Sd).sum(axis=1) + (Neff - k) * np.log(delta)
+    return Neff * (LOG2PI + np.log(rWr / Neff) + 1.0) + logdet
+
+
+def fit_delta_grid_lowrank(spec: dict, *, n_grid: int = 64, log_delta_min: float = -10.0,
+                           log_delta_max: float = 10.0, refine: bool = True) -> np.ndarray:
+    """Grid argmin then 50 golden-section steps on the low-rank loss (fasterlmm/lowrank.py:172-208)."""
+    s, UY, Neff = spec["s"], spec["UY"], spec["Neff"]
+    yy_off = (spec["UUY"] * spec["UUY"]).sum(axis=0)
+    grid = delta_grid(n_grid, log_delta_min, log_delta_max)
+    idx = profile_loss_lowrank(grid, s, UY, yy_off, Neff).argmin(axis=0)
+    if not refine:
+        return grid[idx]
+    a = grid[np.clip(idx - 1, 0, n_grid - 1)].copy()
+    b = grid[np.clip(idx + 1, 0, n_grid - 1)].copy()
+    inv_phi = 2.0 / (1.0 + 5.0 ** 0.5)
+    inv_phi2 = inv_phi * inv_phi
+    c = a + inv_phi2 * (b - a)
+    d = a + inv_phi * (b - a)
+    fc = profile_loss_lowrank_per_pheno(c, s, UY, yy_off, Neff)
+    fd = profile_loss_lowrank_per_pheno(d, s, UY, yy_off, Neff)
+    for _ in range(50):
+        cond = fc < fd
+        b = np.where(cond, d, b)
+        a = np.where(cond, a, c)
+        c = a + inv_phi2 * (b - a)
+        d = a + inv_phi * (b - a)
+        fc = profile_loss_lowrank_per_pheno(c, s, UY, yy_off, Neff)
+        fd = profile_loss_lowrank_per_pheno(d, s, UY, yy_off, Neff)
+    return np.clip(0.5 * (a + b), log_delta_min, log_delta_max)
+
+
+def snp_wald_scan_lowrank(spec: dict, log_delta: np.ndarray, S: np.ndarray, *, n_real: int | None = None) -> dict:
+    """
+    Low-rank Wald scan (fasterlmm/lowrank.py:239-316): every quadratic form has an on-rank part weighted by
+    1 / (s + delta) and an off-rank part weighted by 1 / delta (UUS = S_r - U US, UUY as rotated).
+    """
+    s, UY, UUY, X, Xpinv, U = spec["s"], spec["UY"], spec["UUY"], spec["X"], spec["Xpinv"], spec["U_eff"]
+    Neff = spec["Neff"]
+    P = UY.shape[1]
+    M = S.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    floor = pos_floor()
+    delta = np.exp(log_delta)
+    w = 1.0 / (s[None, :] + delta[:, None])
+    rWr = np.maximum((w * UY.T * UY.T).sum(axis=1) + (UUY * UUY).sum(axis=0) / delta, floor)
+    S_r = S - X @ (Xpinv @ S)
+    US = U.T @ S_r
+    UUS = S_r - U @ US
+    sWs = w @ (US * US) + (UUS * UUS).sum(axis=0)[None, :] / delta[:, None]
+    denom = np.maximum(sWs, floor)
+    sWy = (w * UY.T) @ US + (UUS.T @ UUY).T / delta[:, None]
+    beta = sWy / denom
+    rss = np.maximum(rWr[:, None] - sWy * sWy / denom, floor)
+    var_beta = rss / (Neff - 1) / denom
+    F = beta * beta / var_beta
+    max_F = F.max(axis=1) if M > 0 else np.full(P, -np.inf)
+    r = slice(0, n_real)
+    sfve = np.sqrt(np.maximum((sWy[r] * sWy[r]) / (denom[r] * rWr[r, None]), 0.0))
+    h2 = 1.0 / (1.0 + np.exp(log_delta[:n_real]))
+    return {"f": F[r].T.copy(), "beta": beta[r].T.copy(), "se": np.sqrt(var_beta[r]).T.copy(), "sfve": sfve.T.copy(),
+            "nullh2": np.broadcast_to(h2[None, :], (M, n_real)).copy(), "max_F": max_F}
+
+
+def loco_scan_lowrank(G: np.ndarray, g_chrom: np.ndarray, Z: np.ndarray, z_chrom: np.ndarray, X: np.ndarray,
+                      Y: np.ndarray, *, n_real: int | None = None, on_chrom=None) -> dict:
+    """Low-rank LOCO driver (fasterlmm/lowrank.py:322-359): the kinship factor drops chromosome c's markers."""
+    M = Z.shape[1]
+    P = Y.shape[1]
+    n_real = P if n_real is None else min(n_real, P)
+    out = {k: np.zeros((M, n_real)) for k in ("f", "beta", "se", "sfve", "nullh2")}
+    max_F = np.full(P, -np.inf)
+    chroms = sorted(np.unique(z_chrom).tolist())
+    log_deltas = {}
+    for k_idx, c in enumerate(chroms):
+        test_mask = np.asarray(z_chrom) == c
+        spec = lowrank_rotate(G[:, np.asarray(g_chrom) != c], X, Y)
+        ld = fit_delta_grid_lowrank(spec)
+        log_deltas[c] = ld
+        res = snp_wald_scan_lowrank(spec, ld, Z[:, test_mask], n_real=n_real)
+        if n_real > 0:
+            for key in out:
+                out[key][test_mask, :] = res[key]
+        max_F = np.maximum(max_F, res["max_F"])
+        if on_chrom is not None:
+            on_chrom(k_idx + 1, len(chroms))
+    out["max_F"] = max_F
+    out["log_delta"] = log_deltas
+    return out
+
+
+def single_k_scan_lowrank(G: np.ndarray, Z: np.ndarray, X: np.ndarray, Y: np.ndarray, *,
+                          n_real: int | None = None) -> dict:
+    """Low-rank whole-genome scan (fasterlmm/lowrank.py:362-373)."""
+    spec = lowrank_rotate(G, X, Y)
+    ld = fit_delta_grid_lowrank(spec)
+    res = snp_wald_scan_lowrank(spec, ld, Z, n_real=n_real)
+    res["log_delta"] = ld
+    return res
+
+
+# --------------------------------------------------------------------------------------------------------------
 # permutations and the batch driver
 # --------------------------------------------------------------------------------------------------------------
 

@@ -175,18 +175,68 @@ def _plain_fixtures(core, fio, torch):
                         **_res_dict(res1, "sk_"))
 
 
+def _lowrank_fixtures(ref_path, fio, torch):
+    """The low-rank path (fasterlmm/lowrank.py) and its resident block engine (fasterlmm/extreme_scan.py)."""
+    import fasterlmm.lowrank as lr
+    import fasterlmm.extreme_scan as xs
+    rng = np.random.default_rng(91)
+    # components: k < N (the k x k Gram branch) and k >= N (the N x N branch)
+    Nt, Pt = 90, 4
+    Xc = torch.from_numpy(np.concatenate([np.ones((Nt, 1)), rng.normal(size=(Nt, 2))], axis=1))
+    Yc = torch.from_numpy(rng.normal(size=(Nt, Pt)))
+    S = fio.standardise_columns(torch.from_numpy(rng.integers(0, 3, size=(Nt, 70)).astype(np.float64)))
+    out = {"X": Xc.numpy(), "Y": Yc.numpy(), "S": S.numpy()}
+    for tag, k in (("lo", 40), ("hi", 120)):
+        G = fio.standardise_columns(torch.from_numpy(rng.integers(0, 3, size=(Nt, k)).astype(np.float64)))
+        spec = lr.lowrank_rotate(G, Xc, Yc)
+        yy_off = (spec.UUY * spec.UUY).sum(dim=0)
+        grid = torch.linspace(-10.0, 10.0, 64, dtype=torch.float64)
+        ld = lr.fit_delta_grid_lowrank(spec)
+        res = lr.snp_wald_scan_lowrank(spec, ld, S, n_real=2)
+        out.update({f"{tag}_G": G.numpy(), f"{tag}_s": spec.s.numpy(), f"{tag}_UY": spec.UY.numpy(),
+                    f"{tag}_UUY": spec.UUY.numpy(), f"{tag}_Neff": spec.Neff,
+                    f"{tag}_grid_loss": lr._profile_loss_lowrank(grid, spec.s, spec.UY, yy_off, spec.Neff).numpy(),
+                    f"{tag}_log_delta": ld.numpy(), f"{tag}_log_delta_grid": lr.fit_delta_grid_lowrank(spec, refine=False).numpy(),
+                    **_res_dict(res, f"{tag}_")})
+    np.savez_compressed(HERE / "lowrank_components.npz", **out)
+
+    # LOCO over a pruned kinship factor, real + permuted columns, the single-K driver and the resident block
+    # engine (FP64 and its FP32 default) with blocks that split chromosomes
+    d = make_dataset(100, 700, 5, 3, 5, seed=777, config_id=9, k_lo=2, k_hi=8)
+    dk = make_dataset(100, 300, 5, 1, 1, seed=778, config_id=10)
+    B, n_perm = 5, 2
+    N = d.X.shape[0]
+    orders = np.stack([np.random.default_rng([19930909, b]).random((n_perm, N)).argsort(axis=1) for b in range(B)])
+    y_real = d.Y[:, :B]
+    Y_all = np.concatenate([y_real] + [y_real[orders[b, k], b][:, None] for b in range(B) for k in range(n_perm)],
+                           axis=1)
+    Z = fio.standardise_columns(torch.from_numpy(d.Z_float()))
+    G = fio.standardise_columns(torch.from_numpy(dk.Z_float()))
+    X = torch.from_numpy(d.X.copy())
+    Yt = torch.from_numpy(Y_all)
+    res = lr.loco_scan_lowrank(G, dk.chrom, Z, d.chrom, X, Yt, n_real=B)
+    res1 = lr.single_k_scan_lowrank(G, Z, X, Yt, n_real=B)
+    res64 = xs.loco_scan_resident(Z, d.chrom, G, dk.chrom, X, Yt, n_real=B, block_size=37, dtype=torch.float64)
+    res32 = xs.loco_scan_resident(Z.float(), d.chrom, G, dk.chrom, X, Yt, n_real=B, block_size=37)
+    np.savez_compressed(HERE / "lowrank_loco.npz", **_inputs(d), G_kin=dk.G, chrom_kin=dk.chrom, Y_all=Y_all,
+                        n_real=B, **_res_dict(res), **_res_dict(res1, "sk_"), **_res_dict(res64, "res64_"),
+                        **{k: v.astype(np.float32) for k, v in _res_dict(res32, "res32_").items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("FASTERLMM_REFERENCE", ""))
-    ap.add_argument("--only", choices=["compat", "plain"], default=None,
-                    help="write only the compat-path fixtures or only the plain-GLS fixtures")
+    ap.add_argument("--only", choices=["compat", "plain", "lowrank"], default=None,
+                    help="write only the compat-path, the plain-GLS or the low-rank fixtures")
     args = ap.parse_args()
     if not args.reference:
         sys.exit("pass --reference PATH (or set FASTERLMM_REFERENCE) to the reference checkout")
     core, fio, perms, torch = _import_reference(args.reference)
-    if args.only != "compat":
+    if args.only in (None, "plain"):
         _plain_fixtures(core, fio, torch)
-    if args.only == "plain":
+    if args.only in (None, "lowrank"):
+        _lowrank_fixtures(args.reference, fio, torch)
+    if args.only in ("plain", "lowrank"):
         return
 
     # 1. the 150 x 1,500 / 16-chromosome workload through perm_threshold, reference defaults (64-pt grid)

@@ -167,3 +167,44 @@ def test_oracle_plain_loco_and_single_k(golden):
         assert np.abs(res["log_delta"][c] - ref_ld[i]).max() < 1e-3
     res1 = orc.single_k_scan(Zs, g["X"], g["Y_all"], n_real=B)
     assert_scan_close(res1, g, prefix="sk_")
+
+
+def test_oracle_lowrank_components(golden):
+    """Low-rank restatement vs the reference's lowrank_rotate / loss / fit / Wald, both rank branches."""
+    g = golden("lowrank_components")
+    for tag in ("lo", "hi"):
+        spec = orc.lowrank_rotate(g[f"{tag}_G"], g["X"], g["Y"])
+        assert spec["Neff"] == int(g[f"{tag}_Neff"])
+        # In the k >= N branch the reference keeps eigenvalues above (1e-10)^2 / k, which admits O(1e-17) rounding
+        # noise of the projected-out directions; how many such directions are kept varies with rounding, and a kept
+        # noise direction (s ~ 0, weight 1 / delta) counts exactly like an off-rank one.  Compare the real spectrum
+        # and the loss, which does not depend on that split.
+        big, gbig = spec["s"] > 1e-12, g[f"{tag}_s"] > 1e-12
+        _close(spec["s"][big], g[f"{tag}_s"][gbig], atol=1e-10)
+        _close(spec["UY"][big] ** 2, g[f"{tag}_UY"][gbig] ** 2, atol=1e-10)
+        grid = orc.delta_grid(64, -10.0, 10.0)
+        for s_, UY_, UUY_ in ((spec["s"], spec["UY"], spec["UUY"]), (g[f"{tag}_s"], g[f"{tag}_UY"], g[f"{tag}_UUY"])):
+            _close(orc.profile_loss_lowrank(grid, s_, UY_, (UUY_ ** 2).sum(axis=0), spec["Neff"]),
+                   g[f"{tag}_grid_loss"], rtol=1e-10, atol=1e-9)
+        ref = {**spec, "s": g[f"{tag}_s"], "UY": g[f"{tag}_UY"], "UUY": g[f"{tag}_UUY"]}
+        assert np.array_equal(orc.fit_delta_grid_lowrank(ref, refine=False), g[f"{tag}_log_delta_grid"])
+        ld = orc.fit_delta_grid_lowrank(ref)
+        assert np.abs(ld - g[f"{tag}_log_delta"]).max() < 1e-3
+        res = orc.snp_wald_scan_lowrank(spec, g[f"{tag}_log_delta"], g["S"], n_real=2)
+        for k in DETAIL + ("max_F",):
+            _close(res[k], g[f"{tag}_{k}"])
+
+
+def test_oracle_lowrank_loco_single_k_and_resident(golden):
+    g = golden("lowrank_loco")
+    Z = orc.standardise_columns(z_float(g["G"]))
+    G = orc.standardise_columns(z_float(g["G_kin"]))
+    B = int(g["n_real"])
+    seen = []
+    res = orc.loco_scan_lowrank(G, g["chrom_kin"], Z, g["chrom"], g["X"], g["Y_all"], n_real=B,
+                                on_chrom=lambda k, n: seen.append(k))
+    assert seen == list(range(1, len(np.unique(g["chrom"])) + 1))
+    assert_scan_close(res, g)
+    assert_scan_close(res, g, prefix="res64_")  # the reference's resident block engine gives the same scan
+    res1 = orc.single_k_scan_lowrank(G, Z, g["X"], g["Y_all"], n_real=B)
+    assert_scan_close(res1, g, prefix="sk_")
