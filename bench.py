@@ -257,10 +257,13 @@ def run_ours(args):
         R = interp_nodes(w["log_delta_min"], w["log_delta_max"])[1]
         exec_flop = 3 * 2.0 * (Neff + R) * P * mc_mean
         peak = peaks["tensor_tflops"]
+        # DRAM bytes per launch from the committed ncu summary of this workload (measured at full size)
         traffic = None
-        tp = ROOT / "profiles" / "wald_traffic.json"
-        if tp.exists():
-            traffic = json.loads(tp.read_text()).get("bytes_per_launch_scaled")
+        tp = ROOT / "profiles" / f"wald_k_tc2_{WORKLOAD}.md"
+        if tp.exists() and args.B is None and args.M is None and args.form == "fast":
+            for line in tp.read_text().splitlines():
+                if line.startswith("traffic_bytes_per_launch:"):
+                    traffic = int(line.split(":")[1])
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": "k_tc<wald> (fused split-FP16 Wald)", "launch_ms": 1e3 * mean_s,
                 "algorithmic_flop_per_launch": alg_flop, "executed_flop_per_launch": exec_flop,
