@@ -1,0 +1,195 @@
+// Exact evaluation of the fast delta fit's derivative and the safeguarded Newton refinement, shared by the grid
+// path (flmm_delta_fast.cu) and the learned-proposal path (flmm_delta_learned.cu).
+#pragma once
+
+#include <math.h>
+
+#include "flmm_common.cuh"
+
+namespace flmm {
+namespace dfit {
+
+struct NewtonEval {
+    double g;      // T1 - Neff S2 / S1 (sign of d loss / d log delta)
+    double gp;     // dg / dx
+    double loss;   // Neff log S1 + sum log (s + delta), up to constants
+};
+
+// One evaluation by a warp at x = log delta (x is warp-uniform), all in FP32.
+//
+// g is formed around the centre c = 1 / (sbar + delta), sbar the mean eigenvalue: with d_n = r_n - c =
+// (sbar - s_n) r_n c,
+//     g = sum d - Neff (c E1 + E2) / (c U + E1),   U = sum u^2, E1 = sum u^2 d, E2 = sum u^2 d^2,
+// which is T1 - Neff S2 / S1 rearranged so that no O(r) terms cancel: when delta >> s the r_n are nearly equal and
+// the information in g is in their O(s / delta) spread, which the centred terms carry at full FP32 precision
+// (compensated sums for the first-order terms).  delta = exp(x) is formed from a hi / lo split of x so that it is
+// exact to FP32 rounding at any x.
+struct EvalPoint {
+    float delta, c;
+};
+
+__device__ __forceinline__ EvalPoint eval_point(double x, float sbar) {
+    const float xh = static_cast<float>(x);
+    const float xl = static_cast<float>(x - static_cast<double>(xh));
+    const float delta = expf(xh) * (1.0f + xl);
+    return {delta, 1.0f / (sbar + delta)};
+}
+
+// per-lane partial sums of one evaluation
+struct EvalSums {
+    float d1 = 0.f, cd1 = 0.f, e1 = 0.f, ce1 = 0.f, e2 = 0.f, e3 = 0.f, f2 = 0.f, sl = 0.f;
+
+    __device__ __forceinline__ void add(float sn, float dsn, float uu, const EvalPoint& pt, bool want_loss) {
+        const float sd = sn + pt.delta;
+        const float r = __frcp_rn(sd);  // correctly rounded, cheaper than the IEEE division
+        const float d = dsn * r * pt.c;
+        neumaier(d1, cd1, d);
+        neumaier(e1, ce1, uu * d);
+        const float ud = uu * d * d;
+        e2 += ud;
+        e3 += ud * d;
+        f2 += d * d;
+        if (want_loss) sl += __logf(sd);
+    }
+};
+
+__device__ inline NewtonEval finish_eval(const EvalSums& t, float U, int Neff, const EvalPoint& pt, bool want_loss) {
+    const float D1 = warp_sum_pair(t.d1, t.cd1);
+    const float E1 = warp_sum_pair(t.e1, t.ce1);
+    const float E2 = warp_sum(t.e2);
+    const float E3 = warp_sum(t.e3);
+    const float F2 = warp_sum(t.f2);
+    const float c = pt.c;
+    NewtonEval e;
+    const float neff = static_cast<float>(Neff);
+    if (U > 0.0f) {
+        e.g = D1 - neff * (c * E1 + E2) / (c * U + E1);
+        // dg/dx = delta (-T2 + Neff (2 S3 / S1 - (S2 / S1)^2)) in the same centred sums: with F2 = sum d^2,
+        // E3 = sum u^2 d^3, a = E1 / (c U), b = E2 / (c^2 U), t3 = E3 / (c^3 U) one has T2 = Neff c^2 + 2 c D1 + F2,
+        // S1 = c U (1 + a), S2 = c^2 U (1 + 2a + b), S3 = c^3 U (1 + 3a + 3b + t3), and the O(1) terms cancel exactly
+        const float a = E1 / (c * U), b = E2 / (c * c * U), t3 = E3 / (c * c * c * U);
+        const float br = -2.0f * D1 / (c * neff) - F2 / (c * c * neff) + (2.0f * a + 4.0f * b + 2.0f * t3) / (1.0f + a) -
+                         (a + b) * (a + b) / ((1.0f + a) * (1.0f + a));
+        e.gp = static_cast<double>(pt.delta) * neff * c * c * br;
+    } else {  // all-zero rotated column: the loss only grows with delta
+        e.g = 1.0;
+        e.gp = 1.0;
+    }
+    e.loss = 0.0;
+    if (want_loss) e.loss = neff * logf(fmaxf(c * U + E1, 1e-30f)) + warp_sum(t.sl);
+    return e;
+}
+
+// Evaluator over a column read from global (L1 / L2) memory on every evaluation; dsb[n] = sbar - s[n] and the
+// column's sum of squares U are precomputed.  (Keeping the squares in registers instead cost occupancy and ran
+// slower.)
+struct GlobalColumn {
+    const float* s32;
+    const float* dsb;
+    const float* u;
+    int Neff;
+    float sbar, U;
+
+    __device__ NewtonEval operator()(double x, bool want_loss) const {
+        const int lane = threadIdx.x & 31;
+        const EvalPoint pt = eval_point(x, sbar);
+        EvalSums t;
+        for (int n = lane; n < Neff; n += 32) t.add(s32[n], dsb[n], u[n] * u[n], pt, want_loss);
+        return finish_eval(t, U, Neff, pt, want_loss);
+    }
+};
+
+// Safeguarded Newton on g in a bracket with g(lo) < 0 < g(hi), starting at x0 (the bracket's midpoint if x0 is not
+// inside).  The FP32 sums put a noise floor of ~1e-7 on x: near the root the Newton steps stop shrinking and jump
+// around the root by that much, so the iteration ends once a step or the bracket is below 1e-7.
+template <class Ev>
+__device__ double newton_in_bracket(const Ev& ev, double lo, double hi, double x0, const NewtonEval* first = nullptr) {
+    const bool inside = x0 > lo && x0 < hi;
+    double x = inside ? x0 : 0.5 * (lo + hi);
+    for (int it = 0; it < 60; ++it) {
+        const NewtonEval e = (it == 0 && inside && first) ? *first : ev(x, false);
+        if (e.g == 0.0) break;
+        if (e.g < 0.0) lo = x; else hi = x;
+        double xn = x - e.g / e.gp;
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const double stepx = fabs(xn - x);
+        x = xn;
+        if (stepx < 1e-7 || hi - lo < 1e-7) break;
+    }
+    return x;
+}
+
+// log delta of one column from its grid argmin i (warp-uniform result)
+template <class Ev>
+__device__ double refine_column(const Ev& ev, const double* __restrict__ grid, int G, int i, int refine) {
+    double out = grid[i];
+    if (refine && i > 0 && i < G - 1) {
+        // the usual case: d loss / d log delta changes sign between the argmin's neighbours
+        const double a = grid[i - 1], b = grid[i + 1];
+        if (ev(a, false).g < 0.0 && ev(b, false).g > 0.0) return newton_in_bracket(ev, a, b, grid[i]);
+    }
+    if (refine && G > 1) {
+        // The FP32 grid argmin is only as good as the FP32 loss (~1e-4 absolute); on flat losses it can sit several
+        // nodes from the minimum.  The exact derivative sign at that node says which side the minimum is on, and a
+        // binary search over the grid nodes on that side finds where d loss / d log delta changes sign, so the
+        // bracket [grid[i-1], grid[i+1]] always contains the minimum (for losses with one minimum on that side).
+        const double gi = ev(grid[i], false).g;
+        if (gi < 0.0) {
+            if (ev(grid[G - 1], false).g < 0.0) {
+                i = G - 1;  // still falling at the top of the grid
+            } else {
+                int lo = i, hi = G - 1;  // g(lo) < 0 <= g(hi)
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (ev(grid[mid], false).g < 0.0) lo = mid; else hi = mid;
+                }
+                i = hi;
+            }
+        } else if (gi > 0.0) {
+            if (ev(grid[0], false).g > 0.0) {
+                i = 0;  // already rising at the bottom of the grid
+            } else {
+                int lo = 0, hi = i;  // g(lo) <= 0 < g(hi)
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (ev(grid[mid], false).g > 0.0) hi = mid; else lo = mid;
+                }
+                i = lo;
+            }
+        }
+        const double a = grid[max(i - 1, 0)], b = grid[min(i + 1, G - 1)];
+        const NewtonEval ea = ev(a, false);
+        const NewtonEval eb = ev(b, false);
+        if (ea.g >= 0.0 && eb.g <= 0.0) {
+            // loss rises from a and falls towards b: the minimum is an edge
+            out = (ev(a, true).loss <= ev(b, true).loss) ? a : b;
+        } else if (ea.g >= 0.0) {
+            out = a;
+        } else if (eb.g <= 0.0) {
+            out = b;
+        } else {
+            out = newton_in_bracket(ev, a, b, grid[i]);
+        }
+    }
+    return out;
+}
+
+
+// Spectrum in shared memory as FP32 (s32) and sbar - s (dsb), sbar the mean eigenvalue; all threads call it.
+__device__ inline float load_spectrum(const double* __restrict__ s, int Neff, float* s32, float* dsb, float* sbar_s) {
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) s32[n] = static_cast<float>(s[n]);
+    if (threadIdx.x < 32) {
+        double acc = 0.0;
+        for (int n = threadIdx.x; n < Neff; n += 32) acc += s[n];
+        acc = warp_sum(acc);
+        if (threadIdx.x == 0) *sbar_s = static_cast<float>(acc / Neff);
+    }
+    __syncthreads();
+    const float sbar = *sbar_s;
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) dsb[n] = sbar - s32[n];
+    __syncthreads();
+    return sbar;
+}
+
+}  // namespace dfit
+}  // namespace flmm

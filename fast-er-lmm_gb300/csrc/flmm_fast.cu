@@ -44,8 +44,11 @@ struct Cfg {
     static constexpr uint32_t kSBO = 8u * BK * 2u;             // bytes between 8-row groups
     static constexpr int kTmemCols = NG * kBN * 2;
     static constexpr int kBarBytes = 256;
-    static constexpr int kSmemBytes = kStages * kStageBytes + kBarBytes + 1024;  // + alignment slack
-    static_assert(kStageBytes * kStages + kBarBytes + 1024 <= 227 * 1024, "shared memory budget");
+    // per epilogue warp: the scales of its 64 variants (two products) and their output rows, staged once per tile
+    static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
+    static constexpr int kEpiBytes = 8 * kEpiWarpBytes;
+    static constexpr int kSmemBytes = kStages * kStageBytes + kBarBytes + kEpiBytes + 1024;  // + alignment slack
+    static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
 };
 
 struct TcMaps {
@@ -78,24 +81,6 @@ struct TcArgs {
     double* max_F;
 };
 
-// 16 consecutive row scales (fewer than 16 valid: the rest read as 0); all lanes of a warp read the same addresses
-__device__ __forceinline__ void load16(const float* __restrict__ p, int n, float (&v)[16]) {
-    if (n >= 16 && (reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
-        const float4* p4 = reinterpret_cast<const float4*>(p);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float4 x = __ldg(p4 + k);
-            v[4 * k] = x.x;
-            v[4 * k + 1] = x.y;
-            v[4 * k + 2] = x.z;
-            v[4 * k + 3] = x.w;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) v[k] = k < n ? __ldg(p + k) : 0.0f;
-    }
-}
-
 // hardware reciprocal (relative error ~2^-23); arguments here are clamped to normal numbers
 __device__ __forceinline__ float rcp_approx(float x) {
     float y;
@@ -115,6 +100,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     uint64_t* acc_empty = acc_full + 2;              // [2]
     uint64_t* final_bar = acc_empty + 2;             // [1]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(final_bar + 1);
+    uint8_t* epi_smem = smem + C::kStages * C::kStageBytes + C::kBarBytes;  // [8][kEpiWarpBytes]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
@@ -220,33 +206,71 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
         }
     } else {
         // ---- epilogue: warps 2..9.  Warp w reads TMEM lanes 32 (w % 4) .. +31 (thread = one accumulator row) and
-        // half (w - 2) / 4 of the tile's columns, so two warps share each lane quarter.
+        // half (w - 2) / 4 of the tile's columns, so two warps share each lane quarter.  Each warp stages the scales
+        // (and output rows) of its 64 variants in its own shared-memory slot before waiting for the accumulator,
+        // so those loads overlap the MMAs instead of stalling the epilogue.
         const int q = warp & 3;
         const int cbeg = ((warp - 2) >> 2) * (kBN / 2);
         const int r = q * 32 + lane;
+        float* sc1 = reinterpret_cast<float*>(epi_smem + (warp - 2) * C::kEpiWarpBytes);  // [64]
+        float* sc2 = sc1 + 64;                                                           // [64]
+        int64_t* rws = reinterpret_cast<int64_t*>(sc2 + 64);                             // [64]
         int ab = 0;
         uint32_t aphase = 0;
         for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
             const int ta = t / tiles_b, tb = t % tiles_b;
+            const int nvalid = min(kBN, args.Nr - tb * kBN);  // columns of this tile inside B
+            const bool real_tile = NG == 2 && ta * kBM < args.n_real;  // uniform over the CTA
+            __syncwarp();  // every lane is done with the previous tile's slot
+            for (int k = lane; k < kBN / 2; k += 32) {
+                const int c = cbeg + k;
+                const int m = tb * kBN + c;
+                const bool ok = c < nvalid;
+                sc1[k] = ok ? args.sb[m] : 0.0f;
+                if constexpr (NG == 2) {
+                    sc2[k] = ok ? args.sb2[m] : 0.0f;
+                    if (real_tile) rws[k] = ok ? args.rows[m] : 0;
+                }
+            }
+            __syncwarp();
             if (!mbar_wait(&acc_full[ab], aphase, args.err, 4)) break;
             fence_after_sync();
             const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
             const int i = ta * kBM + r;  // A row
             const bool row_ok = i < args.Mr;
-            const int nvalid = min(kBN, args.Nr - tb * kBN);  // columns of this tile inside B
             if constexpr (NG == 1) {
                 const float sa = row_ok ? args.sa[i] : 0.0f;
                 float* crow = args.C + static_cast<int64_t>(i) * args.ldc + tb * kBN;
                 for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-                    float v[16], sbv[16];
-                    load16(args.sb + tb * kBN + c0, nvalid - c0, sbv);
+                    float v[16];
                     tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
                     if (!row_ok) continue;
+                    const float* sc = sc1 + (c0 - cbeg);
+                    float* dst = crow + c0;
+                    if (c0 + 16 <= nvalid && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+                        // a thread owns 16 consecutive outputs of its row: four 16-byte stores
+                        float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+                        for (int q4 = 0; q4 < 4; ++q4) {
+                            float4 x = make_float4(v[4 * q4] * sa * sc[4 * q4], v[4 * q4 + 1] * sa * sc[4 * q4 + 1],
+                                                   v[4 * q4 + 2] * sa * sc[4 * q4 + 2],
+                                                   v[4 * q4 + 3] * sa * sc[4 * q4 + 3]);
+                            if (args.accumulate) {
+                                const float4 o = d4[q4];
+                                x.x += o.x;
+                                x.y += o.y;
+                                x.z += o.z;
+                                x.w += o.w;
+                            }
+                            d4[q4] = x;
+                        }
+                        continue;
+                    }
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         if (c0 + j < nvalid) {
-                            const float x = v[j] * sa * sbv[j];
-                            crow[c0 + j] = args.accumulate ? crow[c0 + j] + x : x;
+                            const float x = v[j] * sa * sc[j];
+                            dst[j] = args.accumulate ? dst[j] + x : x;
                         }
                     }
                 }
@@ -259,22 +283,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                 const float sa2 = row_ok ? args.sa2[p] : 0.0f;
                 const float rwr = row_ok ? args.rWr[p] : 1.0f;
                 const float df = args.var_df;
-                const bool real_tile = ta * kBM < args.n_real;  // uniform over the CTA
                 const bool real = row_ok && p < args.n_real;
                 float colmax = -INFINITY;
                 bool col_nan = false;
                 for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-                    float vy[16], vs[16], sbv[16], sb2v[16];
-                    load16(args.sb + tb * kBN + c0, nvalid - c0, sbv);
-                    load16(args.sb2 + tb * kBN + c0, nvalid - c0, sb2v);
+                    float vy[16], vs[16];
                     tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
                     if (!row_ok) continue;
+                    const float* s1 = sc1 + (c0 - cbeg);
+                    const float* s2 = sc2 + (c0 - cbeg);
                     if (!real_tile) {
                         // permutation columns: F and the column maximum only
 #pragma unroll
                         for (int j = 0; j < 16; ++j) {
-                            const float swy = vy[j] * sa1 * sbv[j];
-                            const float sws = vs[j] * sa2 * sb2v[j];
+                            const float swy = vy[j] * sa1 * s1[j];
+                            const float sws = vs[j] * sa2 * s2[j];
                             const float qv = swy * swy * rcp_approx(fmaxf(sws, 1e-30f));
                             float F = qv * df * rcp_approx(fmaxf(rwr - qv, 1e-30f));
                             F = (sws > 0.0f) ? F : 0.0f;  // no variance left: the reference's clamp gives F = 0
@@ -288,10 +311,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                     const float inv_rwr = 1.0f / rwr;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int m = tb * kBN + c0 + j;
                         if (c0 + j >= nvalid) continue;
-                        const float swy = vy[j] * sa1 * sbv[j];
-                        const float sws = vs[j] * sa2 * sb2v[j];
+                        const float swy = vy[j] * sa1 * s1[j];
+                        const float sws = vs[j] * sa2 * s2[j];
                         const float inv_d = rcp_approx(fmaxf(sws, 1e-30f));
                         const float qv = swy * swy * inv_d;
                         const float rss = fmaxf(rwr - qv, 1e-30f);
@@ -300,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                         colmax = fmaxf(colmax, F);
                         col_nan |= (F != F);
                         if (!real) continue;
-                        const int64_t o = args.rows[m] * args.ldo + p;
+                        const int64_t o = rws[c0 - cbeg + j] * args.ldo + p;
                         if (var_ok) {
                             args.f[o] = F;
                             args.beta[o] = swy * inv_d;

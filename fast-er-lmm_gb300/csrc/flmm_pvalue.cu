@@ -16,6 +16,20 @@ __global__ void k_neglog10p_f64(const double* __restrict__ F, int64_t n, double 
         out[i] = neglog10_fsf<double>(F[i], df2, lbeta);
 }
 
+// 1-df chi-square quantile of each test's p-value, the input of the genomic inflation factor
+// (fasterlmm/inflation.py:19-29): chi2.isf(p, 1) = (Phi^-1(1 - p / 2))^2 = 2 erfcinv(p)^2, p = P(F(1, df2) > F).
+// NaN F gives NaN; p below the FP64 range gives +inf, as scipy's isf(0).
+__global__ void k_chisq1_f64(const double* __restrict__ F, int64_t n, double df2, double lbeta,
+                             double* __restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double v = neglog10_fsf<double>(F[i], df2, lbeta);
+        const double p = exp(-v * 2.302585092994046);  // 10^-v
+        const double z = erfcinv(p);
+        out[i] = isnan(v) ? NAN : 2.0 * z * z;
+    }
+}
+
 // Genome-wide threshold per phenotype (fasterlmm/cli.py:128): p = P(F(1, df2) > perm_max_F) for the row's n_perm
 // permutation maxima, then numpy.quantile(p, q) with linear interpolation between order statistics.  p is
 // decreasing in F, so the ascending p order is the descending F order: the row is sorted once (bitonic, shared
@@ -86,4 +100,15 @@ extern "C" int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double*
     const unsigned blocks = static_cast<unsigned>(n / 256 + 1 < 152 * 16 ? n / 256 + 1 : 152 * 16);
     k_neglog10p_f64<<<blocks, 256, 0, as_stream(stream)>>>(F, n, static_cast<double>(df2), lbeta, out);
     return check_launch("k_neglog10p_f64");
+}
+
+extern "C" int flmm_chisq1_from_f(const double* F, int64_t n, int df2, double* out, void* stream) {
+    FLMM_REQUIRE((F && out) || n == 0, "flmm_chisq1_from_f: NULL argument");
+    FLMM_REQUIRE(df2 >= 1, "flmm_chisq1_from_f: df2 must be >= 1 (got %d)", df2);
+    if (n == 0) return FLMM_OK;
+    const double a = 0.5 * df2;
+    const double lbeta = lgamma(a) + lgamma(0.5) - lgamma(a + 0.5);
+    const unsigned blocks = static_cast<unsigned>(n / 256 + 1 < 152 * 16 ? n / 256 + 1 : 152 * 16);
+    k_chisq1_f64<<<blocks, 256, 0, as_stream(stream)>>>(F, n, static_cast<double>(df2), lbeta, out);
+    return check_launch("k_chisq1_f64");
 }

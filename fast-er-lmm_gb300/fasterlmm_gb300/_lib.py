@@ -58,6 +58,9 @@ SIGNATURES: dict[str, list] = {
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_delta_features_f32": [_p, _i, _p, _i64, _i, _p, _p],
+    "flmm_delta_mlp_f32": [_p, _i, _p, _p, _p, _p, _p, C.c_float, _d, _d, _p, _p],
+    "flmm_newton_from_proposal": [_p, _i, _p, _i64, _i, _p, _i, _p, _p, _p, _p, _p],
     "flmm_fit_delta_lowrank_f64": [_p, _i, _p, _i64, _p, _i, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
     "flmm_wald_lowrank_f64_workspace_bytes": [_i, _i, _i, _i, _psz],
     "flmm_wald_lowrank_f64": [_p, _i, _p, _i64, _p, _i64, _i, _i, _p, _i, _i, _p, _i64, _p, _i64, _i, _p, _p, _p, _p,
@@ -72,6 +75,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_wald_gls_workspace_bytes": [_i, _i, _i, _psz],
     "flmm_wald_gls_f64": [_p, _i, _p, _i64, _i, _p, _i64, _p, _i, _i, _p, _i64, _i, _p, _p, _p, _p, _p, _i64, _p,
                           _p, _sz, _p],
+    "flmm_chisq1_from_f": [_p, _i64, _i, _p, _p],
     "flmm_perm_threshold_p": [_p, _i, _i, _i, _d, _p, _p],
     "flmm_context_check": [_p, _p],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],

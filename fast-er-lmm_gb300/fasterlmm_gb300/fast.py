@@ -36,6 +36,9 @@ F32 = torch.float32
 #   "f64": the FP64 batched call (EIGH_MODE: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on worker streams).
 EIGH_PRECISION = "f32r"
 EIGH_MODE = 1
+# Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
+# fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
+DELTA_PROPOSAL = "grid"
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -99,6 +102,13 @@ def fit_delta_fast(s: Tensor, UYt: Tensor, *, n_grid: int = 64, log_delta_min: f
     _lib.call("flmm_fit_delta_fast", _ptr(s), Neff, _ptr(UYt), UYt.stride(0), P, n_grid, float(log_delta_min),
               float(log_delta_max), int(bool(refine)), _ptr(ld), _ptr(idx), w, wb, _stream(dev))
     return ld, idx
+
+
+def _fit_delta(s: Tensor, UYt: Tensor, **kw) -> tuple[Tensor, Tensor]:
+    if DELTA_PROPOSAL == "learned":
+        from .learned import fit_delta_learned
+        return fit_delta_learned(s, UYt, **kw)
+    return fit_delta_fast(s, UYt, **kw)
 
 
 def _chrom_order(chrom: np.ndarray) -> tuple[np.ndarray | None, list]:
@@ -299,7 +309,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         Ut = Kp[k_idx, D:]
         Us = SplitRows.of(Ut)
         gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
-        ld, _ = fit_delta_fast(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
+        ld, _ = _fit_delta(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
                                log_delta_max=log_delta_max, refine=refine)
         USt = torch.empty((n, ldk), dtype=F32, device=dev)
         gemm_split(ctx, Zs.view(a, n), Us.view(), USt[:, :Neff])

@@ -3,7 +3,8 @@ Post-scan statistics of the CLI (fasterlmm/cli.py:128-132, :405-406) on the devi
 
 neg_log10_pvalue: -log10 P(F(1, df2) > F) from the regularized incomplete beta in log space (finite where scipy's
 f.sf underflows to 0).  perm_threshold_p: the genome-wide threshold, the linear-interpolated q-quantile of the
-per-permutation minimum p (monotone in the per-permutation max F).
+per-permutation minimum p (monotone in the per-permutation max F).  lambda_gc: the genomic inflation factor
+(fasterlmm/inflation.py).  rank_by_p: the p-ascending row order of the output tables.  effect_size: EffectSize.
 """
 from __future__ import annotations
 
@@ -34,6 +35,49 @@ def perm_threshold_p(perm_max_F: Tensor, df2: int, q: float = 0.05) -> Tensor:
     out = torch.empty(B, dtype=F64, device=dev)
     _lib.call("flmm_perm_threshold_p", _ptr(Fm), B, n_perm, int(df2), float(q), _ptr(out), _stream(dev))
     return out if not isinstance(perm_max_F, Tensor) or perm_max_F.is_cuda else out.to(perm_max_F.device)
+
+
+CHI2_1_MEDIAN = 0.45493642311957283  # scipy.stats.chi2.ppf(0.5, 1)
+
+
+def _nan_median_cols(x: Tensor) -> tuple[Tensor, Tensor]:
+    """numpy.median over the non-NaN entries of each column (mean of the two middle values for even counts)."""
+    valid = ~torch.isnan(x)
+    n = valid.sum(dim=0)
+    srt = torch.sort(torch.where(valid, x, torch.full_like(x, float("inf"))), dim=0).values
+    lo = ((n - 1).clamp(min=0) // 2).unsqueeze(0)
+    hi = (n // 2).clamp(max=x.shape[0] - 1).unsqueeze(0)
+    med = 0.5 * (srt.gather(0, lo) + srt.gather(0, hi)).squeeze(0)
+    return torch.where(n > 0, med, torch.full_like(med, float("nan"))), n
+
+
+def lambda_gc(F: Tensor, df2: int) -> tuple[Tensor, Tensor]:
+    """
+    Genomic inflation factor per phenotype column of F (M, B) (fasterlmm/inflation.py:19-29): median over variants
+    of chi2.isf(p, 1) for p = P(F(1, df2) > F), NaN p dropped, divided by chi2.ppf(0.5, 1).  Returns (lambda (B,),
+    number of variants used (B,)), on the device of F.
+    """
+    dev = _cuda_device(F)
+    Fd = _f64(F, dev)
+    chisq = torch.empty_like(Fd)
+    _lib.call("flmm_chisq1_from_f", _ptr(Fd), Fd.numel(), int(df2), _ptr(chisq), _stream(dev))
+    med, n = _nan_median_cols(chisq.reshape(Fd.shape[0], -1))
+    lam = med / CHI2_1_MEDIAN
+    if isinstance(F, Tensor) and not F.is_cuda:
+        return lam.to(F.device), n.to(F.device)
+    return lam, n
+
+
+def rank_by_p(F: Tensor, df2: int) -> Tensor:
+    """
+    Per phenotype column of F (M, B), the variant order of the CLI's output tables (fasterlmm/cli.py:145): p
+    ascending with ties (e.g. p underflowing to 0) in variant order, NaN last.  (M, B) int64 indices.
+    """
+    dev = _cuda_device(F)
+    p = torch.pow(10.0, -neg_log10_pvalue(_f64(F, dev), df2))
+    key = torch.where(torch.isnan(p), torch.full_like(p, float("inf")), p)
+    order = torch.sort(key, dim=0, stable=True).indices
+    return order if not isinstance(F, Tensor) or F.is_cuda else order.to(F.device)
 
 
 def effect_size(beta: Tensor, g_var: Tensor, p_var: Tensor) -> Tensor:

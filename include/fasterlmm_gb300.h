@@ -262,6 +262,24 @@ int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
 
+/* ---- learned delta proposal (no counterpart in the reference) ---------------------------------------------------
+ *
+ * Features of each rotated column, feats (P, 65): log energy fractions of UY^2 over 32 equal-count bins of the
+ * ascending spectrum s (Neff >= 32), log mean eigenvalue per bin, log(Neff) / 10.  The MLP 65 -> 128 -> 128 -> 1
+ * (tanh-GELU; W1 (128, 65), W2 (128, 128) row-major, w3 (128,)) maps them to a proposed log delta, clamped to
+ * [lo, hi].  flmm_newton_from_proposal then refines every column exactly: a proposal inside the FP32 grid argmin's
+ * basin [grid[i-1], grid[i+1]] (grid_idx from flmm_fit_delta_fast with refine = 0) splits it, the half holding the
+ * sign change of d loss / d log delta is confirmed and the fast fit's safeguarded Newton runs there from the
+ * proposal; other columns take the fast fit's grid refinement and are counted in *n_fallback (device int,
+ * add-only).  Results equal the grid path's to the Newton noise floor (~1e-7 in log delta). */
+int flmm_delta_features_f32(const double* s, int Neff, const float* UYt, int64_t ldu, int P, float* feats,
+                            void* stream);
+int flmm_delta_mlp_f32(const float* feats, int P, const float* W1, const float* b1, const float* W2, const float* b2,
+                       const float* w3, float b3, double lo, double hi, double* x_out, void* stream);
+int flmm_newton_from_proposal(const double* s, int Neff, const float* UYt, int64_t ldu, int P, const double* grid,
+                              int n_grid, const int32_t* grid_idx, const double* x_prop, double* log_delta,
+                              int32_t* n_fallback, void* stream);
+
 /* ---- low-rank path (fasterlmm/lowrank.py): kinship factor G (N, k), k < N --------------------------------------
  *
  * s (k,) kept eigenvalues, UYt (P, k) on-rank rotated columns, UUYt (P, N) off-rank residuals, USt / UUSt the same
@@ -316,6 +334,10 @@ int flmm_wald_gls_f64(const double* s, int N, const double* Xrt, int64_t ldx, in
                       const double* log_delta, int P, int n_real, const double* Srt, int64_t lds, int M,
                       const int64_t* rows, double* f, double* beta, double* se, double* sfve, int64_t ldo,
                       double* max_F, void* work, size_t work_bytes, void* stream);
+
+/* chi2.isf(P(F(1, df2) > F), 1) for every element (the genomic inflation factor's input,
+ * fasterlmm/inflation.py:19-29): 2 erfcinv(p)^2; NaN stays NaN, p below the FP64 range gives +inf. */
+int flmm_chisq1_from_f(const double* F, int64_t n, int df2, double* out, void* stream);
 
 /* Genome-wide permutation threshold per phenotype (fasterlmm/cli.py:128, :406): thresh[b] = numpy.quantile(p, q) with
  * linear interpolation, p = P(F(1, df2) > perm_max_F[b, :]) over the row's n_perm permutation maxima (B, n_perm). */

@@ -229,3 +229,30 @@ def test_grouped_driver_matches_golden(golden):
         assert gr.cols == g[f"g{gi}_cols"].tolist() and gr.df2 == len(gr.keep) - g["X"].shape[1] - 1
         assert_scan_close(_np(gr.res), g, prefix=f"g{gi}_")
         assert_scan_close({"perm_max_F": gr.perm_max_F.cpu().numpy()}, g, keys=("perm_max_F",), prefix=f"g{gi}_")
+
+
+def test_lambda_gc_and_rank_by_p_match_scipy(golden):
+    """Device post-scan: lambda GC (fasterlmm/inflation.py) and the p-ascending table order, on golden F."""
+    import scipy.stats as ss
+    from fasterlmm_gb300 import post
+    g = golden("loco_n150_m1500")
+    N, D = g["X"].shape
+    df2 = N - D - 1
+    F = g["f"].copy()
+    F[3, 2] = np.nan  # a dropped p-value
+    lam, n = post.lambda_gc(torch.from_numpy(F).cuda(), df2)
+    for b in range(F.shape[1]):
+        p = ss.f.sf(F[:, b], 1, df2)
+        p = p[~np.isnan(p)]
+        ref = np.median(ss.chi2.isf(p, 1)) / ss.chi2.ppf(0.5, 1)
+        assert int(n[b].item()) == p.size
+        np.testing.assert_allclose(lam[b].item(), ref, rtol=1e-9)
+    order = post.rank_by_p(torch.from_numpy(F).cuda(), df2).cpu().numpy()
+    for b in range(F.shape[1]):
+        p = ss.f.sf(F[:, b], 1, df2)
+        assert np.array_equal(np.sort(order[:, b]), np.arange(F.shape[0]))  # a permutation
+        pv = p[order[:, b]]
+        k = int((~np.isnan(pv)).sum())
+        assert np.isnan(pv[k:]).all() and np.all(np.diff(pv[:k]) >= -1e-15 * pv[1:k])  # p ascending, NaN last
+        ref = np.argsort(np.where(np.isnan(p), np.inf, p), kind="stable")
+        assert (order[:, b] == ref).mean() > 0.99  # the reference's order up to near-ties of the last bits
