@@ -119,27 +119,82 @@ k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_lo
     if (tid < TP && p0 + tid < P) idx_out[p0 + tid] = best_g;
 }
 
-__global__ void k_newton_refine(const double* __restrict__ s, int Neff, const float* __restrict__ UYt, int64_t ldu,
+// The spectrum as the evaluations read it, once per fit: s32 = fl32(s), dsb = sbar - s32, sbar = mean(s).
+__global__ void k_spectrum_prep(const double* __restrict__ s, int Neff, float* __restrict__ s32,
+                                float* __restrict__ dsb, float* __restrict__ sbar_out) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) acc += s[n];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) red[0] = v;
+    }
+    __syncthreads();
+    const float sbar = static_cast<float>(red[0] / Neff);
+    for (int n = threadIdx.x; n < Neff; n += blockDim.x) {
+        const float sn = static_cast<float>(s[n]);
+        s32[n] = sn;
+        dsb[n] = sbar - sn;
+    }
+    if (threadIdx.x == 0) *sbar_out = sbar;
+}
+
+// One warp per column; the spectrum arrays are shared by every warp of the grid through L1 / L2.
+__global__ void k_newton_refine(const float* __restrict__ s32, const float* __restrict__ dsb,
+                                const float* __restrict__ sbar_p, int Neff, const float* __restrict__ UYt, int64_t ldu,
                                 int P, const double* __restrict__ grid, int G, const int32_t* __restrict__ idx,
                                 int refine, double* __restrict__ log_delta) {
-    extern __shared__ float sm[];
-    float* s32 = sm;          // spectrum
-    float* dsb = sm + Neff;   // sbar - s
-    __shared__ float sbar_s;
-    const float sbar = load_spectrum(s, Neff, s32, dsb, &sbar_s);
     const int lane = threadIdx.x & 31;
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
     const float* u = UYt + p * ldu;
     float uh = 0.f, uc = 0.f;
     for (int n = lane; n < Neff; n += 32) neumaier(uh, uc, u[n] * u[n]);
-    const GlobalColumn ev{s32, dsb, u, Neff, sbar, warp_sum_pair(uh, uc)};
+    const GlobalColumn ev{s32, dsb, u, Neff, *sbar_p, warp_sum_pair(uh, uc)};
     const double out = refine_column(ev, grid, G, idx[p], refine);
     if (lane == 0) log_delta[p] = out;
 }
 
+// workspace: grid (G doubles) | Wg (G x Neff) | sum_log (G) | s32 (Neff) | dsb (Neff) | sbar
 size_t fast_ws(int Neff, int G) {
-    return sizeof(float) * (static_cast<size_t>(G) * Neff + static_cast<size_t>(G)) + sizeof(double) * G + 512;
+    return sizeof(float) * (static_cast<size_t>(G) * Neff + static_cast<size_t>(G) + 2 * static_cast<size_t>(Neff) + 4) +
+           sizeof(double) * G + 512;
+}
+
+struct FastWs {
+    double* grid;
+    float *Wg, *sum_log, *s32, *dsb, *sbar;
+};
+
+FastWs carve_fast(void* base, int Neff, int G) {
+    FastWs w;
+    w.grid = static_cast<double*>(base);
+    w.Wg = reinterpret_cast<float*>(w.grid + G);
+    w.sum_log = w.Wg + static_cast<size_t>(G) * Neff;
+    w.s32 = w.sum_log + G;
+    w.dsb = w.s32 + Neff;
+    w.sbar = w.dsb + Neff;
+    return w;
+}
+
+int launch_fast_fit(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid, double lo,
+                    double hi, int refine, double* log_delta, int32_t* grid_idx, void* scratch, cudaStream_t st) {
+    const FastWs w = carve_fast(scratch, Neff, n_grid);
+    int rc = flmm_delta_grid_nodes(lo, hi, n_grid, w.grid, st);
+    if (rc) return rc;
+    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, w.grid, w.Wg, w.sum_log);
+    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
+    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(w.Wg, w.sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
+    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
+    k_spectrum_prep<<<1, 256, 0, st>>>(s, Neff, w.s32, w.dsb, w.sbar);
+    if ((rc = check_launch("k_spectrum_prep"))) return rc;
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(
+        w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, n_grid, grid_idx, refine, log_delta);
+    return check_launch("k_newton_refine");
 }
 
 }  // namespace
@@ -155,25 +210,10 @@ extern "C" int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, 
                                    size_t work_bytes, void* stream) {
     FLMM_REQUIRE(s && UYt && log_delta && grid_idx && work && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
                  "flmm_fit_delta_fast: bad arguments");
-    FLMM_REQUIRE(Neff <= 12288, "flmm_fit_delta_fast: Neff must be <= 12288 (shared-memory spectrum)");
     if (work_bytes < fast_ws(Neff, n_grid))
         return fail(FLMM_ERR_WORKSPACE, "flmm_fit_delta_fast: need %zu bytes, got %zu", fast_ws(Neff, n_grid), work_bytes);
     if (P == 0) return FLMM_OK;
-    cudaStream_t st = as_stream(stream);
-    double* grid = static_cast<double*>(work);
-    float* Wg = reinterpret_cast<float*>(grid + n_grid);
-    float* sum_log = Wg + static_cast<size_t>(n_grid) * Neff;
-    int rc = flmm_delta_grid_nodes(lo, hi, n_grid, grid, stream);
-    if (rc) return rc;
-    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, grid, Wg, sum_log);
-    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
-    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
-    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
-    const size_t smem = 2 * sizeof(float) * static_cast<size_t>(Neff);
-    if (smem > 48 * 1024) FLMM_CUDA(cudaFuncSetAttribute(k_newton_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, st>>>(s, Neff, UYt, ldu, P, grid,
-                                                                                    n_grid, grid_idx, refine, log_delta);
-    return check_launch("k_newton_refine");
+    return launch_fast_fit(s, Neff, UYt, ldu, P, n_grid, lo, hi, refine, log_delta, grid_idx, work, as_stream(stream));
 }
 
 // ---- allocation-free variant ------------------------------------------------------------------------------------
@@ -223,7 +263,6 @@ extern "C" int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const floa
                                            void* stream) {
     FLMM_REQUIRE(s && UYt && log_delta && grid_idx && Neff > 0 && n_grid > 0 && ldu >= Neff && P >= 0,
                  "flmm_fit_delta_fast_noalloc: bad arguments");
-    FLMM_REQUIRE(Neff <= 12288, "flmm_fit_delta_fast_noalloc: Neff must be <= 12288 (shared-memory spectrum)");
     const size_t need = fast_ws(Neff, n_grid);
     if (need > kNoAllocScratchBytes)
         return fail(FLMM_ERR_WORKSPACE,
@@ -234,18 +273,6 @@ extern "C" int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const floa
     int rc = scratch_address(&scratch);
     if (rc) return rc;
     if (P == 0) return FLMM_OK;
-    cudaStream_t st = as_stream(stream);
-    double* grid = static_cast<double*>(scratch);
-    float* Wg = reinterpret_cast<float*>(grid + n_grid);
-    float* sum_log = Wg + static_cast<size_t>(n_grid) * Neff;
-    if ((rc = flmm_delta_grid_nodes(lo, hi, n_grid, grid, stream))) return rc;
-    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, grid, Wg, sum_log);
-    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
-    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(Wg, sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
-    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
-    const size_t smem = 2 * sizeof(float) * static_cast<size_t>(Neff);  // spectrum and sbar - spectrum
-    if (smem > 48 * 1024) FLMM_CUDA(cudaFuncSetAttribute(k_newton_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, st>>>(s, Neff, UYt, ldu, P, grid,
-                                                                                    n_grid, grid_idx, refine, log_delta);
-    return check_launch("k_newton_refine");
+    return launch_fast_fit(s, Neff, UYt, ldu, P, n_grid, lo, hi, refine, log_delta, grid_idx, scratch,
+                           as_stream(stream));
 }

@@ -58,6 +58,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_fill_nullh2": [_p, _i, _p, _i, _p, _i64, _p],
     "flmm_fill_f64": [_p, _i64, _d, _p],
     "flmm_neglog10_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_bed_decode": [_p, _i64, _i, _i, _p, _i, _i, _p, _i64, _p],
     "flmm_delta_features_f32": [_p, _i, _p, _i64, _i, _p, _p],
     "flmm_delta_mlp_f32": [_p, _i, _p, _p, _p, _p, _p, C.c_float, _d, _d, _p, _p],
     "flmm_newton_from_proposal": [_p, _i, _p, _i64, _i, _p, _i, _p, _p, _p, _p, _p],

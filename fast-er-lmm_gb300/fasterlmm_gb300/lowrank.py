@@ -227,7 +227,7 @@ def _loco_scan_core(chroms: list, block_source, M: int, G: Tensor, g_chrom: np.n
     N, D = Xd.shape
     P = Yt.shape[0]
     n_real = P if n_real is None else min(n_real, P)
-    out, max_F = _alloc_outputs(M, n_real, P, dev)
+    out, max_F = _alloc_outputs(M, n_real, P, dev, zero=True)  # a block reader need not cover every variant
     g_chrom = np.asarray(g_chrom)
     log_deltas = {}
     for k_idx, c in enumerate(chroms):

@@ -262,6 +262,15 @@ int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
 
+/* ---- PLINK .bed input (fasterlmm/io.py:54-67, fasterlmm/io_stream.py:60-71) ------------------------------------
+ *
+ * Decode n_variants SNP-major .bed records (each bytes_per_variant = ceil(n_fam / 4) bytes, header stripped) into
+ * int8 dosages G (n_variants, ldg): kept sample i is .fam row rows[i] (rows NULL: the first n_keep rows); A1 allele
+ * counts with count_a1 != 0 (the reference's default), else A2 counts; missing calls and rows outside [0, n_fam)
+ * give -1.  flmm_standardise_dosage then produces the standardised variant-major block. */
+int flmm_bed_decode(const uint8_t* bed, int64_t bytes_per_variant, int n_variants, int n_fam, const int32_t* rows,
+                    int n_keep, int count_a1, int8_t* G, int64_t ldg, void* stream);
+
 /* ---- learned delta proposal (no counterpart in the reference) ---------------------------------------------------
  *
  * Features of each rotated column, feats (P, 65): log energy fractions of UY^2 over 32 equal-count bins of the

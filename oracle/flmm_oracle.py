@@ -585,6 +585,55 @@ def single_k_scan_lowrank(G: np.ndarray, Z: np.ndarray, X: np.ndarray, Y: np.nda
 
 
 # --------------------------------------------------------------------------------------------------------------
+# PLINK 1 .bed (SNP-major) -- the published file format the reference reads through pysnptools (fasterlmm/io.py:54-67)
+# --------------------------------------------------------------------------------------------------------------
+
+def write_bed(prefix: str, G: np.ndarray, *, chrom=None, sid=None, pos=None, iid=None, count_A1: bool = True) -> None:
+    """
+    Write dosages G (N, M) (NaN or negative = missing) as .bed/.bim/.fam.  With count_A1 a dosage counts the first
+    allele: 2 -> 00, 1 -> 10, 0 -> 11; missing -> 01; four samples per byte from the low bits up.
+    """
+    N, M = G.shape
+    chrom = np.ones(M, dtype=int) if chrom is None else np.asarray(chrom)
+    sid = [f"v{j}" for j in range(M)] if sid is None else sid
+    pos = np.arange(1, M + 1) if pos is None else np.asarray(pos)
+    iid = [f"s{i}" for i in range(N)] if iid is None else iid
+    with open(f"{prefix}.fam", "w") as fh:
+        for s in iid:
+            fh.write(f"{s} {s} 0 0 0 -9\n")
+    with open(f"{prefix}.bim", "w") as fh:
+        for j in range(M):
+            fh.write(f"{chrom[j]}\t{sid[j]}\t0\t{int(pos[j])}\tA\tG\n")
+    Gf = np.asarray(G, dtype=np.float64)
+    miss = ~np.isfinite(Gf) | (Gf < 0)
+    a1 = np.where(miss, 0, Gf).astype(np.int64)
+    a2 = 2 - a1 if count_A1 else a1
+    code = np.select([a2 == 0, a2 == 1, a2 == 2], [0, 2, 3]).astype(np.uint8)
+    code[miss] = 1
+    bpv = (N + 3) // 4
+    pad = np.zeros((bpv * 4, M), dtype=np.uint8)
+    pad[:N] = code
+    q = pad.reshape(bpv, 4, M)
+    rec = (q[:, 0] | (q[:, 1] << 2) | (q[:, 2] << 4) | (q[:, 3] << 6)).T.astype(np.uint8)  # (M, bpv)
+    with open(f"{prefix}.bed", "wb") as fh:
+        fh.write(bytes([0x6C, 0x1B, 0x01]))
+        fh.write(np.ascontiguousarray(rec).tobytes())
+
+
+def read_bed(prefix: str, *, count_A1: bool = True) -> np.ndarray:
+    """(N, M) FP64 dosages, NaN for missing calls, from a SNP-major .bed (the format write_bed writes)."""
+    with open(f"{prefix}.fam") as fh:
+        N = sum(1 for line in fh if line.strip())
+    raw = np.fromfile(f"{prefix}.bed", dtype=np.uint8)
+    assert bytes(raw[:3]) == bytes([0x6C, 0x1B, 0x01])
+    bpv = (N + 3) // 4
+    rec = raw[3:].reshape(-1, bpv)
+    codes = np.stack([(rec >> (2 * k)) & 3 for k in range(4)], axis=2).reshape(rec.shape[0], -1)[:, :N].T
+    a2 = np.select([codes == 0, codes == 2, codes == 3], [0.0, 1.0, 2.0], np.nan)
+    return 2.0 - a2 if count_A1 else a2
+
+
+# --------------------------------------------------------------------------------------------------------------
 # permutations and the batch driver
 # --------------------------------------------------------------------------------------------------------------
 
