@@ -50,6 +50,17 @@ def _dist():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The slowest rank's value (the job's time), over the initialised process group when world > 1."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi sampler running during the timed region."""
 
@@ -234,12 +245,7 @@ def run_ours(args):
     wall = time.perf_counter() - w0
     launches = _lib.kernel_launches() - launches0
     clk = clocks.stop()
-    elapsed = ev0.elapsed_time(ev1) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([elapsed], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    elapsed = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
     value = world * tests_per_step * args.steps / elapsed
 
     # dominant kernel: the fused Wald scan, timed by events around its launches inside the timed steps
