@@ -18,6 +18,7 @@
 #include <cuda_fp16.h>
 #include <math.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -86,6 +87,77 @@ __device__ __forceinline__ float rcp_approx(float x) {
     float y;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// Wald statistics of one epilogue thread: accumulator row p (a column of the phenotype table) against tile columns
+// [cbeg, cbeg + 64) (variants), TMEM address tl of product 0 for this thread's lane quarter (product 1 lies kBN
+// columns further), the warp's staged scales sc1 / sc2 and output rows rws.
+__device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p, bool real_tile, int nvalid,
+                                          int cbeg, const float* sc1, const float* sc2, const int64_t* rws) {
+    // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each test needs
+    // two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
+    //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
+    const bool row_ok = p < args.Mr;
+    const float sa1 = row_ok ? args.sa[p] : 0.0f;
+    const float sa2 = row_ok ? args.sa2[p] : 0.0f;
+    const float rwr = row_ok ? args.rWr[p] : 1.0f;
+    const float df = args.var_df;
+    const bool real = row_ok && p < args.n_real;
+    float colmax = -INFINITY;
+    bool col_nan = false;
+    for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
+        float vy[16], vs[16];
+        tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
+        if (!row_ok) continue;
+        const float* s1 = sc1 + (c0 - cbeg);
+        const float* s2 = sc2 + (c0 - cbeg);
+        if (!real_tile) {
+            // permutation columns: F and the column maximum only
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float swy = vy[j] * sa1 * s1[j];
+                const float sws = vs[j] * sa2 * s2[j];
+                const float qv = swy * swy * rcp_approx(fmaxf(sws, 1e-30f));
+                float F = qv * df * rcp_approx(fmaxf(rwr - qv, 1e-30f));
+                F = (sws > 0.0f) ? F : 0.0f;  // no variance left: the reference's clamp gives F = 0
+                F = (c0 + j < nvalid) ? F : -INFINITY;
+                colmax = fmaxf(colmax, F);
+                col_nan |= (F != F);
+            }
+            continue;
+        }
+        const float inv_df = 1.0f / df;
+        const float inv_rwr = 1.0f / rwr;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (c0 + j >= nvalid) continue;
+            const float swy = vy[j] * sa1 * s1[j];
+            const float sws = vs[j] * sa2 * s2[j];
+            const float inv_d = rcp_approx(fmaxf(sws, 1e-30f));
+            const float qv = swy * swy * inv_d;
+            const float rss = fmaxf(rwr - qv, 1e-30f);
+            const bool var_ok = sws > 0.0f;
+            const float F = var_ok ? qv * df * rcp_approx(rss) : 0.0f;
+            colmax = fmaxf(colmax, F);
+            col_nan |= (F != F);
+            if (!real) continue;
+            const int64_t o = rws[c0 - cbeg + j] * args.ldo + p;
+            if (var_ok) {
+                args.f[o] = F;
+                args.beta[o] = swy * inv_d;
+                args.se[o] = sqrtf(rss * inv_d * inv_df);
+                args.sfve[o] = sqrtf(fmaxf(qv * inv_rwr, 0.0f));
+            } else {
+                // a variant with no variance left (e.g. monomorphic): the reference clamps sWs to 1e-300 in FP64,
+                // which gives beta = F = SFVE = 0 and SE = sqrt(rWr / df / 1e-300)
+                args.f[o] = 0.0;
+                args.beta[o] = 0.0;
+                args.se[o] = sqrt(fmax(static_cast<double>(args.rWr0[p]), 1e-300) / args.var_df / 1e-300);
+                args.sfve[o] = 0.0;
+            }
+        }
+    }
+    if (row_ok && (colmax >= 0.0f || col_nan)) atomic_max_nonneg(args.max_F + p, col_nan ? NAN : (double)colmax);
 }
 
 template <int NG, int BK>
@@ -275,70 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                     }
                 }
             } else {
-                // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each
-                // test needs two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
-                //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
-                const int p = i;
-                const float sa1 = row_ok ? args.sa[p] : 0.0f;
-                const float sa2 = row_ok ? args.sa2[p] : 0.0f;
-                const float rwr = row_ok ? args.rWr[p] : 1.0f;
-                const float df = args.var_df;
-                const bool real = row_ok && p < args.n_real;
-                float colmax = -INFINITY;
-                bool col_nan = false;
-                for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-                    float vy[16], vs[16];
-                    tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
-                    if (!row_ok) continue;
-                    const float* s1 = sc1 + (c0 - cbeg);
-                    const float* s2 = sc2 + (c0 - cbeg);
-                    if (!real_tile) {
-                        // permutation columns: F and the column maximum only
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const float swy = vy[j] * sa1 * s1[j];
-                            const float sws = vs[j] * sa2 * s2[j];
-                            const float qv = swy * swy * rcp_approx(fmaxf(sws, 1e-30f));
-                            float F = qv * df * rcp_approx(fmaxf(rwr - qv, 1e-30f));
-                            F = (sws > 0.0f) ? F : 0.0f;  // no variance left: the reference's clamp gives F = 0
-                            F = (c0 + j < nvalid) ? F : -INFINITY;
-                            colmax = fmaxf(colmax, F);
-                            col_nan |= (F != F);
-                        }
-                        continue;
-                    }
-                    const float inv_df = 1.0f / df;
-                    const float inv_rwr = 1.0f / rwr;
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        if (c0 + j >= nvalid) continue;
-                        const float swy = vy[j] * sa1 * s1[j];
-                        const float sws = vs[j] * sa2 * s2[j];
-                        const float inv_d = rcp_approx(fmaxf(sws, 1e-30f));
-                        const float qv = swy * swy * inv_d;
-                        const float rss = fmaxf(rwr - qv, 1e-30f);
-                        const bool var_ok = sws > 0.0f;
-                        const float F = var_ok ? qv * df * rcp_approx(rss) : 0.0f;
-                        colmax = fmaxf(colmax, F);
-                        col_nan |= (F != F);
-                        if (!real) continue;
-                        const int64_t o = rws[c0 - cbeg + j] * args.ldo + p;
-                        if (var_ok) {
-                            args.f[o] = F;
-                            args.beta[o] = swy * inv_d;
-                            args.se[o] = sqrtf(rss * inv_d * inv_df);
-                            args.sfve[o] = sqrtf(fmaxf(qv * inv_rwr, 0.0f));
-                        } else {
-                            // a variant with no variance left (e.g. monomorphic): the reference clamps sWs to 1e-300
-                            // in FP64, which gives beta = F = SFVE = 0 and SE = sqrt(rWr / df / 1e-300)
-                            args.f[o] = 0.0;
-                            args.beta[o] = 0.0;
-                            args.se[o] = sqrt(fmax(static_cast<double>(args.rWr0[p]), 1e-300) / args.var_df / 1e-300);
-                            args.sfve[o] = 0.0;
-                        }
-                    }
-                }
-                if (row_ok && (colmax >= 0.0f || col_nan)) atomic_max_nonneg(args.max_F + p, col_nan ? NAN : (double)colmax);
+                wald_rows(args, tl, i, real_tile, nvalid, cbeg, sc1, sc2, rws);
             }
             fence_before_sync();
             mbar_arrive(&acc_empty[ab]);
@@ -351,6 +360,214 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     if (warp == 1) {
         fence_after_sync();
         tmem_dealloc(tmem_base, C::kTmemCols);
+    }
+}
+
+// ---- the Wald scan on CTA pairs --------------------------------------------------------------------------------
+// Each tile is 256 A rows (phenotype columns) x 128 B rows (variants), run by a cluster of two CTAs with
+// tcgen05.mma.cta_group::2 (M = 256, N = 128): CTA r of the pair loads A rows 128 r .. +127 and B rows 64 r .. +63
+// of the tile into its own shared memory, the even CTA issues the MMAs, and each CTA's tensor memory receives its
+// 128 A rows against all 128 B rows, so the epilogue is the single-CTA one.  Per SM, one MMA step reads 128 + 64
+// operand rows from shared memory instead of 128 + 128, and a pipeline stage is 48 KB instead of 64 KB: shared
+// memory bandwidth is what bounds the single-CTA form.
+//
+// Synchronisation: both CTAs' TMA loads of a stage complete on the even CTA's full[stage] (its producer expects the
+// pair's bytes); the MMA issuer's commits arrive on empty[stage], acc_full[] and the final barrier of both CTAs
+// (multicast); the epilogue warps of both CTAs arrive on the even CTA's acc_empty[] (16 warps).  Every wait is
+// bounded as in the single-CTA kernel.
+struct PairCfg {
+    static constexpr int kBK = 64;
+    static constexpr int kATileBytes = 128 * kBK * 2;                      // 16 KB: 128 A rows of one half
+    static constexpr int kBTileBytes = 64 * kBK * 2;                       // 8 KB: 64 B rows of one half
+    static constexpr int kStageBytes = 2 * kATileBytes + 2 * kBTileBytes;  // A hi, A lo, B hi, B lo
+    static constexpr int kStages = 4;
+    static constexpr uint32_t kSwizzle = 2u;   // 128-byte
+    static constexpr uint32_t kSBO = 1024u;    // bytes between 8-row groups
+    static constexpr int kTmemCols = 2 * 2 * kBN;  // two products, double-buffered
+    static constexpr int kBarBytes = 256;
+    static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
+    static constexpr int kEpiBytes = 8 * kEpiWarpBytes;
+    static constexpr int kSmemBytes = kStages * kStageBytes + kBarBytes + kEpiBytes + 1024;
+    static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
+};
+
+constexpr int kPairRows = 256;  // A rows per pair tile
+
+__global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant__ TcMaps maps, const TcArgs args) {
+    using C = PairCfg;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kStageBytes);
+    uint64_t* full = bars;                        // [kStages], used in the even CTA
+    uint64_t* empty = bars + C::kStages;          // [kStages]
+    uint64_t* acc_full = bars + 2 * C::kStages;   // [2]
+    uint64_t* acc_empty = acc_full + 2;           // [2], used in the even CTA
+    uint64_t* final_bar = acc_empty + 2;          // [1]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(final_bar + 1);
+    uint8_t* epi_smem = smem + C::kStages * C::kStageBytes + C::kBarBytes;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_ctarank();
+    const bool leader = rank == 0;
+    const int cl = static_cast<int>(cluster_id_x()), n_cl = static_cast<int>(cluster_count_x());
+    const int tiles_b = (args.Nr + kBN - 1) / kBN;
+    const int n_tiles = ((args.Mr + kPairRows - 1) / kPairRows) * tiles_b;
+    const int n_kb0 = (args.K + C::kBK - 1) / C::kBK;
+    const int n_kb = n_kb0 + (args.K2 + C::kBK - 1) / C::kBK;
+    constexpr uint32_t idesc = idesc_f16_f32(kPairRows, kBN);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 2 * (kEpilogueThreads / 32));
+        }
+        mbar_init(final_bar, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0 && lane == 0) {
+        for (int i = 0; i < 8; ++i) tma_prefetch_desc(&maps.m[i]);
+    }
+    if (warp == 1) {
+        tmem_alloc_pair(tmem_slot, C::kTmemCols);
+        tmem_relinquish_pair();
+    }
+    fence_before_sync();
+    __syncwarp();
+    cluster_sync();  // barriers initialised and tensor memory allocated in both CTAs
+    fence_after_sync();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ---- TMA producer (both CTAs): this CTA's halves of the tile, counted on the even CTA's full[] ----
+        if (lane == 0) {
+            const uint32_t full0 = map_to_rank(smem_u32(full), 0);
+            int stage = 0;
+            uint32_t phase = 0;
+            bool armed[C::kStages] = {};
+            uint32_t armed_phase[C::kStages] = {};
+            bool ok = true;
+            for (int t = cl; t < n_tiles && ok; t += n_cl) {
+                const int ta = t / tiles_b, tb = t % tiles_b;
+                const int arow = ta * kPairRows + static_cast<int>(rank) * 128;
+                const int brow = tb * kBN + static_cast<int>(rank) * (kBN / 2);
+                for (int kb = 0; kb < n_kb; ++kb) {
+                    if (!mbar_wait(&empty[stage], phase ^ 1u, args.err, 1)) { ok = false; break; }
+                    if (leader) {
+                        mbar_arrive_expect_tx(&full[stage], 2 * C::kStageBytes);
+                        armed[stage] = true;
+                        armed_phase[stage] = phase;
+                    }
+                    uint8_t* base = smem + stage * C::kStageBytes;
+                    const uint32_t bar = full0 + static_cast<uint32_t>(stage * 8);
+                    const int g = kb < n_kb0 ? 0 : 1;
+                    const int kx = (kb - g * n_kb0) * C::kBK;
+                    tma_load_2d_pair(base, &maps.m[g * 4 + 0], kx, arow, bar);
+                    tma_load_2d_pair(base + C::kATileBytes, &maps.m[g * 4 + 1], kx, arow, bar);
+                    tma_load_2d_pair(base + 2 * C::kATileBytes, &maps.m[g * 4 + 2], kx, brow, bar);
+                    tma_load_2d_pair(base + 2 * C::kATileBytes + C::kBTileBytes, &maps.m[g * 4 + 3], kx, brow, bar);
+                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                }
+            }
+            if (leader) {
+                // the pair's copies of every armed phase have landed before the CTAs leave
+                for (int s = 0; s < C::kStages; ++s)
+                    if (armed[s]) mbar_drain(&full[s], armed_phase[s]);
+            } else if (*reinterpret_cast<volatile int*>(args.err) != 0) {
+                // the even CTA may have stopped waiting on this CTA's last copies: give them time to land
+                for (int i = 0; i < 100; ++i) __nanosleep(1000);
+            }
+        }
+    } else if (warp == 1) {
+        if (leader && lane == 0) {
+            // ---- MMA issuer (even CTA) ----
+            int stage = 0;
+            uint32_t phase = 0;
+            int ab = 0;
+            uint32_t aphase = 0;
+            bool ok = true;
+            for (int t = cl; t < n_tiles && ok; t += n_cl) {
+                if (!mbar_wait_cluster(&acc_empty[ab], aphase ^ 1u, args.err, 2)) break;
+                fence_after_sync();
+                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * 2 * kBN);
+                for (int kb = 0; kb < n_kb; ++kb) {
+                    if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                    fence_after_sync();
+                    const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
+                    const int g = kb < n_kb0 ? 0 : 1;
+                    const int kb_g = kb - g * n_kb0;
+                    const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
+#pragma unroll
+                    for (int kk = 0; kk < C::kBK / 16; ++kk) {
+                        const uint64_t ah = smem_desc(sbase, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t al = smem_desc(sbase + C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t bh = smem_desc(sbase + 2 * C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        const uint64_t bl =
+                            smem_desc(sbase + 2 * C::kATileBytes + C::kBTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                        mma_f16_pair(d, ah, bh, idesc, (kb_g | kk) ? 1u : 0u);
+                        mma_f16_pair(d, ah, bl, idesc, 1u);
+                        mma_f16_pair(d, al, bh, idesc, 1u);
+                    }
+                    mma_commit_pair(&empty[stage], 3);
+                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                }
+                if (!ok) break;
+                mma_commit_pair(&acc_full[ab], 3);
+                if (++ab == 2) { ab = 0; aphase ^= 1u; }
+            }
+            mma_commit_pair(final_bar, 3);
+            mbar_drain(final_bar, 0);
+        } else if (lane == 0) {
+            // odd CTA: its shared and tensor memory stay live until the even CTA's last MMA has completed
+            mbar_drain(final_bar, 0);
+        }
+    } else {
+        // ---- epilogue (both CTAs): as in k_tc, rows of this CTA's half of the pair tile ----
+        const int q = warp & 3;
+        const int cbeg = ((warp - 2) >> 2) * (kBN / 2);
+        const int r = q * 32 + lane;
+        float* sc1 = reinterpret_cast<float*>(epi_smem + (warp - 2) * C::kEpiWarpBytes);
+        float* sc2 = sc1 + 64;
+        int64_t* rws = reinterpret_cast<int64_t*>(sc2 + 64);
+        const uint32_t acc_empty0 = map_to_rank(smem_u32(acc_empty), 0);
+        int ab = 0;
+        uint32_t aphase = 0;
+        for (int t = cl; t < n_tiles; t += n_cl) {
+            const int ta = t / tiles_b, tb = t % tiles_b;
+            const int nvalid = min(kBN, args.Nr - tb * kBN);
+            const int row0 = ta * kPairRows + static_cast<int>(rank) * 128;
+            const bool real_tile = row0 < args.n_real;  // uniform over the CTA
+            __syncwarp();
+            for (int k = lane; k < kBN / 2; k += 32) {
+                const int c = cbeg + k;
+                const int m = tb * kBN + c;
+                const bool okc = c < nvalid;
+                sc1[k] = okc ? args.sb[m] : 0.0f;
+                sc2[k] = okc ? args.sb2[m] : 0.0f;
+                if (real_tile) rws[k] = okc ? args.rows[m] : 0;
+            }
+            __syncwarp();
+            const bool ok = mbar_wait(&acc_full[ab], aphase, args.err, 4);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            fence_after_sync();
+            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * 2 * kBN);
+            wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, sc1, sc2, rws);
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(acc_empty0 + static_cast<uint32_t>(ab * 8));
+            if (++ab == 2) { ab = 0; aphase ^= 1u; }
+        }
+    }
+
+    fence_before_sync();
+    __syncwarp();
+    cluster_sync();  // no CTA leaves while its peer may still signal its barriers or read its operands
+    if (warp == 1) {
+        fence_after_sync();
+        tmem_dealloc_pair(tmem_base, C::kTmemCols);
     }
 }
 
@@ -556,8 +773,8 @@ int encode_fn(PFN_cuTensorMapEncodeTiled_v12000* out) {
     return FLMM_OK;
 }
 
-// FP16 matrix (rows, K) with row pitch ld elements -> tiled map with box {BK, 128} and the matching swizzle.
-int make_map(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK) {
+// FP16 matrix (rows, K) with row pitch ld elements -> tiled map with box {BK, box_rows} and the matching swizzle.
+int make_map(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK, int box_rows = 128) {
     PFN_cuTensorMapEncodeTiled_v12000 enc;
     int rc = encode_fn(&enc);
     if (rc) return rc;
@@ -565,7 +782,7 @@ int make_map(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, in
         return fail(FLMM_ERR_ARG, "split operand must be 16-byte aligned with a row pitch that is a multiple of 8");
     cuuint64_t gdim[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
     cuuint64_t gstride[1] = {static_cast<cuuint64_t>(ld * 2)};
-    cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), 128u};
+    cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(box_rows)};
     cuuint32_t estride[2] = {1u, 1u};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), gdim, gstride, box, estride,
                      CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -584,6 +801,73 @@ int launch_tc(const TcMaps& maps, const TcArgs& args, int sm_count, cudaStream_t
     const int grid = tiles < sm_count ? tiles : sm_count;
     k_tc<NG, BK><<<grid, kThreads, C::kSmemBytes, st>>>(maps, args);
     return check_launch(NG == 1 ? "k_tc<gemm>" : "k_tc<wald>");
+}
+
+// Clusters of the pair kernel that fit on the device at once (0 if it cannot be launched as pairs), per device.
+int pair_clusters(int device) {
+    static std::mutex mu;
+    static int cache[64];
+    static bool done[64];
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 64) return 0;
+    if (!done[device]) {
+        done[device] = true;
+        cache[device] = 0;
+        if (cudaFuncSetAttribute(k_wald_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, PairCfg::kSmemBytes) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        int sm = 0;
+        cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(static_cast<unsigned>(sm & ~1), 1, 1);
+        cfg.blockDim = dim3(kThreads, 1, 1);
+        cfg.dynamicSmemBytes = PairCfg::kSmemBytes;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_wald_pair, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        cache[device] = n;
+    }
+    return cache[device];
+}
+
+int launch_wald_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max, cudaStream_t st) {
+    const int tiles = ((args.Mr + kPairRows - 1) / kPairRows) * ((args.Nr + kBN - 1) / kBN);
+    if (tiles == 0 || args.K <= 0) return FLMM_OK;
+    const int n_cl = tiles < n_clusters_max ? tiles : n_clusters_max;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(2 * n_cl), 1, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = PairCfg::kSmemBytes;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FLMM_CUDA(cudaLaunchKernelEx(&cfg, k_wald_pair, maps, args));
+    return check_launch("k_wald_pair");
+}
+
+// Wald kernel form: CTA pairs unless FLMM_WALD_PAIR=0 asks for the single-CTA kernel (kept for cross-checks)
+bool use_pair_kernel() {
+    static const bool on = [] {
+        const char* e = std::getenv("FLMM_WALD_PAIR");
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
 }  // namespace
@@ -723,5 +1007,18 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sfve = sfve;
     a.ldo = ldo;
     a.max_F = max_F;
+    if (use_pair_kernel()) {
+        int dev = 0;
+        FLMM_CUDA(cudaGetDevice(&dev));
+        const int n_cl = pair_clusters(dev);
+        if (n_cl > 0) {
+            // the pair kernel loads 64 B rows per CTA: variant-side maps with half-height boxes
+            if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
+            if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
+            if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, kBK, kBN / 2))) return rc;
+            if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, kBK, kBN / 2))) return rc;
+            return launch_wald_pair(maps, a, n_cl, as_stream(stream));
+        }
+    }
     return launch_tc<2, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }

@@ -1,4 +1,4 @@
-// -log10 p of the F(1, df2) tail in FP64 over an array of F statistics (the CLI's post-scan step,
+// The F(1, df2) tail in FP64 over an array of F statistics, as p or -log10 p (the CLI's post-scan step,
 // fasterlmm/cli.py:405-406); the maths is in flmm_pvalue.cuh.
 #include <math.h>
 
@@ -16,6 +16,13 @@ __global__ void k_neglog10p_f64(const double* __restrict__ F, int64_t n, double 
         out[i] = neglog10_fsf<double>(F[i], df2, lbeta);
 }
 
+__global__ void k_fsf_f64(const double* __restrict__ F, int64_t n, double df2, double lbeta,
+                          double* __restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = fsf<double>(F[i], df2, lbeta);
+}
+
 // 1-df chi-square quantile of each test's p-value, the input of the genomic inflation factor
 // (fasterlmm/inflation.py:19-29): chi2.isf(p, 1) = (Phi^-1(1 - p / 2))^2 = 2 erfcinv(p)^2, p = P(F(1, df2) > F).
 // NaN F gives NaN; p below the FP64 range gives +inf, as scipy's isf(0).
@@ -23,10 +30,9 @@ __global__ void k_chisq1_f64(const double* __restrict__ F, int64_t n, double df2
                              double* __restrict__ out) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const double v = neglog10_fsf<double>(F[i], df2, lbeta);
-        const double p = exp(-v * 2.302585092994046);  // 10^-v
+        const double p = fsf<double>(F[i], df2, lbeta);
         const double z = erfcinv(p);
-        out[i] = isnan(v) ? NAN : 2.0 * z * z;
+        out[i] = isnan(p) ? NAN : 2.0 * z * z;
     }
 }
 
@@ -61,10 +67,10 @@ __global__ void k_perm_threshold(const double* __restrict__ pmax, int B, int n_p
         const double h = (n_perm - 1) * q;
         const int j = static_cast<int>(floor(h));
         const double frac = h - j;
-        const double p0 = exp(-neglog10_fsf<double>(-v[j], df2, lbeta) * 2.302585092994045684);
+        const double p0 = fsf<double>(-v[j], df2, lbeta);
         double out = p0;
         if (frac > 0.0 && j + 1 < n_perm) {
-            const double p1 = exp(-neglog10_fsf<double>(-v[j + 1], df2, lbeta) * 2.302585092994045684);
+            const double p1 = fsf<double>(-v[j + 1], df2, lbeta);
             out = p0 + frac * (p1 - p0);
         }
         thresh[b] = out;
@@ -111,4 +117,15 @@ extern "C" int flmm_chisq1_from_f(const double* F, int64_t n, int df2, double* o
     const unsigned blocks = static_cast<unsigned>(n / 256 + 1 < 152 * 16 ? n / 256 + 1 : 152 * 16);
     k_chisq1_f64<<<blocks, 256, 0, as_stream(stream)>>>(F, n, static_cast<double>(df2), lbeta, out);
     return check_launch("k_chisq1_f64");
+}
+
+extern "C" int flmm_f_pvalue(const double* F, int64_t n, int df2, double* out, void* stream) {
+    FLMM_REQUIRE((F && out) || n == 0, "flmm_f_pvalue: NULL argument");
+    FLMM_REQUIRE(df2 >= 1, "flmm_f_pvalue: df2 must be >= 1 (got %d)", df2);
+    if (n == 0) return FLMM_OK;
+    const double a = 0.5 * df2;
+    const double lbeta = lgamma(a) + lgamma(0.5) - lgamma(a + 0.5);
+    const unsigned blocks = static_cast<unsigned>(n / 256 + 1 < 152 * 16 ? n / 256 + 1 : 152 * 16);
+    k_fsf_f64<<<blocks, 256, 0, as_stream(stream)>>>(F, n, static_cast<double>(df2), lbeta, out);
+    return check_launch("k_fsf_f64");
 }

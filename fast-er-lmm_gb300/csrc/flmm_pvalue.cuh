@@ -53,28 +53,45 @@ FLMM_HD T betacf_lentz(T a, T b, T x, int max_iter) {
     return h;
 }
 
-// -log10 P(F(1, df2) > F); lbeta = log B(df2 / 2, 1 / 2).  F <= 0 gives 0 (p = 1); NaN propagates.
+// P(F(1, df2) > F) for F > 0 and finite, lbeta = log B(df2 / 2, 1 / 2), returned as one of two terms: true with v =
+// log p (the fraction for I_x(a, b) itself, x < (a + 1) / (a + b + 2)), or false with v = I_{1-x}(b, a) = 1 - p.
 template <typename T>
-FLMM_HD T neglog10_fsf(T F, T df2, T lbeta) {
-    if (!(F > T(0))) return (F == F) ? T(0) : F;
-    if (isinf(F)) return T(INFINITY);
+FLMM_HD bool fsf_terms(T F, T df2, T lbeta, T& v) {
     const T a = df2 * T(0.5), b = T(0.5);
-    const T ln10 = T(2.302585092994045684);
     // log x = -log1p(F / n), log(1 - x) = log(F / (n + F))
     const T logx = -log1p(F / df2);
     const T y = F / (df2 + F);  // 1 - x without cancellation
     const T log1mx = log(y);
     const T lpre = a * logx + b * log1mx - lbeta;
     const T x = df2 / (df2 + F);
-    T logp;
     if (x < (a + T(1)) / (a + b + T(2))) {
         const T h = betacf_lentz<T>(a, b, x, 4000);
-        logp = lpre + log(h) - log(a);
-    } else {
-        const T h = betacf_lentz<T>(b, a, y, 4000);
-        logp = log1p(-exp(lpre) * h / b);
+        v = lpre + log(h) - log(a);
+        return true;
     }
+    const T h = betacf_lentz<T>(b, a, y, 4000);
+    v = exp(lpre) * h / b;
+    return false;
+}
+
+// -log10 P(F(1, df2) > F); lbeta = log B(df2 / 2, 1 / 2).  F <= 0 gives 0 (p = 1); NaN propagates.
+template <typename T>
+FLMM_HD T neglog10_fsf(T F, T df2, T lbeta) {
+    if (!(F > T(0))) return (F == F) ? T(0) : F;
+    if (isinf(F)) return T(INFINITY);
+    const T ln10 = T(2.302585092994045684);
+    T v;
+    const T logp = fsf_terms<T>(F, df2, lbeta, v) ? v : log1p(-v);
     return -logp / ln10;
+}
+
+// P(F(1, df2) > F) itself (scipy.stats.f.sf(F, 1, df2)): F <= 0 gives 1, +inf gives 0, NaN propagates.
+template <typename T>
+FLMM_HD T fsf(T F, T df2, T lbeta) {
+    if (!(F > T(0))) return (F == F) ? T(1) : F;
+    if (isinf(F)) return T(0);
+    T v;
+    return fsf_terms<T>(F, df2, lbeta, v) ? exp(v) : T(1) - v;
 }
 
 }  // namespace flmm

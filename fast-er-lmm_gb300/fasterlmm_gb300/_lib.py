@@ -14,7 +14,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libfasterlmm_gb300.so"
 
-_i, _i64, _d, _p, _sz = C.c_int, C.c_int64, C.c_double, C.c_void_p, C.c_size_t
+_i, _i64, _d, _p, _sz, _s = C.c_int, C.c_int64, C.c_double, C.c_void_p, C.c_size_t, C.c_char_p
 _pi32 = C.POINTER(C.c_int32)
 _psz = C.POINTER(C.c_size_t)
 
@@ -78,6 +78,10 @@ SIGNATURES: dict[str, list] = {
                           _p, _sz, _p],
     "flmm_chisq1_from_f": [_p, _i64, _i, _p, _p],
     "flmm_perm_threshold_p": [_p, _i, _i, _i, _d, _p, _p],
+    "flmm_f_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_format_f64": [_p, _i64, _p, _i64, _p],
+    "flmm_write_gwas_tsv": [_s, _i64, _p, _p, _p, _p, _p, _d, _p, _p, _p, _p, _p, _i64, _p, _i64, _s, _i64],
+    "flmm_write_column_tsv": [_s, _s, _p, _i64],
     "flmm_context_check": [_p, _p],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],

@@ -1,8 +1,8 @@
 """
 Post-scan statistics of the CLI (fasterlmm/cli.py:128-132, :405-406) on the device.
 
-neg_log10_pvalue: -log10 P(F(1, df2) > F) from the regularized incomplete beta in log space (finite where scipy's
-f.sf underflows to 0).  perm_threshold_p: the genome-wide threshold, the linear-interpolated q-quantile of the
+pvalue: P(F(1, df2) > F), scipy's f.sf.  neg_log10_pvalue: -log10 of it from the regularized incomplete beta in log
+space (finite where f.sf underflows to 0).  perm_threshold_p: the genome-wide threshold, the linear-interpolated q-quantile of the
 per-permutation minimum p (monotone in the per-permutation max F).  lambda_gc: the genomic inflation factor
 (fasterlmm/inflation.py).  rank_by_p: the p-ascending row order of the output tables.  effect_size: EffectSize.
 """
@@ -21,6 +21,16 @@ def neg_log10_pvalue(F: Tensor, df2: int) -> Tensor:
     Fd = _f64(F, dev)
     out = torch.empty_like(Fd)
     _lib.call("flmm_neglog10_pvalue", _ptr(Fd), Fd.numel(), int(df2), _ptr(out), _stream(dev))
+    return out if not isinstance(F, Tensor) or F.is_cuda else out.to(F.device)
+
+
+def pvalue(F: Tensor, df2: int) -> Tensor:
+    """P(F(1, df2) > F) for every element of F (scipy.stats.f.sf(F, 1, df2), fasterlmm/cli.py:405), FP64, on the
+    device of F (host tensors round-trip)."""
+    dev = _cuda_device(F)
+    Fd = _f64(F, dev)
+    out = torch.empty_like(Fd)
+    _lib.call("flmm_f_pvalue", _ptr(Fd), Fd.numel(), int(df2), _ptr(out), _stream(dev))
     return out if not isinstance(F, Tensor) or F.is_cuda else out.to(F.device)
 
 
@@ -74,7 +84,7 @@ def rank_by_p(F: Tensor, df2: int) -> Tensor:
     ascending with ties (e.g. p underflowing to 0) in variant order, NaN last.  (M, B) int64 indices.
     """
     dev = _cuda_device(F)
-    p = torch.pow(10.0, -neg_log10_pvalue(_f64(F, dev), df2))
+    p = pvalue(_f64(F, dev), df2)
     key = torch.where(torch.isnan(p), torch.full_like(p, float("inf")), p)
     order = torch.sort(key, dim=0, stable=True).indices
     return order if not isinstance(F, Tensor) or F.is_cuda else order.to(F.device)

@@ -36,6 +36,7 @@ extern "C" {
 #define FLMM_ERR_WORKSPACE 4    /* work_bytes smaller than the *_workspace_bytes query */
 #define FLMM_ERR_DEVICE 5       /* the device is not an sm_103 (GB300) part */
 #define FLMM_ERR_TIMEOUT 6      /* a bounded device-side wait gave up; the kernel returned without its result */
+#define FLMM_ERR_IO 7           /* an output file could not be opened or written */
 
 typedef struct flmm_context flmm_context;
 
@@ -352,6 +353,33 @@ int flmm_chisq1_from_f(const double* F, int64_t n, int df2, double* out, void* s
  * linear interpolation, p = P(F(1, df2) > perm_max_F[b, :]) over the row's n_perm permutation maxima (B, n_perm). */
 int flmm_perm_threshold_p(const double* perm_max_F, int B, int n_perm, int df2, double q, double* thresh,
                           void* stream);
+
+/* P(F(1, df2) > F) for every element, the CLI's PValue column (fasterlmm/cli.py:405, scipy.stats.f.sf(F, 1, df2)):
+ * F <= 0 gives 1, +inf gives 0, NaN stays NaN. */
+int flmm_f_pvalue(const double* F, int64_t n, int df2, double* out, void* stream);
+
+/* ---- output files (host code; fasterlmm/cli.py:100-161) ---------------------------------------------------------
+ * Numbers are written as the reference's pyarrow CSV writer writes them: shortest round-trip digits, fixed notation
+ * for decimal exponents -6 .. 9, d.ddde+X otherwise, nan / inf / -inf.  Each call writes one file and holds no
+ * lock, so phenotypes can be written from parallel threads.  Errors: FLMM_ERR_ARG, FLMM_ERR_IO. */
+
+/* The text of v[0..n) back to back in buf (buf_bytes; 40 bytes per value always suffice), value i at
+ * [offsets[i], offsets[i + 1]) (offsets holds n + 1 entries). */
+int flmm_format_f64(const double* v, int64_t n, char* buf, int64_t buf_bytes, int64_t* offsets);
+
+/* One phenotype's gwas.tsv (fasterlmm/cli.py:150-153): header plus M rows sid_index, SNP, Chr, GenDist (null),
+ * ChrPos, PValue, SnpWeight, SnpWeightSE, EffectSize = beta^2 g_var / p_var, SnpFractVarExpl, Mixing (0), Nullh2,
+ * Pheno, PhenoCount, in the row order order[i * ld_order] (variant indices; NULL = variant order).  Per-variant
+ * columns chrom, pos, g_var have stride 1; result columns pvalue .. nullh2 have stride ld (e.g. B for an (M, B)
+ * variant-major table).  SNP ids are snp_ids[snp_offsets[v] .. snp_offsets[v + 1]). */
+int flmm_write_gwas_tsv(const char* path, int64_t M, const char* snp_ids, const int64_t* snp_offsets,
+                        const double* chrom, const double* pos, const double* g_var, double p_var,
+                        const double* pvalue, const double* beta, const double* se, const double* sfve,
+                        const double* nullh2, int64_t ld, const int64_t* order, int64_t ld_order,
+                        const char* pheno_name, int64_t pheno_count);
+
+/* A one-column table (e.g. perms.tsv, fasterlmm/cli.py:154): the header line, then one value per line. */
+int flmm_write_column_tsv(const char* path, const char* header, const double* v, int64_t n);
 
 #ifdef __cplusplus
 }
