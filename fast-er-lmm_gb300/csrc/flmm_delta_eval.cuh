@@ -9,10 +9,12 @@
 namespace flmm {
 namespace dfit {
 
+// FP32 throughout: the sums behind g are FP32, and the FP64 pipe of this part runs at a small fraction of the FP32
+// rate, so only the abscissa x = log delta itself is kept in FP64.
 struct NewtonEval {
-    double g;      // T1 - Neff S2 / S1 (sign of d loss / d log delta)
-    double gp;     // dg / dx
-    double loss;   // Neff log S1 + sum log (s + delta), up to constants
+    float g;      // T1 - Neff S2 / S1 (sign of d loss / d log delta)
+    float gp;     // dg / dx
+    float loss;   // Neff log S1 + sum log (s + delta), up to constants
 };
 
 // One evaluation by a warp at x = log delta (x is warp-uniform), all in FP32.
@@ -70,18 +72,31 @@ __device__ inline NewtonEval finish_eval(const EvalSums& t, float U, int Neff, c
         const float a = E1 / (c * U), b = E2 / (c * c * U), t3 = E3 / (c * c * c * U);
         const float br = -2.0f * D1 / (c * neff) - F2 / (c * c * neff) + (2.0f * a + 4.0f * b + 2.0f * t3) / (1.0f + a) -
                          (a + b) * (a + b) / ((1.0f + a) * (1.0f + a));
-        e.gp = static_cast<double>(pt.delta) * neff * c * c * br;
+        e.gp = pt.delta * neff * c * c * br;
     } else {  // all-zero rotated column: the loss only grows with delta
-        e.g = 1.0;
-        e.gp = 1.0;
+        e.g = 1.0f;
+        e.gp = 1.0f;
     }
-    e.loss = 0.0;
+    e.loss = 0.0f;
     if (want_loss) e.loss = neff * logf(fmaxf(c * U + E1, 1e-30f)) + warp_sum(t.sl);
     return e;
 }
 
-// Evaluator over a column read from global (L1 / L2) memory on every evaluation; dsb[n] = sbar - s[n] and the
-// column's sum of squares U are precomputed.  (Keeping the squares in registers instead cost occupancy and ran
+// One evaluation over a column read from global (L1 / L2) memory; dsb[n] = sbar - s[n] and the column's sum of
+// squares U are precomputed.  Not inlined: the refinement calls the evaluator from a dozen places, and one shared
+// copy of the loop keeps the instruction cache warm (inlined copies made instruction fetch the main stall).
+static __device__ __noinline__ NewtonEval eval_global_column(const float* __restrict__ s32,
+                                                             const float* __restrict__ dsb,
+                                                             const float* __restrict__ u, int Neff, float sbar,
+                                                             float U, double x, bool want_loss) {
+    const int lane = threadIdx.x & 31;
+    const EvalPoint pt = eval_point(x, sbar);
+    EvalSums t;
+    for (int n = lane; n < Neff; n += 32) t.add(s32[n], dsb[n], u[n] * u[n], pt, want_loss);
+    return finish_eval(t, U, Neff, pt, want_loss);
+}
+
+// Evaluator over a column in global memory.  (Keeping the squares in registers instead cost occupancy and ran
 // slower.)
 struct GlobalColumn {
     const float* s32;
@@ -91,11 +106,7 @@ struct GlobalColumn {
     float sbar, U;
 
     __device__ NewtonEval operator()(double x, bool want_loss) const {
-        const int lane = threadIdx.x & 31;
-        const EvalPoint pt = eval_point(x, sbar);
-        EvalSums t;
-        for (int n = lane; n < Neff; n += 32) t.add(s32[n], dsb[n], u[n] * u[n], pt, want_loss);
-        return finish_eval(t, U, Neff, pt, want_loss);
+        return eval_global_column(s32, dsb, u, Neff, sbar, U, x, want_loss);
     }
 };
 
@@ -108,9 +119,9 @@ __device__ double newton_in_bracket(const Ev& ev, double lo, double hi, double x
     double x = inside ? x0 : 0.5 * (lo + hi);
     for (int it = 0; it < 60; ++it) {
         const NewtonEval e = (it == 0 && inside && first) ? *first : ev(x, false);
-        if (e.g == 0.0) break;
-        if (e.g < 0.0) lo = x; else hi = x;
-        double xn = x - e.g / e.gp;
+        if (e.g == 0.0f) break;
+        if (e.g < 0.0f) lo = x; else hi = x;
+        double xn = x - static_cast<double>(e.g / e.gp);
         if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
         const double stepx = fabs(xn - x);
         x = xn;
@@ -119,40 +130,42 @@ __device__ double newton_in_bracket(const Ev& ev, double lo, double hi, double x
     return x;
 }
 
-// log delta of one column from its grid argmin i (warp-uniform result)
+// log delta of one column from its grid argmin i (warp-uniform result).  `first`, if given, is the evaluation at
+// grid[i].
 template <class Ev>
-__device__ double refine_column(const Ev& ev, const double* __restrict__ grid, int G, int i, int refine) {
+__device__ double refine_column(const Ev& ev, const double* __restrict__ grid, int G, int i, int refine,
+                                const NewtonEval* first = nullptr) {
     double out = grid[i];
     if (refine && i > 0 && i < G - 1) {
         // the usual case: d loss / d log delta changes sign between the argmin's neighbours
         const double a = grid[i - 1], b = grid[i + 1];
-        if (ev(a, false).g < 0.0 && ev(b, false).g > 0.0) return newton_in_bracket(ev, a, b, grid[i]);
+        if (ev(a, false).g < 0.0f && ev(b, false).g > 0.0f) return newton_in_bracket(ev, a, b, grid[i], first);
     }
     if (refine && G > 1) {
         // The FP32 grid argmin is only as good as the FP32 loss (~1e-4 absolute); on flat losses it can sit several
         // nodes from the minimum.  The exact derivative sign at that node says which side the minimum is on, and a
         // binary search over the grid nodes on that side finds where d loss / d log delta changes sign, so the
         // bracket [grid[i-1], grid[i+1]] always contains the minimum (for losses with one minimum on that side).
-        const double gi = ev(grid[i], false).g;
-        if (gi < 0.0) {
-            if (ev(grid[G - 1], false).g < 0.0) {
+        const float gi = first ? first->g : ev(grid[i], false).g;
+        if (gi < 0.0f) {
+            if (ev(grid[G - 1], false).g < 0.0f) {
                 i = G - 1;  // still falling at the top of the grid
             } else {
                 int lo = i, hi = G - 1;  // g(lo) < 0 <= g(hi)
                 while (hi - lo > 1) {
                     const int mid = (lo + hi) >> 1;
-                    if (ev(grid[mid], false).g < 0.0) lo = mid; else hi = mid;
+                    if (ev(grid[mid], false).g < 0.0f) lo = mid; else hi = mid;
                 }
                 i = hi;
             }
-        } else if (gi > 0.0) {
-            if (ev(grid[0], false).g > 0.0) {
+        } else if (gi > 0.0f) {
+            if (ev(grid[0], false).g > 0.0f) {
                 i = 0;  // already rising at the bottom of the grid
             } else {
                 int lo = 0, hi = i;  // g(lo) <= 0 < g(hi)
                 while (hi - lo > 1) {
                     const int mid = (lo + hi) >> 1;
-                    if (ev(grid[mid], false).g > 0.0) hi = mid; else lo = mid;
+                    if (ev(grid[mid], false).g > 0.0f) hi = mid; else lo = mid;
                 }
                 i = lo;
             }
@@ -160,12 +173,12 @@ __device__ double refine_column(const Ev& ev, const double* __restrict__ grid, i
         const double a = grid[max(i - 1, 0)], b = grid[min(i + 1, G - 1)];
         const NewtonEval ea = ev(a, false);
         const NewtonEval eb = ev(b, false);
-        if (ea.g >= 0.0 && eb.g <= 0.0) {
+        if (ea.g >= 0.0f && eb.g <= 0.0f) {
             // loss rises from a and falls towards b: the minimum is an edge
             out = (ev(a, true).loss <= ev(b, true).loss) ? a : b;
-        } else if (ea.g >= 0.0) {
+        } else if (ea.g >= 0.0f) {
             out = a;
-        } else if (eb.g <= 0.0) {
+        } else if (eb.g <= 0.0f) {
             out = b;
         } else {
             out = newton_in_bracket(ev, a, b, grid[i]);

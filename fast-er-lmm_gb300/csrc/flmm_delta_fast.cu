@@ -152,10 +152,22 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
     const float* u = UYt + p * ldu;
+    const float sbar = *sbar_p;
+    const int i = idx[p];
+    // one pass gives the column's sum of squares and the evaluation at the grid argmin
+    const EvalPoint pt = eval_point(grid[i], sbar);
+    EvalSums t;
     float uh = 0.f, uc = 0.f;
-    for (int n = lane; n < Neff; n += 32) neumaier(uh, uc, u[n] * u[n]);
-    const GlobalColumn ev{s32, dsb, u, Neff, *sbar_p, warp_sum_pair(uh, uc)};
-    const double out = refine_column(ev, grid, G, idx[p], refine);
+    for (int n = lane; n < Neff; n += 32) {
+        const float un = u[n];
+        const float uu = un * un;
+        neumaier(uh, uc, uu);
+        t.add(s32[n], dsb[n], uu, pt, false);
+    }
+    const float U = warp_sum_pair(uh, uc);
+    const NewtonEval e0 = finish_eval(t, U, Neff, pt, false);
+    const GlobalColumn ev{s32, dsb, u, Neff, sbar, U};
+    const double out = refine_column(ev, grid, G, i, refine, &e0);
     if (lane == 0) log_delta[p] = out;
 }
 

@@ -118,14 +118,14 @@ __global__ void k_newton_from_proposal(const double* __restrict__ s, int Neff, c
     if (i > 0 && i < G - 1 && x0 > a && x0 < b) {
         // the proposal splits the grid argmin's basin: the half towards -g must end with the opposite sign
         const NewtonEval e0 = ev(x0, false);
-        if (e0.g == 0.0) {
+        if (e0.g == 0.0f) {
             out = x0;
             done = true;
         } else {
-            const double xe = e0.g < 0.0 ? b : a;
+            const double xe = e0.g < 0.0f ? b : a;
             const NewtonEval ee = ev(xe, false);
-            if ((e0.g < 0.0 && ee.g > 0.0) || (e0.g > 0.0 && ee.g < 0.0)) {
-                const double blo = e0.g < 0.0 ? x0 : xe, bhi = e0.g < 0.0 ? xe : x0;
+            if ((e0.g < 0.0f && ee.g > 0.0f) || (e0.g > 0.0f && ee.g < 0.0f)) {
+                const double blo = e0.g < 0.0f ? x0 : xe, bhi = e0.g < 0.0f ? xe : x0;
                 out = newton_in_bracket(ev, blo, bhi, x0, &e0);
                 done = true;
             }

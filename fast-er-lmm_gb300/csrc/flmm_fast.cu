@@ -160,6 +160,47 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p
     if (row_ok && (colmax >= 0.0f || col_nan)) atomic_max_nonneg(args.max_F + p, col_nan ? NAN : (double)colmax);
 }
 
+// C = sa sb^T (acc) for one epilogue thread: accumulator row i against tile columns [cbeg, cbeg + 64) starting at
+// column col0 of C, TMEM address tl for this thread's lane quarter, staged column scales sc1.
+__device__ __forceinline__ void gemm_rows(const TcArgs& args, uint32_t tl, int i, int col0, int nvalid, int cbeg,
+                                          const float* sc1) {
+    const bool row_ok = i < args.Mr;
+    const float sa = row_ok ? args.sa[i] : 0.0f;
+    float* crow = args.C + static_cast<int64_t>(i) * args.ldc + col0;
+    for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
+        float v[16];
+        tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
+        if (!row_ok) continue;
+        const float* sc = sc1 + (c0 - cbeg);
+        float* dst = crow + c0;
+        if (c0 + 16 <= nvalid && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+            // a thread owns 16 consecutive outputs of its row: four 16-byte stores
+            float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+                float4 x = make_float4(v[4 * q4] * sa * sc[4 * q4], v[4 * q4 + 1] * sa * sc[4 * q4 + 1],
+                                       v[4 * q4 + 2] * sa * sc[4 * q4 + 2], v[4 * q4 + 3] * sa * sc[4 * q4 + 3]);
+                if (args.accumulate) {
+                    const float4 o = d4[q4];
+                    x.x += o.x;
+                    x.y += o.y;
+                    x.z += o.z;
+                    x.w += o.w;
+                }
+                d4[q4] = x;
+            }
+            continue;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (c0 + j < nvalid) {
+                const float x = v[j] * sa * sc[j];
+                dst[j] = args.accumulate ? dst[j] + x : x;
+            }
+        }
+    }
+}
+
 template <int NG, int BK>
 __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMaps maps, const TcArgs args) {
     using C = Cfg<NG, BK>;
@@ -309,43 +350,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             fence_after_sync();
             const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
             const int i = ta * kBM + r;  // A row
-            const bool row_ok = i < args.Mr;
             if constexpr (NG == 1) {
-                const float sa = row_ok ? args.sa[i] : 0.0f;
-                float* crow = args.C + static_cast<int64_t>(i) * args.ldc + tb * kBN;
-                for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-                    float v[16];
-                    tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
-                    if (!row_ok) continue;
-                    const float* sc = sc1 + (c0 - cbeg);
-                    float* dst = crow + c0;
-                    if (c0 + 16 <= nvalid && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
-                        // a thread owns 16 consecutive outputs of its row: four 16-byte stores
-                        float4* d4 = reinterpret_cast<float4*>(dst);
-#pragma unroll
-                        for (int q4 = 0; q4 < 4; ++q4) {
-                            float4 x = make_float4(v[4 * q4] * sa * sc[4 * q4], v[4 * q4 + 1] * sa * sc[4 * q4 + 1],
-                                                   v[4 * q4 + 2] * sa * sc[4 * q4 + 2],
-                                                   v[4 * q4 + 3] * sa * sc[4 * q4 + 3]);
-                            if (args.accumulate) {
-                                const float4 o = d4[q4];
-                                x.x += o.x;
-                                x.y += o.y;
-                                x.z += o.z;
-                                x.w += o.w;
-                            }
-                            d4[q4] = x;
-                        }
-                        continue;
-                    }
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        if (c0 + j < nvalid) {
-                            const float x = v[j] * sa * sc[j];
-                            dst[j] = args.accumulate ? dst[j] + x : x;
-                        }
-                    }
-                }
+                gemm_rows(args, tl, i, tb * kBN, nvalid, cbeg, sc1);
             } else {
                 wald_rows(args, tl, i, real_tile, nvalid, cbeg, sc1, sc2, rws);
             }
@@ -363,8 +369,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     }
 }
 
-// ---- the Wald scan on CTA pairs --------------------------------------------------------------------------------
-// Each tile is 256 A rows (phenotype columns) x 128 B rows (variants), run by a cluster of two CTAs with
+// ---- the tcgen05 kernels on CTA pairs -----------------------------------------------------------------------------
+// k_pair<NG> is k_tc<NG, 64> run on CTA pairs (NG = 2: the Wald scan, NG = 1: the split GEMM).
+// Each tile is 256 A rows (e.g. phenotype columns) x 128 B rows (e.g. variants), run by a cluster of two CTAs with
 // tcgen05.mma.cta_group::2 (M = 256, N = 128): CTA r of the pair loads A rows 128 r .. +127 and B rows 64 r .. +63
 // of the tile into its own shared memory, the even CTA issues the MMAs, and each CTA's tensor memory receives its
 // 128 A rows against all 128 B rows, so the epilogue is the single-CTA one.  Per SM, one MMA step reads 128 + 64
@@ -375,6 +382,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
 // pair's bytes); the MMA issuer's commits arrive on empty[stage], acc_full[] and the final barrier of both CTAs
 // (multicast); the epilogue warps of both CTAs arrive on the even CTA's acc_empty[] (16 warps).  Every wait is
 // bounded as in the single-CTA kernel.
+template <int NG>
 struct PairCfg {
     static constexpr int kBK = 64;
     static constexpr int kATileBytes = 128 * kBK * 2;                      // 16 KB: 128 A rows of one half
@@ -383,7 +391,7 @@ struct PairCfg {
     static constexpr int kStages = 4;
     static constexpr uint32_t kSwizzle = 2u;   // 128-byte
     static constexpr uint32_t kSBO = 1024u;    // bytes between 8-row groups
-    static constexpr int kTmemCols = 2 * 2 * kBN;  // two products, double-buffered
+    static constexpr int kTmemCols = NG * 2 * kBN;  // NG products, double-buffered
     static constexpr int kBarBytes = 256;
     static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
     static constexpr int kEpiBytes = 8 * kEpiWarpBytes;
@@ -393,8 +401,10 @@ struct PairCfg {
 
 constexpr int kPairRows = 256;  // A rows per pair tile
 
-__global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant__ TcMaps maps, const TcArgs args) {
-    using C = PairCfg;
+
+template <int NG>
+__global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ TcMaps maps, const TcArgs args) {
+    using C = PairCfg<NG>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kStageBytes);
@@ -413,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
     const int n_tiles = ((args.Mr + kPairRows - 1) / kPairRows) * tiles_b;
     const int n_kb0 = (args.K + C::kBK - 1) / C::kBK;
-    const int n_kb = n_kb0 + (args.K2 + C::kBK - 1) / C::kBK;
+    const int n_kb = n_kb0 + (NG == 2 ? (args.K2 + C::kBK - 1) / C::kBK : 0);
     constexpr uint32_t idesc = idesc_f16_f32(kPairRows, kBN);
 
     if (threadIdx.x == 0) {
@@ -429,7 +439,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant
         fence_barrier_init();
     }
     if (warp == 0 && lane == 0) {
-        for (int i = 0; i < 8; ++i) tma_prefetch_desc(&maps.m[i]);
+        for (int i = 0; i < NG * 4; ++i) tma_prefetch_desc(&maps.m[i]);
     }
     if (warp == 1) {
         tmem_alloc_pair(tmem_slot, C::kTmemCols);
@@ -492,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant
             for (int t = cl; t < n_tiles && ok; t += n_cl) {
                 if (!mbar_wait_cluster(&acc_empty[ab], aphase ^ 1u, args.err, 2)) break;
                 fence_after_sync();
-                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * 2 * kBN);
+                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * NG * kBN);
                 for (int kb = 0; kb < n_kb; ++kb) {
                     if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
                     fence_after_sync();
@@ -539,22 +549,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_wald_pair(const __grid_constant
             const int ta = t / tiles_b, tb = t % tiles_b;
             const int nvalid = min(kBN, args.Nr - tb * kBN);
             const int row0 = ta * kPairRows + static_cast<int>(rank) * 128;
-            const bool real_tile = row0 < args.n_real;  // uniform over the CTA
+            const bool real_tile = NG == 2 && row0 < args.n_real;  // uniform over the CTA
             __syncwarp();
             for (int k = lane; k < kBN / 2; k += 32) {
                 const int c = cbeg + k;
                 const int m = tb * kBN + c;
                 const bool okc = c < nvalid;
                 sc1[k] = okc ? args.sb[m] : 0.0f;
-                sc2[k] = okc ? args.sb2[m] : 0.0f;
-                if (real_tile) rws[k] = okc ? args.rows[m] : 0;
+                if constexpr (NG == 2) {
+                    sc2[k] = okc ? args.sb2[m] : 0.0f;
+                    if (real_tile) rws[k] = okc ? args.rows[m] : 0;
+                }
             }
             __syncwarp();
             const bool ok = mbar_wait(&acc_full[ab], aphase, args.err, 4);
             if (!__all_sync(0xffffffffu, ok)) break;
             fence_after_sync();
-            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * 2 * kBN);
-            wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, sc1, sc2, rws);
+            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
+            if constexpr (NG == 1)
+                gemm_rows(args, tl, row0 + r, tb * kBN, nvalid, cbeg, sc1);
+            else
+                wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, sc1, sc2, rws);
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive_cluster(acc_empty0 + static_cast<uint32_t>(ab * 8));
@@ -803,7 +818,8 @@ int launch_tc(const TcMaps& maps, const TcArgs& args, int sm_count, cudaStream_t
     return check_launch(NG == 1 ? "k_tc<gemm>" : "k_tc<wald>");
 }
 
-// Clusters of the pair kernel that fit on the device at once (0 if it cannot be launched as pairs), per device.
+// Clusters of the pair kernel k_pair<NG> that fit on the device at once (0 if it cannot run as pairs), per device.
+template <int NG>
 int pair_clusters(int device) {
     static std::mutex mu;
     static int cache[64];
@@ -813,7 +829,7 @@ int pair_clusters(int device) {
     if (!done[device]) {
         done[device] = true;
         cache[device] = 0;
-        if (cudaFuncSetAttribute(k_wald_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, PairCfg::kSmemBytes) !=
+        if (cudaFuncSetAttribute(k_pair<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, PairCfg<NG>::kSmemBytes) !=
             cudaSuccess) {
             cudaGetLastError();
             return 0;
@@ -828,11 +844,11 @@ int pair_clusters(int device) {
         attr[0].val.clusterDim.z = 1;
         cfg.gridDim = dim3(static_cast<unsigned>(sm & ~1), 1, 1);
         cfg.blockDim = dim3(kThreads, 1, 1);
-        cfg.dynamicSmemBytes = PairCfg::kSmemBytes;
+        cfg.dynamicSmemBytes = PairCfg<NG>::kSmemBytes;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, k_wald_pair, &cfg) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveClusters(&n, k_pair<NG>, &cfg) != cudaSuccess) {
             cudaGetLastError();
             n = 0;
         }
@@ -841,7 +857,8 @@ int pair_clusters(int device) {
     return cache[device];
 }
 
-int launch_wald_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max, cudaStream_t st) {
+template <int NG>
+int launch_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max, cudaStream_t st) {
     const int tiles = ((args.Mr + kPairRows - 1) / kPairRows) * ((args.Nr + kBN - 1) / kBN);
     if (tiles == 0 || args.K <= 0) return FLMM_OK;
     const int n_cl = tiles < n_clusters_max ? tiles : n_clusters_max;
@@ -853,18 +870,18 @@ int launch_wald_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max,
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(static_cast<unsigned>(2 * n_cl), 1, 1);
     cfg.blockDim = dim3(kThreads, 1, 1);
-    cfg.dynamicSmemBytes = PairCfg::kSmemBytes;
+    cfg.dynamicSmemBytes = PairCfg<NG>::kSmemBytes;
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    FLMM_CUDA(cudaLaunchKernelEx(&cfg, k_wald_pair, maps, args));
-    return check_launch("k_wald_pair");
+    FLMM_CUDA(cudaLaunchKernelEx(&cfg, k_pair<NG>, maps, args));
+    return check_launch(NG == 1 ? "k_pair<gemm>" : "k_pair<wald>");
 }
 
-// Wald kernel form: CTA pairs unless FLMM_WALD_PAIR=0 asks for the single-CTA kernel (kept for cross-checks)
+// tcgen05 kernel form: CTA pairs unless FLMM_TC_PAIR=0 asks for the single-CTA kernels (kept for cross-checks)
 bool use_pair_kernel() {
     static const bool on = [] {
-        const char* e = std::getenv("FLMM_WALD_PAIR");
+        const char* e = std::getenv("FLMM_TC_PAIR");
         return !(e && e[0] == '0');
     }();
     return on;
@@ -917,6 +934,16 @@ extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void
     a.C = Cout;
     a.ldc = ldc;
     a.accumulate = accumulate;
+    if (use_pair_kernel()) {
+        int dev = 0;
+        FLMM_CUDA(cudaGetDevice(&dev));
+        const int n_cl = pair_clusters<1>(dev);
+        if (n_cl > 0) {
+            if ((rc = make_map(&maps.m[2], Bh, Nr, K, ldb, kBK, kBN / 2))) return rc;
+            if ((rc = make_map(&maps.m[3], Bl, Nr, K, ldb, kBK, kBN / 2))) return rc;
+            return launch_pair<1>(maps, a, n_cl, as_stream(stream));
+        }
+    }
     return launch_tc<1, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
 }
 
@@ -1010,14 +1037,14 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     if (use_pair_kernel()) {
         int dev = 0;
         FLMM_CUDA(cudaGetDevice(&dev));
-        const int n_cl = pair_clusters(dev);
+        const int n_cl = pair_clusters<2>(dev);
         if (n_cl > 0) {
             // the pair kernel loads 64 B rows per CTA: variant-side maps with half-height boxes
             if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
             if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
             if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, kBK, kBN / 2))) return rc;
             if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, kBK, kBN / 2))) return rc;
-            return launch_wald_pair(maps, a, n_cl, as_stream(stream));
+            return launch_pair<2>(maps, a, n_cl, as_stream(stream));
         }
     }
     return launch_tc<2, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));

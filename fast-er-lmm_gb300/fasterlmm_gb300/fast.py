@@ -239,7 +239,8 @@ def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: T
               _ptr(out["sfve"]), n_real, _ptr(max_F), st)
     if done:
         done(slot)
-    _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, st)
+    if "nullh2" in out:  # (the streamed path fills nullh2 rows in host memory instead)
+        _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, st)
 
 
 def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int, on_chrom=None,
@@ -274,10 +275,14 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
             slot[1] = ev
 
     out, max_F = _alloc_outputs(M, n_real, P, dev)
-    sink = _RowSink(out, host_out, dev) if host_out is not None else None
     basis = CovariateBasis(X)
     Ys = SplitRows.of(basis.regress_out(Yt))
     order, blocks = _chrom_order(chrom)
+    host_nullh2 = host_out is not None and loco and _RowSink.host_fill_possible(host_out, order, blocks)
+    if host_nullh2:
+        del out["nullh2"]  # filled in host memory, chromosome by chromosome
+        nullh2_row = torch.zeros(1, dtype=torch.int64, device=dev)
+    sink = _RowSink(out, host_out, dev, host_nullh2) if host_out is not None else None
     order_t = None if order is None else torch.from_numpy(order).to(dev)
     Zs = SplitRows.of(Zt if order_t is None else Zt.index_select(0, order_t))
     row_map = torch.arange(M, dtype=torch.int64, device=dev) if order_t is None else order_t.to(torch.int64)
@@ -318,6 +323,10 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         log_deltas[c if c is not None else 0] = ld
         if sink is not None:
             sink.push(order, a, n)
+            if host_nullh2 and n:
+                vec = torch.empty(n_real, dtype=F64, device=dev)
+                _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(nullh2_row), 1, _ptr(vec), n_real, st)
+                sink.push_nullh2(vec, order, a, n)
         if on_chrom is not None:
             on_chrom(k_idx + 1, len(units))
     _lib.call("flmm_context_check", ctx, st)
@@ -366,14 +375,58 @@ class _RowSink:
     Copies finished result rows into caller tensors on a side stream.  A chromosome whose rows are contiguous in
     the caller's variant order is copied as soon as its scan is queued; other rows (unsorted chromosome labels)
     and max_F are copied at the end.
+
+    nullh2 repeats one value per (chromosome, phenotype) over the chromosome's rows.  When every chromosome's rows
+    are contiguous and the caller's nullh2 lives in host memory, only each chromosome's (n_real,) vector crosses the
+    link and host threads fill its rows (flmm_fill_rows_host_f64) while the GPU runs on: a fifth of the result bytes
+    never leave the device.
     """
 
     KEYS = ("f", "beta", "se", "sfve", "nullh2")
+    FILL_THREADS = 8
 
-    def __init__(self, out: dict, host_out: dict, dev: torch.device):
+    def __init__(self, out: dict, host_out: dict, dev: torch.device, host_nullh2: bool = False):
         self.out, self.host, self.dev = out, host_out, dev
         self.stream = torch.cuda.Stream(device=dev)
         self.pending = []  # row ranges not copied early
+        self.host_nullh2 = host_nullh2
+        self.fills = []
+        self.pool = None
+        if host_nullh2:
+            from concurrent.futures import ThreadPoolExecutor
+            self.pool = ThreadPoolExecutor(max_workers=2)
+
+    @staticmethod
+    def host_fill_possible(host_out: dict | None, order, blocks) -> bool:
+        h = (host_out or {}).get("nullh2")
+        if h is None or h.is_cuda or not h.is_contiguous() or h.dtype != F64:
+            return False
+        return order is None or all(np.array_equal(order[a:a + n], np.arange(order[a], order[a] + n))
+                                    for _, a, n in blocks if n)
+
+    def push_nullh2(self, vec: Tensor, order, a: int, n: int) -> None:
+        """Copy one chromosome's nullh2 vector (n_real,) to the host and fill its n rows there."""
+        if n == 0:
+            return
+        r0 = a if order is None else int(order[a])
+        vh = torch.empty(vec.shape, dtype=vec.dtype, pin_memory=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.dev))
+        self.stream.wait_event(ev)
+        done = torch.cuda.Event()
+        with torch.cuda.stream(self.stream):
+            vh.copy_(vec, non_blocking=True)
+            done.record(self.stream)
+        dst = self.host["nullh2"]
+        ld = dst.stride(0)
+
+        def fill():
+            done.synchronize()
+            _lib.call("flmm_fill_rows_host_f64", dst.data_ptr() + 8 * r0 * ld, ld, n, vh.data_ptr(), vh.numel(),
+                      self.FILL_THREADS)
+
+        # vec and vh stay referenced until finish(): the side stream may copy vec after this call returns
+        self.fills.append((self.pool.submit(fill), vh, vec))
 
     def push(self, order, a: int, n: int) -> None:
         if n == 0:
@@ -387,19 +440,25 @@ class _RowSink:
         self.stream.wait_event(ev)
         with torch.cuda.stream(self.stream):
             for k in self.KEYS:
-                if k in self.host:
+                if k in self.host and k in self.out:
                     self.host[k][r0:r0 + n].copy_(self.out[k][r0:r0 + n], non_blocking=True)
 
     def finish(self, max_F: Tensor, log_deltas: dict) -> ScanResult:
         main = torch.cuda.current_stream(self.dev)
         if self.pending:  # at least one chromosome was not contiguous: copy everything once more at the end
             for k in self.KEYS:
-                if k in self.host:
+                if k in self.host and k in self.out:
                     self.host[k].copy_(self.out[k], non_blocking=True)
         if "max_F" in self.host:
             self.host["max_F"].copy_(max_F, non_blocking=True)
         main.synchronize()
         self.stream.synchronize()
+        for f, _, _ in self.fills:
+            f.result()
+        if self.pool is not None:
+            self.pool.shutdown(wait=True)
         pick = lambda k, t: self.host[k] if k in self.host else t
-        return ScanResult(max_F=pick("max_F", max_F), log_delta=log_deltas,
-                          **{k: pick(k, v) for k, v in self.out.items()})
+        res = {k: pick(k, v) for k, v in self.out.items()}
+        if self.host_nullh2:
+            res["nullh2"] = self.host["nullh2"]
+        return ScanResult(max_F=pick("max_F", max_F), log_delta=log_deltas, **res)

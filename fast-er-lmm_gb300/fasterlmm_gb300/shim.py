@@ -11,7 +11,8 @@ the copies ``fasterlmm.extreme`` imported by name (fasterlmm/extreme.py:19) are 
 the low-rank names of ``fasterlmm.lowrank`` and the copies ``fasterlmm.extreme_scan`` imported (fasterlmm/
 extreme_scan.py:21-22) to the low-rank kernels, so the streamed engine's block loop runs its math on the GPU.  The
 CLI and any user code that goes through those names then runs on the GPU unchanged.  ``uninstall()`` restores
-the originals.
+the originals.  The CLI's per-phenotype writer ``fasterlmm.cli._write_pheno`` is rebound to fasterlmm_gb300.output,
+whose files are byte-identical to the reference's.
 """
 from __future__ import annotations
 
@@ -36,10 +37,11 @@ def _set(mod, name, value):
     setattr(mod, name, value)
 
 
-def install(form: str = "fast", modules: dict | None = None) -> list[str]:
+def install(form: str = "fast", modules: dict | None = None, outputs: bool = True) -> list[str]:
     """
     Patch the reference's modules (imported from sys.modules, or given as ``modules`` = {"core": ..., "perms":
-    ..., "cli": ...}).  ``form`` picks the numeric form of the scan drivers.  Returns the patched qualified names.
+    ..., "cli": ...}).  ``form`` picks the numeric form of the scan drivers; ``outputs`` also routes the CLI's
+    per-phenotype writer through fasterlmm_gb300.output.  Returns the patched qualified names.
     """
     from . import core, gls, lowrank, perms
     mods = dict(modules or {})
@@ -74,6 +76,11 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
             if m is not None and hasattr(m, name):
                 _set(m, name, getattr(lowrank, name))
                 patched.append(f"{m.__name__}.{name}")
+    cli = mods.get("cli")
+    if outputs and cli is not None and hasattr(cli, "_write_pheno"):
+        key = (cli.__name__, "_write_pheno")
+        _set(cli, "_write_pheno", _cli_writer(_saved[key][1] if key in _saved else cli._write_pheno))
+        patched.append(f"{cli.__name__}._write_pheno")
     pt = functools.partial(perms.perm_threshold, form=form)
     for key in ("perms", "cli"):
         m = mods.get(key)
@@ -87,6 +94,34 @@ def install(form: str = "fast", modules: dict | None = None) -> list[str]:
             _set(m, "perm_threshold", pt)
             patched.append(f"{m.__name__}.perm_threshold")
     return patched
+
+
+def _cli_writer(original):
+    """
+    Stand-in for fasterlmm.cli._write_pheno (fasterlmm/cli.py:114-158) that writes through fasterlmm_gb300.output.
+    The CLI's writer context is turned into a VariantTable once per (ids, genotype variances) pair; calls with LD
+    clumping on (the optional LDGroup column) go to the original writer.
+    """
+    from .output import VariantTable, write_pheno
+    cache: dict = {}
+
+    def write(ctx, outdir_str, pheno_name, p_col, beta_col, se_col, sfve_col, nullh2_col, p_var, perm_min_p,
+              perm_quantile, per_pheno_dirs, bundle_writer):
+        if ctx.get("clump") is not None:
+            return original(ctx, outdir_str, pheno_name, p_col, beta_col, se_col, sfve_col, nullh2_col, p_var,
+                            perm_min_p, perm_quantile, per_pheno_dirs, bundle_writer)
+        key = (id(ctx["snp_id"]), id(ctx["g_var"]))
+        hit = cache.get(key)
+        if hit is None or hit[0] is not ctx["snp_id"] or hit[1] is not ctx["g_var"]:
+            ids = ctx["snp_id"].to_pylist() if hasattr(ctx["snp_id"], "to_pylist") else list(ctx["snp_id"])
+            table = VariantTable.of(ids, ctx["chrom"], ctx["pos"], ctx["g_var"], int(ctx["phenocount"][0]) - 1)
+            if len(cache) > 8:
+                cache.clear()
+            hit = cache[key] = (ctx["snp_id"], ctx["g_var"], table)  # the objects are kept so their ids stay theirs
+        write_pheno(hit[2], outdir_str, pheno_name, p_col, beta_col, se_col, sfve_col, nullh2_col, p_var,
+                    perm_min_p, perm_quantile, per_pheno_dirs, bundle_writer, lambda_rows=ctx["lambda_rows"])
+
+    return write
 
 
 def uninstall() -> None:

@@ -381,6 +381,11 @@ int flmm_write_gwas_tsv(const char* path, int64_t M, const char* snp_ids, const 
 /* A one-column table (e.g. perms.tsv, fasterlmm/cli.py:154): the header line, then one value per line. */
 int flmm_write_column_tsv(const char* path, const char* header, const double* v, int64_t n);
 
+/* Host memory: dst[r * ld + j] = vec[j] for r < rows, j < n, on up to `threads` host threads.  The streamed result
+ * path fills each chromosome's nullh2 rows this way from one (B,) vector instead of copying repeats from the
+ * device.  No counterpart in the reference, which keeps its results on one device. */
+int flmm_fill_rows_host_f64(double* dst, int64_t ld, int64_t rows, const double* vec, int64_t n, int threads);
+
 #ifdef __cplusplus
 }
 #endif

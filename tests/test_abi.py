@@ -65,3 +65,17 @@ def test_no_cpu_fallback_without_cuda():
     from fasterlmm_gb300 import core
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         core.grm(torch.zeros(4, 4, dtype=torch.float64))
+
+
+def test_host_row_fill(built):
+    """flmm_fill_rows_host_f64 (host code: the streamed nullh2 rows) fills exactly the rows and columns asked for."""
+    import numpy as np
+    from fasterlmm_gb300 import _lib
+    for rows, threads in ((2000, 8), (100, 8), (1, 1), (5000, 3)):
+        dst = np.zeros((rows + 20, 70))
+        vec = np.random.default_rng(rows).standard_normal(64)
+        _lib.call("flmm_fill_rows_host_f64", dst.ctypes.data + 8 * 70 * 10, 70, rows, vec.ctypes.data, 64, threads)
+        assert (dst[10:10 + rows, :64] == vec).all()
+        assert not dst[:10].any() and not dst[10 + rows:].any() and not dst[:, 64:].any()
+    with pytest.raises(_lib.FlmmError):
+        _lib.call("flmm_fill_rows_host_f64", None, 70, 10, None, 64, 1)

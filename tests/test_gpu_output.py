@@ -65,7 +65,9 @@ def test_write_batch_files(golden, tmp_path):
         pv = np.array([float(r[5]) for r in body])
         # rows: a permutation of the variants in ascending written p, ties in variant order, NaN last
         assert sorted(sid) == list(range(M))
-        np.testing.assert_array_equal(sid, np.argsort(pv, kind="stable"))
+        p_by_variant = np.empty(M)
+        p_by_variant[sid] = pv
+        np.testing.assert_array_equal(sid, np.argsort(p_by_variant, kind="stable"))
         np.testing.assert_allclose(pv, p_host[sid, j], rtol=1e-11)
         assert all(r[1] == f"v{s}" and r[3] == "" and r[10] == "0" and r[12] == name and r[13] == "21"
                    for r, s in zip(body, sid))

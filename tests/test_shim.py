@@ -43,3 +43,34 @@ def test_install_and_uninstall_rebind_reference_names():
     finally:
         for k in ("fasterlmm.core", "fasterlmm.perms", "fasterlmm.cli"):
             sys.modules.pop(k, None)
+
+
+def test_cli_writer_is_routed_through_output_module(golden, tmp_path):
+    """With outputs=True the CLI's per-phenotype writer writes the reference's files through this package."""
+    import numpy as np
+    from fasterlmm_gb300 import build, shim
+    build()
+    g = golden("output_files")
+    calls = []
+    cli = types.ModuleType("fasterlmm.cli")
+    cli._write_pheno = lambda *a, **k: calls.append(a)
+    shim.install(form="fast", modules={"cli": cli}, outputs=True)
+    try:
+        M, n_perm = int(g["M"]), int(g["n_perm"])
+        ctx = {"snp_id": list(g["snp"]), "chrom": g["chrom"], "pos": g["pos"], "g_var": g["g_var"],
+               "sid_index": np.arange(M), "gendist": None, "mixing": np.zeros(M),
+               "phenocount": np.full(M, 1 + n_perm), "pheno_idx": None, "lambda_rows": []}
+        for j, name in enumerate(g["pheno"]):
+            cli._write_pheno({**ctx}, str(tmp_path), str(name), p_col=g["p"][:, j], beta_col=g["beta"][:, j],
+                             se_col=g["se"][:, j], sfve_col=g["sfve"][:, j], nullh2_col=g["nullh2"][:, j],
+                             p_var=float(g["p_var"][j]), perm_min_p=g["perm_min_p"][j],
+                             perm_quantile=float(g["perm_quantile"]), per_pheno_dirs=True, bundle_writer=None)
+            for fname in ("gwas.tsv", "perms.tsv", "threshold.txt", "lambda_gc.txt"):
+                assert (tmp_path / str(name) / fname).read_bytes() == bytes(g[f"file_{j}_{fname}"])
+        assert [r[0] for r in ctx["lambda_rows"]] == [str(n) for n in g["pheno"]]
+        cli._write_pheno({**ctx, "clump": {"z": None}}, str(tmp_path), "x", None, None, None, None, None, 1.0, None,
+                         0.05, True, None)
+        assert len(calls) == 1  # clumping goes to the original writer
+    finally:
+        shim.uninstall()
+    assert not hasattr(cli._write_pheno, "__wrapped__") and cli._write_pheno(1) is None and len(calls) == 2
