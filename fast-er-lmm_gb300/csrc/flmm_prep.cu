@@ -58,14 +58,16 @@ k_standardise_f64(const double* __restrict__ Z, int64_t ldz, int N, int M, doubl
         std_s[tx] = (sd == 0.0) ? INFINITY : sd;
     }
     __syncthreads();
-    const double sd = std_s[tx];
+    // one reciprocal per variant and a multiply per element: FP64 division is a multi-instruction sequence on an
+    // FP64 pipe with a small fraction of the FP32 rate (the result moves by at most one rounding)
+    const double inv_sd = 1.0 / std_s[tx];
     for (int i0 = 0; i0 < N; i0 += kStdCols) {
         for (int r = ty; r < kStdCols; r += kStdRows) {
             int i = i0 + r;
             double v = 0.0;
             if (col_ok && i < N) {
                 double a = Z[static_cast<int64_t>(i) * ldz + j];
-                v = isnan(a) ? 0.0 : (a - mean) / sd;
+                v = isnan(a) ? 0.0 : (a - mean) * inv_sd;
             }
             tile[r][tx] = v;  // tile[sample][variant]
         }

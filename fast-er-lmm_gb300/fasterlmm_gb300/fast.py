@@ -28,14 +28,18 @@ F16 = torch.float16
 F32 = torch.float32
 
 # Precision of the per-chromosome eigendecompositions.
-#   "f32r" (default): one FP32 cusolverDnXsyevBatched call for all LOCO kinships, then one refinement step of the
-#          eigenvectors against the FP64 kinships (flmm_eigh_refine_f32) and FP64 Rayleigh-quotient eigenvalues.
+#   "f32r" (default): one FP32 cusolverDnXsyevBatched call for all LOCO kinships, then EIGH_REFINE_STEPS refinement
+#          steps of the eigenvectors against the FP64 kinships (flmm_eigh_refine_f32) with FP64 Rayleigh-quotient
+#          eigenvalues.  At N = 1,000 the kinship spectrum is a tight bulk (gaps ~1e-4 of its width), where one step
+#          leaves beta ~1e-4 off the FP64 result on a fifth of the tests; two steps match the FP64 decomposition's
+#          outputs (beta and SE within 1e-5 of the FP64 oracle), a third changes nothing.
 #   "f32": the FP32 call alone.  F, beta, SE, SFVE and -log10 p stay inside the parity tolerance, but on phenotypes
 #          with a flat likelihood (h2 near 0) the decomposition's ~1e-7 error moves the fitted delta, and with it
 #          nullh2 = 1 / (1 + delta), by more than 1e-5 relative; the refinement step removes that.
 #   "f64": the FP64 batched call (EIGH_MODE: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on worker streams).
 EIGH_PRECISION = "f32r"
 EIGH_MODE = 1
+EIGH_REFINE_STEPS = 2
 # Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
 # fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
 DELTA_PROPOSAL = "grid"
@@ -357,8 +361,11 @@ def _eigh_batched_f32_refined(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
     U_ref = torch.empty_like(U)
     evals = torch.empty((batch, N), dtype=F64, device=dev)
     w, wb = _work.get(dev, _lib.query_bytes("flmm_eigh_refine_workspace_bytes", N, batch))
-    _lib.call("flmm_eigh_refine_f32", _ptr(Kp), _ptr(U), _ptr(U_ref), _ptr(evals), N, batch, w, wb, _stream(dev))
-    return U_ref, evals
+    for _ in range(max(1, EIGH_REFINE_STEPS)):
+        _lib.call("flmm_eigh_refine_f32", _ptr(Kp), _ptr(U), _ptr(U_ref), _ptr(evals), N, batch, w, wb,
+                  _stream(dev))
+        U, U_ref = U_ref, U
+    return U, evals
 
 
 def _spectrum(evals: Tensor, D: int) -> Tensor:
