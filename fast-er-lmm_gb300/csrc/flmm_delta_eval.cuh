@@ -112,7 +112,11 @@ struct GlobalColumn {
 
 // Safeguarded Newton on g in a bracket with g(lo) < 0 < g(hi), starting at x0 (the bracket's midpoint if x0 is not
 // inside).  The FP32 sums put a noise floor of ~1e-7 on x: near the root the Newton steps stop shrinking and jump
-// around the root by that much, so the iteration ends once a step or the bracket is below 1e-7.
+// around the root by that much, so the iteration ends once a step or the bracket is below 1e-7.  It also ends right
+// after a Newton step shorter than kNewtonDone: Newton's error after a step of length h is ~|g'' / 2g'| h^2, below
+// the noise floor for h < 3e-5 on these losses, so the evaluation that would only confirm convergence is skipped.
+constexpr double kNewtonDone = 3e-5;
+
 template <class Ev>
 __device__ double newton_in_bracket(const Ev& ev, double lo, double hi, double x0, const NewtonEval* first = nullptr) {
     const bool inside = x0 > lo && x0 < hi;
@@ -122,31 +126,42 @@ __device__ double newton_in_bracket(const Ev& ev, double lo, double hi, double x
         if (e.g == 0.0f) break;
         if (e.g < 0.0f) lo = x; else hi = x;
         double xn = x - static_cast<double>(e.g / e.gp);
-        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const bool newton = xn > lo && xn < hi;
+        if (!newton) xn = 0.5 * (lo + hi);
         const double stepx = fabs(xn - x);
         x = xn;
-        if (stepx < 1e-7 || hi - lo < 1e-7) break;
+        if (stepx < 1e-7 || hi - lo < 1e-7 || (newton && stepx < kNewtonDone)) break;
     }
     return x;
 }
 
-// log delta of one column from its grid argmin i (warp-uniform result).  `first`, if given, is the evaluation at
-// grid[i].
+// Evaluations a first pass over the column may have done already: at grid[i] (`at`) and, when the argmin is inside
+// the grid, at its neighbours grid[i - 1] and grid[i + 1] (`lo`, `hi`).
+struct FirstEvals {
+    NewtonEval at, lo, hi;
+    bool have_at = false, have_nb = false;
+};
+
+// log delta of one column from its grid argmin i (warp-uniform result).  `first`, if given, holds evaluations
+// already done.
 template <class Ev>
 __device__ double refine_column(const Ev& ev, const double* __restrict__ grid, int G, int i, int refine,
-                                const NewtonEval* first = nullptr) {
+                                const FirstEvals* first = nullptr) {
     double out = grid[i];
+    const NewtonEval* at = (first && first->have_at) ? &first->at : nullptr;
     if (refine && i > 0 && i < G - 1) {
         // the usual case: d loss / d log delta changes sign between the argmin's neighbours
         const double a = grid[i - 1], b = grid[i + 1];
-        if (ev(a, false).g < 0.0f && ev(b, false).g > 0.0f) return newton_in_bracket(ev, a, b, grid[i], first);
+        const bool nb = first && first->have_nb;
+        const float ga = nb ? first->lo.g : ev(a, false).g;
+        if (ga < 0.0f && (nb ? first->hi.g : ev(b, false).g) > 0.0f) return newton_in_bracket(ev, a, b, grid[i], at);
     }
     if (refine && G > 1) {
         // The FP32 grid argmin is only as good as the FP32 loss (~1e-4 absolute); on flat losses it can sit several
         // nodes from the minimum.  The exact derivative sign at that node says which side the minimum is on, and a
         // binary search over the grid nodes on that side finds where d loss / d log delta changes sign, so the
         // bracket [grid[i-1], grid[i+1]] always contains the minimum (for losses with one minimum on that side).
-        const float gi = first ? first->g : ev(grid[i], false).g;
+        const float gi = at ? at->g : ev(grid[i], false).g;
         if (gi < 0.0f) {
             if (ev(grid[G - 1], false).g < 0.0f) {
                 i = G - 1;  // still falling at the top of the grid

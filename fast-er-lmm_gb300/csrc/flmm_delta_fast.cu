@@ -154,20 +154,36 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
     const float* u = UYt + p * ldu;
     const float sbar = *sbar_p;
     const int i = idx[p];
-    // one pass gives the column's sum of squares and the evaluation at the grid argmin
+    // one pass gives the column's sum of squares and the evaluations at the grid argmin and its two neighbours (the
+    // bracket test of the usual case), sharing the loads of the column and the spectrum
+    const bool inner = refine && i > 0 && i < G - 1;
     const EvalPoint pt = eval_point(grid[i], sbar);
-    EvalSums t;
+    const EvalPoint pa = eval_point(grid[inner ? i - 1 : i], sbar);
+    const EvalPoint pb = eval_point(grid[inner ? i + 1 : i], sbar);
+    EvalSums t, ta, tb;
     float uh = 0.f, uc = 0.f;
     for (int n = lane; n < Neff; n += 32) {
         const float un = u[n];
         const float uu = un * un;
+        const float sn = s32[n], dn = dsb[n];
         neumaier(uh, uc, uu);
-        t.add(s32[n], dsb[n], uu, pt, false);
+        t.add(sn, dn, uu, pt, false);
+        if (inner) {
+            ta.add(sn, dn, uu, pa, false);
+            tb.add(sn, dn, uu, pb, false);
+        }
     }
     const float U = warp_sum_pair(uh, uc);
-    const NewtonEval e0 = finish_eval(t, U, Neff, pt, false);
+    FirstEvals first;
+    first.at = finish_eval(t, U, Neff, pt, false);
+    first.have_at = true;
+    if (inner) {
+        first.lo = finish_eval(ta, U, Neff, pa, false);
+        first.hi = finish_eval(tb, U, Neff, pb, false);
+        first.have_nb = true;
+    }
     const GlobalColumn ev{s32, dsb, u, Neff, sbar, U};
-    const double out = refine_column(ev, grid, G, i, refine, &e0);
+    const double out = refine_column(ev, grid, G, i, refine, &first);
     if (lane == 0) log_delta[p] = out;
 }
 
