@@ -12,7 +12,9 @@ the low-rank names of ``fasterlmm.lowrank`` and the copies ``fasterlmm.extreme_s
 extreme_scan.py:21-22) to the low-rank kernels, so the streamed engine's block loop runs its math on the GPU.  The
 CLI and any user code that goes through those names then runs on the GPU unchanged.  ``uninstall()`` restores
 the originals.  The CLI's per-phenotype writer ``fasterlmm.cli._write_pheno`` is rebound to fasterlmm_gb300.output,
-whose files are byte-identical to the reference's.
+whose files are byte-identical to the reference's.  When the LUX epistasis modules are loaded, their batched Wald
+(``fasterlmm_lux.epi._kernel.snp_wald_scan_batched`` and the copy ``fasterlmm_lux.epi.scan`` imported by name) is
+rebound to fasterlmm_gb300.epi.
 """
 from __future__ import annotations
 
@@ -52,6 +54,9 @@ def install(form: str = "fast", modules: dict | None = None, outputs: bool = Tru
         for key in ("cli", "extreme", "lowrank", "extreme_scan"):
             if f"fasterlmm.{key}" in sys.modules:
                 mods[key] = sys.modules[f"fasterlmm.{key}"]
+        for key, name in (("lux_kernel", "fasterlmm_lux.epi._kernel"), ("lux_scan", "fasterlmm_lux.epi.scan")):
+            if name in sys.modules:
+                mods[key] = sys.modules[name]
     ours = {
         "loco_scan_compat": functools.partial(core.loco_scan_compat, form=form),
         "single_k_scan_compat": functools.partial(core.single_k_scan_compat, form=form),
@@ -76,6 +81,12 @@ def install(form: str = "fast", modules: dict | None = None, outputs: bool = Tru
             if m is not None and hasattr(m, name):
                 _set(m, name, getattr(lowrank, name))
                 patched.append(f"{m.__name__}.{name}")
+    from . import epi
+    for key in ("lux_kernel", "lux_scan"):
+        m = mods.get(key)
+        if m is not None and hasattr(m, "snp_wald_scan_batched"):
+            _set(m, "snp_wald_scan_batched", epi.snp_wald_scan_batched)
+            patched.append(f"{m.__name__}.snp_wald_scan_batched")
     cli = mods.get("cli")
     if outputs and cli is not None and hasattr(cli, "_write_pheno"):
         key = (cli.__name__, "_write_pheno")

@@ -358,6 +358,16 @@ int flmm_perm_threshold_p(const double* perm_max_F, int B, int n_perm, int df2, 
  * F <= 0 gives 1, +inf gives 0, NaN stays NaN. */
 int flmm_f_pvalue(const double* F, int64_t n, int df2, double* out, void* stream);
 
+/* Batched epistasis Wald, per anchor and phenotype chunk (lux/src/fasterlmm_lux/epi/_kernel.py:21-150): from
+ * G1 (Pc (C + 1), Mc) FP32 = [Q_p; (w_p o r_p)] S (Q_p = L_p^-1 X^T W_p, C rows per phenotype), G2 (Pc, Mc) FP32 =
+ * W (S o S) and rWr (Pc,): quad = ||Q_p s_m||^2, denom = max(sWs - quad, 1e-300), beta, SE, F (F = 0 where
+ * sWs - quad < floor_rel sWs); detail at (m0 + m) * ldo + p0 + p for p0 + p < n_real; running maximum F and its
+ * first column into max_f / argmax (P,) (a chunk replaces them only when strictly greater, never when its maximum
+ * is NaN).  var_df = N - C - 1. */
+int flmm_epi_wald_f32(const float* G1, int64_t ldg1, const float* G2, int64_t ldg2, const double* rWr, int Pc, int C,
+                      int Mc, int m0, int p0, int n_real, double var_df, double floor_rel, double* beta, double* se,
+                      double* F, int64_t ldo, double* max_f, int64_t* argmax, void* stream);
+
 /* ---- output files (host code; fasterlmm/cli.py:100-161) ---------------------------------------------------------
  * Numbers are written as the reference's pyarrow CSV writer writes them: shortest round-trip digits, fixed notation
  * for decimal exponents -6 .. 9, d.ddde+X otherwise, nan / inf / -inf.  Each call writes one file and holds no

@@ -689,6 +689,61 @@ def perm_threshold(Z_raw: np.ndarray, X: np.ndarray, Y: np.ndarray, chrom: np.nd
 
 
 # --------------------------------------------------------------------------------------------------------------
+# batched epistasis Wald (LUX tier 2)
+# --------------------------------------------------------------------------------------------------------------
+
+def epi_wald_batched(s: np.ndarray, X: np.ndarray, Y: np.ndarray, log_delta: np.ndarray, S: np.ndarray, *,
+                     n_real: int | None = None, denom_floor_rel: float = 0.01):
+    """
+    Batched epistasis Wald over K anchors (lux/src/fasterlmm_lux/epi/_kernel.py:21-150): for anchor k the design is
+    X[k] (N, C) (shared covariates plus the anchor column), the test columns S[k] (N, M).  Per phenotype p with
+    w = 1 / (s + delta_p): A = X^T W X, beta_x = A^-1 X^T W y, r = y - X beta_x, rWr = max(sum w r^2, 1e-300)
+    (:74-83); per test column: B = X^T W s_m, quad = B^T A^-1 B, sWs = sum w s_m^2, num = sum w r s_m,
+    denom = max(sWs - quad, 1e-300), beta = num / denom, rss = max(rWr - num^2 / denom, 1e-300),
+    var_beta = rss / (N - C - 1) / denom, se = sqrt(var_beta), F = beta^2 / var_beta, and F = 0 where
+    sWs - quad < denom_floor_rel sWs (:118-133).  Returns beta, se, F (K, M, n_real), max F (K, P) and the first
+    test column reaching it (K, P) (:135-139; ties keep the earlier column).
+    """
+    K, N, C = X.shape
+    P = Y.shape[1]
+    M = S.shape[2]
+    n_real = P if n_real is None else min(n_real, P)
+    var_df = N - C - 1
+    beta_o = np.empty((K, M, n_real))
+    se_o = np.empty((K, M, n_real))
+    f_o = np.empty((K, M, n_real))
+    max_f = np.full((K, P), -np.inf)
+    arg = np.zeros((K, P), dtype=np.int64)
+    for k in range(K):
+        Xk, Sk = X[k], S[k]
+        for p in range(P):
+            w = 1.0 / (s + np.exp(log_delta[p]))
+            WX = w[:, None] * Xk
+            A = WX.T @ Xk
+            Ainv = np.linalg.inv(A)
+            beta_x = Ainv @ (WX.T @ Y[:, p])
+            r = Y[:, p] - Xk @ beta_x
+            rWr = max(float(np.sum(w * r * r)), 1e-300)
+            B = WX.T @ Sk                       # (C, M)
+            quad = np.einsum("cm,cm->m", B, Ainv @ B)
+            sWs = w @ (Sk * Sk)
+            num = (w * r) @ Sk
+            denom_raw = sWs - quad
+            denom = np.maximum(denom_raw, 1e-300)
+            beta = num / denom
+            rss = np.maximum(rWr - num * num / denom, 1e-300)
+            var_beta = rss / var_df / denom
+            F = beta * beta / var_beta
+            if denom_floor_rel > 0.0:
+                F = np.where(denom_raw < denom_floor_rel * sWs, 0.0, F)
+            j = int(np.argmax(F))
+            max_f[k, p], arg[k, p] = F[j], j
+            if p < n_real:
+                beta_o[k, :, p], se_o[k, :, p], f_o[k, :, p] = beta, np.sqrt(var_beta), F
+    return beta_o, se_o, f_o, max_f, arg
+
+
+# --------------------------------------------------------------------------------------------------------------
 # post-scan statistics and NA grouping
 # --------------------------------------------------------------------------------------------------------------
 

@@ -74,3 +74,18 @@ def test_cli_writer_is_routed_through_output_module(golden, tmp_path):
     finally:
         shim.uninstall()
     assert not hasattr(cli._write_pheno, "__wrapped__") and cli._write_pheno(1) is None and len(calls) == 2
+
+
+def test_lux_batched_wald_is_rebound():
+    from fasterlmm_gb300 import epi, shim
+    kern = _fake("fasterlmm_lux.epi._kernel", ["snp_wald_scan_batched"])
+    scan = _fake("fasterlmm_lux.epi.scan", ["snp_wald_scan_batched", "scan_tier2"])
+    orig = scan.snp_wald_scan_batched
+    patched = shim.install(form="fast", modules={"lux_kernel": kern, "lux_scan": scan})
+    try:
+        assert scan.snp_wald_scan_batched is epi.snp_wald_scan_batched
+        assert kern.snp_wald_scan_batched is epi.snp_wald_scan_batched
+        assert "fasterlmm_lux.epi.scan.snp_wald_scan_batched" in patched
+    finally:
+        shim.uninstall()
+    assert scan.snp_wald_scan_batched is orig
