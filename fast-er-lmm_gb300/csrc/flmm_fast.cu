@@ -647,6 +647,7 @@ __global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int
 // column's x by the 10-point Lagrange polynomial on the nodes around it (interpolation error < 1e-9 relative).  The
 // second product of the Wald kernel then has K = R (~90) instead of K = Neff.
 constexpr int kInterpPoints = 10;
+constexpr int kPrepCache = 32;  // per-lane register cache of k_wald_prep_columns: columns up to 1,024 entries
 
 // Wald column side (fasterlmm/core.py:639-643): w~ = (shat + delta_p) / (s + delta_p), A1 = w~ o UY split,
 // rWr = sum w~ UY^2, and the column's Lagrange weights L (R entries, 10 non-zero) split.  A block of kPrepCols warps
@@ -695,18 +696,44 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
     const float num = *shat_p + delta;
     const float* u = UYt + p * ldu;
     float m1 = 0.0f, acc = 0.0f, comp = 0.0f;
-    for (int n = lane; n < Neff; n += 32) {
-        const float un = u[n];
-        const float a = (num / (s32[n] + delta)) * un;
-        m1 = fmaxf(m1, fabsf(a));
-        neumaier(acc, comp, a * un);
+    // a column of up to 32 * kPrepCache entries is read once and its weighted values kept in registers for the split
+    float av[kPrepCache];
+    const bool cached = Neff <= 32 * kPrepCache;
+    if (cached) {
+#pragma unroll
+        for (int i = 0; i < kPrepCache; ++i) {
+            const int n = lane + 32 * i;
+            av[i] = 0.0f;
+            if (n < Neff) {
+                const float un = u[n];
+                const float a = (num / (s32[n] + delta)) * un;
+                av[i] = a;
+                m1 = fmaxf(m1, fabsf(a));
+                neumaier(acc, comp, a * un);
+            }
+        }
+    } else {
+        for (int n = lane; n < Neff; n += 32) {
+            const float un = u[n];
+            const float a = (num / (s32[n] + delta)) * un;
+            m1 = fmaxf(m1, fabsf(a));
+            neumaier(acc, comp, a * un);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
     const float rwr = warp_sum_pair(acc, comp);
     int e1;
     const float mul1 = row_scale_exp(m1, &e1);
-    for (int n = lane; n < Neff; n += 32) split_store((num / (s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
+    if (cached) {
+#pragma unroll
+        for (int i = 0; i < kPrepCache; ++i) {
+            const int n = lane + 32 * i;
+            if (n < Neff) split_store(av[i], mul1, A1h, A1l, p * lda + n);
+        }
+    } else {
+        for (int n = lane; n < Neff; n += 32) split_store((num / (s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
+    }
     const int base = lbase[j];
     float lm = 0.0f;
 #pragma unroll

@@ -151,6 +151,49 @@ k_perm_orders(const int64_t* __restrict__ cols, uint64_t seed, int n_perm, int N
     for (int i = threadIdx.x; i < N; i += blockDim.x) out[i] = pos[i];
 }
 
+// Same orders for N <= 2048: the 53-bit key and the 11-bit position packed into one word (key << 11 | position),
+// so the bitonic sort moves and compares single 64-bit values; ascending packed order is the (key, position) order.
+constexpr int kPackBits = 11;
+
+__global__ void __launch_bounds__(kThreads)
+k_perm_orders_packed(const int64_t* __restrict__ cols, uint64_t seed, int n_perm, int N, int npow2,
+                     int32_t* __restrict__ orders) {
+    extern __shared__ uint64_t kp[];
+    const int b = blockIdx.x / n_perm, j = blockIdx.x % n_perm;
+    const Pcg g = seed_pcg(seed, static_cast<uint64_t>(cols[b]));
+    u128 m0, p0, ms, ps;
+    lcg_jump(g.inc, static_cast<uint64_t>(j) * N + threadIdx.x, &m0, &p0);
+    lcg_jump(g.inc, blockDim.x, &ms, &ps);
+    u128 s = m0 * g.state + p0;
+    for (int i = threadIdx.x; i < npow2; i += blockDim.x) {
+        if (i < N) {
+            const u128 s1 = s * pcg_mult() + g.inc;
+            kp[i] = ((xsl_rr(s1) >> 11) << kPackBits) | static_cast<uint64_t>(i);
+            s = ms * s + ps;
+        } else {
+            kp[i] = ~0ull;  // padding sorts last
+        }
+    }
+    __syncthreads();
+    for (int size = 2; size <= npow2; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < npow2 / 2; i += blockDim.x) {
+                const int lo = 2 * i - (i & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t a = kp[lo], c = kp[hi];
+                if ((a > c) == up) {
+                    kp[lo] = c;
+                    kp[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    int32_t* out = orders + (static_cast<int64_t>(b) * n_perm + j) * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) out[i] = static_cast<int32_t>(kp[i] & ((1u << kPackBits) - 1));
+}
+
 }  // namespace
 
 extern "C" int flmm_perm_orders(const int64_t* seed_cols, int B, uint64_t seed, int n_perm, int N, int32_t* orders,
@@ -162,6 +205,12 @@ extern "C" int flmm_perm_orders(const int64_t* seed_cols, int B, uint64_t seed, 
     FLMM_REQUIRE(static_cast<int64_t>(B) * n_perm <= 0x7fffffff, "flmm_perm_orders: too many rows");
     int npow2 = 1;
     while (npow2 < N) npow2 <<= 1;
+    if (npow2 <= (1 << kPackBits)) {
+        const size_t smem_p = static_cast<size_t>(npow2) * sizeof(uint64_t);
+        k_perm_orders_packed<<<B * n_perm, kThreads, smem_p, as_stream(stream)>>>(seed_cols, seed, n_perm, N, npow2,
+                                                                                orders);
+        return check_launch("k_perm_orders_packed");
+    }
     const size_t smem = static_cast<size_t>(npow2) * (sizeof(uint64_t) + sizeof(int32_t));
     if (smem > 48 * 1024)
         FLMM_CUDA(cudaFuncSetAttribute(k_perm_orders, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));

@@ -32,13 +32,13 @@ def test_epi_batched_matches_reference(golden, case):
 
 
 def test_epi_rank_deficient_anchor_raises():
-    """A design with a repeated column makes A singular: the batch raises LinAlgError, as the reference's does."""
+    """A design with an all-zero column makes A singular: the batch raises LinAlgError, as the reference's does."""
     from fasterlmm_gb300.epi import snp_wald_scan_batched
     rng = np.random.default_rng(0)
     N, C = 40, 3
     X = rng.standard_normal((1, N, C))
-    X[0, :, 2] = X[0, :, 1]
+    X[0, :, 2] = 0.0  # an exactly zero pivot (a repeated column leaves a rounding-sized one of either sign)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a))
     with pytest.raises(torch.linalg.LinAlgError):
-        snp_wald_scan_batched(torch.rand(N, dtype=torch.float64), torch.from_numpy(X),
-                              torch.randn(N, 2, dtype=torch.float64), torch.zeros(2, dtype=torch.float64),
-                              torch.randn(1, N, 5, dtype=torch.float64))
+        snp_wald_scan_batched(t(rng.uniform(0.5, 2.0, N)), t(X), t(rng.standard_normal((N, 2))), t(np.zeros(2)),
+                              t(rng.standard_normal((1, N, 5))))

@@ -199,7 +199,8 @@ def test_device_permutation_orders_are_bit_identical():
     """The device PCG64 / SeedSequence / argsort path reproduces numpy's orders exactly, incl. large seeds."""
     from fasterlmm_gb300 import perms
     for N, cols, n_perm, seed in [(150, range(20), 100, 19930909), (1000, [0, 5, 6483], 10, 19930909),
-                                  (37, [3, 2**33 + 5], 4, 2**40 + 17), (1, [0], 3, 7)]:
+                                  (37, [3, 2**33 + 5], 4, 2**40 + 17), (1, [0], 3, 7),
+                                  (2048, [4], 2, 5), (3000, [1, 9], 2, 11)]:  # packed-key sort up to 2048
         dev_o = perms.perm_orders_device(N, cols, n_perm, seed, torch.device(DEV)).cpu().numpy()
         host_o = perms.perm_orders(N, cols, n_perm, seed)
         assert np.array_equal(dev_o, host_o), (N, list(cols)[:3], seed)
