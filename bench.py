@@ -202,8 +202,10 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    from fasterlmm_gb300 import _lib, build, perms
+    from fasterlmm_gb300 import _lib, build, fast, perms
     build()
+    if args.delta is not None:
+        fast.DELTA_PROPOSAL = args.delta
     d, w = make_inputs(args.B, args.M)
     N, M, B, n_perm = w["N"], w["M"], w["B"], w["n_perm"]
     P = B * (1 + n_perm)
@@ -277,6 +279,19 @@ def run_ours(args):
                 "executed_tensor_frac": exec_flop / mean_s / 1e12 / peak,
                 "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)"}
 
+    # the phenotype rotation UY = U_eff^T Y_r per chromosome (split-FP16 tcgen05 GEMM): 2 N Neff P algorithmic flop
+    rot_ms = [a.elapsed_time(b) for a, b in timers.get("rotate", []) if b is not None]
+    rotation = None
+    if rot_ms:
+        mean_s = statistics.mean(rot_ms) / 1e3
+        alg = 2.0 * N * Neff * P
+        rotation = {"kernel": "k_pair<1> (split-FP16 GEMM, UY = U_eff^T Y_r)", "launch_ms": 1e3 * mean_s,
+                    "algorithmic_tflops": alg / mean_s / 1e12, "frac": alg / mean_s / 1e12 / peaks["tensor_tflops"],
+                    "executed_tensor_frac": 3 * alg / mean_s / 1e12 / peaks["tensor_tflops"],
+                    "peak_source": peaks["source"] + " bf16 dense"}
+    stages = {k: round(sum(a.elapsed_time(b) for a, b in v if b is not None) / args.steps, 3)
+              for k, v in timers.items()}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -284,9 +299,11 @@ def run_ours(args):
             "data": "synthetic (seeded: Binomial(2, MAF~U[0.01,0.5]) genotypes, RINT phenotypes, 0-50 causal)",
             "config": {"workload": WORKLOAD, "N": N, "M": M, "B": B, "n_perm": n_perm, "P": P, "chromosomes": w["n_chrom"],
                        "covariates": w["D"], "grid": w["n_grid"], "form": args.form,
+                       "delta_fit": fast.DELTA_PROPOSAL,
                        "l2": "inputs larger than L2 (Z 0.8 GB FP64, operands >100 MB per chromosome)",
                        "parallelism": f"{world} replica(s), no cross-GPU exchange"},
-            "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "clocks": clk}
+            "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "rotation_roofline": rotation,
+            "stage_ms_per_step": stages, "clocks": clk}
 
     data_dev = None  # the e2e leg starts from host data only
     if host_bufs is not None:
@@ -347,6 +364,8 @@ def main():
     ap.add_argument("--form", choices=["fast", "plain"], default="fast")
     ap.add_argument("--B", type=int, default=None, help="override the phenotype count (quick runs)")
     ap.add_argument("--M", type=int, default=None, help="override the variant count (quick runs)")
+    ap.add_argument("--delta", choices=["grid", "learned"], default=None,
+                    help="fast form's delta fit: full FP32 grid, or the learned proposal's narrow bracket")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

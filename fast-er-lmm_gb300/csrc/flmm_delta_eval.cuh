@@ -219,5 +219,23 @@ __device__ inline float load_spectrum(const double* __restrict__ s, int Neff, fl
     return sbar;
 }
 
+// ---- pieces of the fast fit shared with the learned-proposal path (defined in flmm_delta_fast.cu) -------------
+
+// workspace of the fast fit: grid (G doubles) | Wg (G x Neff) | sum_log (G) | s32 (Neff) | dsb (Neff) | sbar
+struct FastWs {
+    double* grid;
+    float *Wg, *sum_log, *s32, *dsb, *sbar;
+};
+size_t fast_ws(int Neff, int G);
+FastWs carve_fast(void* base, int Neff, int G);
+// grid nodes, Wg[g, n] = 1 / (s_n + delta_g) and sum_log[g] = sum_n log(s_n + delta_g)
+int launch_grid_tables(const double* s, int Neff, double lo, double hi, int G, const FastWs& w, cudaStream_t st);
+// first FP32 grid argmin of the columns cols[0 .. *count) (device list and count), written to idx[col]
+int launch_grid_argmin_list(const FastWs& w, const float* UYt, int64_t ldu, int Neff, int P, int G,
+                            const int32_t* cols, const int32_t* count, int32_t* idx, cudaStream_t st);
+// exact refinement of every column from its grid index idx[p] (the fast fit's second half)
+int launch_refine(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int G, const int32_t* idx,
+                  int refine, const FastWs& w, double* log_delta, cudaStream_t st);
+
 }  // namespace dfit
 }  // namespace flmm

@@ -48,15 +48,31 @@ __global__ void k_grid_weights_f32(const double* __restrict__ s, int Neff, const
 constexpr int TG = 64, TP = 64, TK = 32, NT = 256;
 
 // loss[g, p] = Neff log(yWy) + sum_log[g] (+ constants that do not move the argmin), first argmin over g
+// kList: the CTA's 64 columns are entries [64 b, 64 b + 64) of the column list cols[0 .. *count) instead of columns
+// [64 b, 64 b + 64); CTAs past the list's end return at once (the grid is sized for the longest list, P).
+template <bool kList>
 __global__ void __launch_bounds__(NT)
 k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_log, const float* __restrict__ UYt,
-                  int64_t ldu, int Neff, int P, int G, int32_t* __restrict__ idx_out) {
+                  int64_t ldu, int Neff, int P, int G, int32_t* __restrict__ idx_out, const int32_t* __restrict__ cols,
+                  const int32_t* __restrict__ count) {
     __shared__ float Ws[TK][TG + 1];
     __shared__ float Us[TK][TP + 1];
     __shared__ float red_v[16][TP];
     __shared__ int red_i[16][TP];
+    __shared__ int col_s[TP];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int p0 = blockIdx.x * TP;
+    if (kList) {
+        const int n = min(*count, P);
+        if (p0 >= n) return;
+        if (tid < TP) col_s[tid] = (p0 + tid < n) ? cols[p0 + tid] : -1;
+        __syncthreads();
+    }
+    // column of tile slot q (-1: none)
+    auto column = [&](int q) -> int {
+        if (kList) return col_s[q];
+        return (p0 + q < P) ? p0 + q : -1;
+    };
     const float neff = static_cast<float>(Neff);
     float best = INFINITY;
     int best_g = 0;
@@ -72,8 +88,8 @@ k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_lo
 #pragma unroll
             for (int l = 0; l < (TP * TK) / NT; ++l) {
                 int t = tid + l * NT, p = t / TK, k = t % TK;
-                int gp = p0 + p, gk = k0 + k;
-                float u = (gp < P && gk < Neff) ? UYt[static_cast<int64_t>(gp) * ldu + gk] : 0.0f;
+                int gp = column(p), gk = k0 + k;
+                float u = (gp >= 0 && gk < Neff) ? UYt[static_cast<int64_t>(gp) * ldu + gk] : 0.0f;
                 Us[k][p] = u * u;
             }
             __syncthreads();
@@ -116,7 +132,10 @@ k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_lo
         }
         __syncthreads();
     }
-    if (tid < TP && p0 + tid < P) idx_out[p0 + tid] = best_g;
+    if (tid < TP) {
+        const int col = column(tid);
+        if (col >= 0) idx_out[col] = best_g;
+    }
 }
 
 // The spectrum as the evaluations read it, once per fit: s32 = fl32(s), dsb = sbar - s32, sbar = mean(s).
@@ -187,16 +206,33 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
     if (lane == 0) log_delta[p] = out;
 }
 
-// workspace: grid (G doubles) | Wg (G x Neff) | sum_log (G) | s32 (Neff) | dsb (Neff) | sbar
+int launch_fast_fit(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid, double lo,
+                    double hi, int refine, double* log_delta, int32_t* grid_idx, void* scratch, cudaStream_t st) {
+    const FastWs w = carve_fast(scratch, Neff, n_grid);
+    int rc = flmm_delta_grid_nodes(lo, hi, n_grid, w.grid, st);
+    if (rc) return rc;
+    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, w.grid, w.Wg, w.sum_log);
+    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
+    k_grid_argmin_f32<false><<<ceil_div(P, TP), NT, 0, st>>>(w.Wg, w.sum_log, UYt, ldu, Neff, P, n_grid, grid_idx,
+                                                             nullptr, nullptr);
+    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
+    k_spectrum_prep<<<1, 256, 0, st>>>(s, Neff, w.s32, w.dsb, w.sbar);
+    if ((rc = check_launch("k_spectrum_prep"))) return rc;
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(
+        w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, n_grid, grid_idx, refine, log_delta);
+    return check_launch("k_newton_refine");
+}
+
+}  // namespace
+
+// Pieces of the fit for the learned-proposal path (flmm_delta_learned.cu), declared in flmm_delta_eval.cuh.
+namespace flmm {
+namespace dfit {
+
 size_t fast_ws(int Neff, int G) {
     return sizeof(float) * (static_cast<size_t>(G) * Neff + static_cast<size_t>(G) + 2 * static_cast<size_t>(Neff) + 4) +
            sizeof(double) * G + 512;
 }
-
-struct FastWs {
-    double* grid;
-    float *Wg, *sum_log, *s32, *dsb, *sbar;
-};
 
 FastWs carve_fast(void* base, int Neff, int G) {
     FastWs w;
@@ -209,23 +245,31 @@ FastWs carve_fast(void* base, int Neff, int G) {
     return w;
 }
 
-int launch_fast_fit(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid, double lo,
-                    double hi, int refine, double* log_delta, int32_t* grid_idx, void* scratch, cudaStream_t st) {
-    const FastWs w = carve_fast(scratch, Neff, n_grid);
-    int rc = flmm_delta_grid_nodes(lo, hi, n_grid, w.grid, st);
+int launch_grid_tables(const double* s, int Neff, double lo, double hi, int G, const FastWs& w, cudaStream_t st) {
+    int rc = flmm_delta_grid_nodes(lo, hi, G, w.grid, st);
     if (rc) return rc;
-    k_grid_weights_f32<<<n_grid, 256, 0, st>>>(s, Neff, w.grid, w.Wg, w.sum_log);
-    if ((rc = check_launch("k_grid_weights_f32"))) return rc;
-    k_grid_argmin_f32<<<ceil_div(P, TP), NT, 0, st>>>(w.Wg, w.sum_log, UYt, ldu, Neff, P, n_grid, grid_idx);
-    if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
+    k_grid_weights_f32<<<G, 256, 0, st>>>(s, Neff, w.grid, w.Wg, w.sum_log);
+    return check_launch("k_grid_weights_f32");
+}
+
+int launch_grid_argmin_list(const FastWs& w, const float* UYt, int64_t ldu, int Neff, int P, int G,
+                            const int32_t* cols, const int32_t* count, int32_t* idx, cudaStream_t st) {
+    k_grid_argmin_f32<true><<<ceil_div(P, TP), NT, 0, st>>>(w.Wg, w.sum_log, UYt, ldu, Neff, P, G, idx, cols, count);
+    return check_launch("k_grid_argmin_f32 (column list)");
+}
+
+int launch_refine(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int G, const int32_t* idx,
+                  int refine, const FastWs& w, double* log_delta, cudaStream_t st) {
     k_spectrum_prep<<<1, 256, 0, st>>>(s, Neff, w.s32, w.dsb, w.sbar);
-    if ((rc = check_launch("k_spectrum_prep"))) return rc;
+    int rc = check_launch("k_spectrum_prep");
+    if (rc) return rc;
     k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(
-        w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, n_grid, grid_idx, refine, log_delta);
+        w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, G, idx, refine, log_delta);
     return check_launch("k_newton_refine");
 }
 
-}  // namespace
+}  // namespace dfit
+}  // namespace flmm
 
 extern "C" int flmm_fit_delta_fast_workspace_bytes(int Neff, int n_grid, size_t* bytes) {
     FLMM_REQUIRE(bytes && Neff > 0 && n_grid > 0, "flmm_fit_delta_fast_workspace_bytes: bad arguments");

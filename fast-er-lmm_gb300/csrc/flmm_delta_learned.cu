@@ -4,12 +4,15 @@
 //   f_b = log(e_b / E + 1e-12), e_b = sum of UY^2 over the b-th of 32 equal-count bins of the ascending spectrum,
 //   g_b = log(mean of s over bin b + 1e-4)   (the spectrum's shape, shared by all columns of a chromosome),
 //   log(Neff) / 10,
-// 65 inputs -> 128 -> 128 -> 1 with tanh-GELU.  The proposal only chooses where the exact refinement starts: it
-// must fall inside the basin of the FP32 grid argmin ([grid[i-1], grid[i+1]], the reference's golden-section
-// bracket), the sign of d loss / d log delta at the proposal picks the half of the basin that holds the stationary
-// point, one more evaluation at that half's end confirms the sign change, and the fast fit's safeguarded Newton
-// iteration runs in that half, starting from the proposal.  Otherwise the column takes the grid path unchanged.
-// Either way the answer is the exact stationary point of the same loss, so the proposal changes speed, not results.
+// 65 inputs -> 128 -> 128 -> 1 with tanh-GELU.  The proposal collapses the fit's grid search to a narrow bracket:
+// each column evaluates the FP32 grid loss only at the 2 h + 1 grid nodes nearest its proposal and takes their
+// argmin.  The full grid stays both the fallback and the judge:
+//   * a column whose window argmin sits on the window's edge (the minimum may lie outside it) is put on a list whose
+//     columns then get the full grid argmin;
+//   * every audit_stride-th column also evaluates the full grid; if a node outside the window beats the window's
+//     argmin there, every column of the call falls back to the full grid.
+// The exact refinement (the fast fit's bracketed Newton iteration) then runs from the chosen node, as in the grid
+// path, so the answer is the same stationary point of the same loss; the proposal saves grid evaluations.
 #include <math.h>
 
 #include "flmm_common.cuh"
@@ -93,49 +96,72 @@ __global__ void k_delta_mlp(const float* __restrict__ feats, int P, const float*
     if (lane == 0) x_out[p] = fmin(fmax(static_cast<double>(o), lo), hi);
 }
 
-// Exact refinement from the proposal, with the grid path as fallback (see the file comment).
-__global__ void k_newton_from_proposal(const double* __restrict__ s, int Neff, const float* __restrict__ UYt,
-                                       int64_t ldu, int P, const double* __restrict__ grid, int G,
-                                       const int32_t* __restrict__ idx, const double* __restrict__ x_prop,
-                                       double* __restrict__ log_delta, int32_t* __restrict__ n_fallback) {
-    extern __shared__ float sm[];
-    float* s32 = sm;
-    float* dsb = sm + Neff;
-    __shared__ float sbar_s;
-    const float sbar = load_spectrum(s, Neff, s32, dsb, &sbar_s);
+// Grid loss of one column at node g (the FP32 grid path's formula): Neff log(sum_n Wg[g, n] u_n^2) + sum_log[g]
+__device__ __forceinline__ float window_loss(const float* __restrict__ Wg, const float* __restrict__ sum_log,
+                                             const float* __restrict__ u, int Neff, int g, int lane) {
+    const float* w = Wg + static_cast<int64_t>(g) * Neff;
+    float acc = 0.0f;
+    for (int n = lane; n < Neff; n += 32) acc = fmaf(w[n], u[n] * u[n], acc);
+    acc = warp_sum(acc);
+    return static_cast<float>(Neff) * logf(fmaxf(acc, 1e-30f)) + sum_log[g];
+}
+
+// stats: [0] columns on the fallback list, [1] audited columns, [2] audits lost, [3] grid nodes evaluated here
+__global__ void k_delta_window(const float* __restrict__ Wg, const float* __restrict__ sum_log,
+                               const double* __restrict__ grid, int G, const float* __restrict__ UYt, int64_t ldu,
+                               int Neff, int P, const double* __restrict__ x_prop, int half, int audit_stride,
+                               int32_t* __restrict__ idx, int32_t* __restrict__ fb_cols, int32_t* __restrict__ stats) {
     const int lane = threadIdx.x & 31;
     const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (p >= P) return;
     const float* u = UYt + p * ldu;
-    float uh = 0.f, uc = 0.f;
-    for (int n = lane; n < Neff; n += 32) neumaier(uh, uc, u[n] * u[n]);
-    const GlobalColumn ev{s32, dsb, u, Neff, sbar, warp_sum_pair(uh, uc)};
-    const int i = idx[p];
-    const double a = grid[max(i - 1, 0)], b = grid[min(i + 1, G - 1)];
-    const double x0 = x_prop[p];
-    double out = 0.0;
-    bool done = false;
-    if (i > 0 && i < G - 1 && x0 > a && x0 < b) {
-        // the proposal splits the grid argmin's basin: the half towards -g must end with the opposite sign
-        const NewtonEval e0 = ev(x0, false);
-        if (e0.g == 0.0f) {
-            out = x0;
-            done = true;
-        } else {
-            const double xe = e0.g < 0.0f ? b : a;
-            const NewtonEval ee = ev(xe, false);
-            if ((e0.g < 0.0f && ee.g > 0.0f) || (e0.g > 0.0f && ee.g < 0.0f)) {
-                const double blo = e0.g < 0.0f ? x0 : xe, bhi = e0.g < 0.0f ? xe : x0;
-                out = newton_in_bracket(ev, blo, bhi, x0, &e0);
-                done = true;
-            }
+    const double h = G > 1 ? (grid[G - 1] - grid[0]) / (G - 1) : 1.0;
+    const double t = (x_prop[p] - grid[0]) / h;
+    const int c = t <= 0.0 ? 0 : (t >= G - 1 ? G - 1 : static_cast<int>(llrint(t)));
+    const int wlo = max(c - half, 0), whi = min(c + half, G - 1);
+    float best = INFINITY;
+    int bi = wlo;
+    for (int g = wlo; g <= whi; ++g) {
+        const float v = window_loss(Wg, sum_log, u, Neff, g, lane);
+        if (v < best) { best = v; bi = g; }
+    }
+    int evals = whi - wlo + 1;
+    bool edge = (bi == wlo && wlo > 0) || (bi == whi && whi < G - 1);
+    if (audit_stride > 0 && p % audit_stride == 0) {
+        float fbest = INFINITY;
+        int fi = 0;
+        for (int g = 0; g < G; ++g) {
+            const float v = (g >= wlo && g <= whi) ? INFINITY : window_loss(Wg, sum_log, u, Neff, g, lane);
+            if (v < fbest) { fbest = v; fi = g; }
         }
+        evals += G - (whi - wlo + 1);
+        if (lane == 0) {
+            atomicAdd(&stats[1], 1);
+            if (!edge && fbest < best) atomicAdd(&stats[2], 1);  // a node outside the window is lower
+        }
+        if (fbest < best || (fbest == best && fi < bi)) bi = fi;  // the audited column keeps the full-grid argmin
+        edge = false;
     }
-    if (!done) {
-        out = refine_column(ev, grid, G, i, 1);
-        if (lane == 0) atomicAdd(n_fallback, 1);
+    if (lane == 0) {
+        if (edge) fb_cols[atomicAdd(&stats[0], 1)] = static_cast<int32_t>(p);
+        else idx[p] = bi;
+        atomicAdd(&stats[3], evals);
     }
-    if (lane == 0) log_delta[p] = out;
+}
+
+// After a lost audit every column goes on the fallback list.
+__global__ void k_window_fallback_all(int P, int32_t* __restrict__ fb_cols, int32_t* __restrict__ stats) {
+    if (stats[2] == 0) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) fb_cols[p] = p;
+    if (p == 0) stats[0] = P;
+}
+
+inline size_t pad256(size_t x) { return (x + 255) / 256 * 256; }
+
+size_t learned_ws(int Neff, int G, int P) {
+    return pad256(fast_ws(Neff, G)) + pad256(sizeof(float) * static_cast<size_t>(P) * kIn) +
+           pad256(sizeof(double) * static_cast<size_t>(P)) + pad256(sizeof(int32_t) * static_cast<size_t>(P));
 }
 
 }  // namespace
@@ -160,19 +186,48 @@ extern "C" int flmm_delta_mlp_f32(const float* feats, int P, const float* W1, co
     return check_launch("k_delta_mlp");
 }
 
-extern "C" int flmm_newton_from_proposal(const double* s, int Neff, const float* UYt, int64_t ldu, int P,
-                                         const double* grid, int n_grid, const int32_t* grid_idx,
-                                         const double* x_prop, double* log_delta, int32_t* n_fallback, void* stream) {
-    FLMM_REQUIRE(s && UYt && grid && grid_idx && x_prop && log_delta && n_fallback && Neff > 0 && n_grid > 0 &&
-                     ldu >= Neff && P >= 0,
-                 "flmm_newton_from_proposal: bad arguments");
-    FLMM_REQUIRE(Neff <= 12288, "flmm_newton_from_proposal: Neff must be <= 12288 (shared-memory spectrum)");
+extern "C" int flmm_fit_delta_learned_workspace_bytes(int Neff, int n_grid, int P, size_t* bytes) {
+    FLMM_REQUIRE(bytes && Neff > 0 && n_grid > 0 && P >= 0, "flmm_fit_delta_learned_workspace_bytes: bad arguments");
+    *bytes = learned_ws(Neff, n_grid, P);
+    return FLMM_OK;
+}
+
+extern "C" int flmm_fit_delta_learned(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
+                                      double lo, double hi, int refine, const float* W1, const float* b1,
+                                      const float* W2, const float* b2, const float* w3, float b3, int half_width,
+                                      int audit_stride, double* log_delta, int32_t* grid_idx, int32_t* stats,
+                                      void* work, size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(s && UYt && W1 && b1 && W2 && b2 && w3 && log_delta && grid_idx && stats && work && n_grid > 0 &&
+                     ldu >= Neff && P >= 0 && half_width >= 1 && audit_stride >= 0,
+                 "flmm_fit_delta_learned: bad arguments");
+    FLMM_REQUIRE(Neff >= kBins, "flmm_fit_delta_learned: Neff must be >= %d (the proposal's features)", kBins);
+    const size_t need = learned_ws(Neff, n_grid, P);
+    if (work_bytes < need)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_fit_delta_learned: need %zu bytes, got %zu", need, work_bytes);
+    cudaStream_t st = as_stream(stream);
+    FLMM_CUDA(cudaMemsetAsync(stats, 0, 4 * sizeof(int32_t), st));
     if (P == 0) return FLMM_OK;
-    const size_t smem = 2 * sizeof(float) * static_cast<size_t>(Neff);
-    if (smem > 48 * 1024)
-        FLMM_CUDA(cudaFuncSetAttribute(k_newton_from_proposal, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem)));
-    k_newton_from_proposal<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, smem, as_stream(stream)>>>(
-        s, Neff, UYt, ldu, P, grid, n_grid, grid_idx, x_prop, log_delta, n_fallback);
-    return check_launch("k_newton_from_proposal");
+    char* base = static_cast<char*>(work);
+    const FastWs w = carve_fast(base, Neff, n_grid);
+    size_t off = pad256(fast_ws(Neff, n_grid));
+    float* feats = reinterpret_cast<float*>(base + off);
+    off += pad256(sizeof(float) * static_cast<size_t>(P) * kIn);
+    double* x_prop = reinterpret_cast<double*>(base + off);
+    off += pad256(sizeof(double) * static_cast<size_t>(P));
+    int32_t* fb_cols = reinterpret_cast<int32_t*>(base + off);
+
+    int rc = launch_grid_tables(s, Neff, lo, hi, n_grid, w, st);
+    if (rc) return rc;
+    const unsigned warps_grid = ceil_div(static_cast<int64_t>(P) * 32, 256);
+    k_delta_features<<<warps_grid, 256, 0, st>>>(s, Neff, UYt, ldu, P, feats);
+    if ((rc = check_launch("k_delta_features"))) return rc;
+    k_delta_mlp<<<warps_grid, 256, 0, st>>>(feats, P, W1, b1, W2, b2, w3, b3, lo, hi, x_prop);
+    if ((rc = check_launch("k_delta_mlp"))) return rc;
+    k_delta_window<<<warps_grid, 256, 0, st>>>(w.Wg, w.sum_log, w.grid, n_grid, UYt, ldu, Neff, P, x_prop, half_width,
+                                               audit_stride, grid_idx, fb_cols, stats);
+    if ((rc = check_launch("k_delta_window"))) return rc;
+    k_window_fallback_all<<<ceil_div(P, 256), 256, 0, st>>>(P, fb_cols, stats);
+    if ((rc = check_launch("k_window_fallback_all"))) return rc;
+    if ((rc = launch_grid_argmin_list(w, UYt, ldu, Neff, P, n_grid, fb_cols, stats, grid_idx, st))) return rc;
+    return launch_refine(s, Neff, UYt, ldu, P, n_grid, grid_idx, refine, w, log_delta, st);
 }

@@ -80,7 +80,23 @@ struct TcArgs {
     double* sfve;
     int64_t ldo;
     double* max_F;
+    // tile order of the persistent schedule (see tile_coords); 0 or 1 = A-major
+    int group;
 };
+
+// Tile t of the persistent schedule -> (A block ta, B block tb).  Tiles are visited in groups of `group` A blocks;
+// inside a group the B block is the major index, so the group's A blocks stay in L2 while every B block passes
+// them once.  group = 1 is A-major order (one A block against every B block), group >= tiles_a B-major order.
+// The map is a bijection of [0, tiles_a * tiles_b) for every group >= 1.
+__device__ __forceinline__ void tile_coords(int t, int tiles_a, int tiles_b, int group, int& ta, int& tb) {
+    const int g = group > 1 ? group : 1;
+    const int per = g * tiles_b;
+    const int k = t / per;
+    const int tl = t - k * per;
+    const int ga = min(g, tiles_a - k * g);
+    tb = tl / ga;
+    ta = k * g + tl % ga;
+}
 
 // hardware reciprocal (relative error ~2^-23); arguments here are clamped to normal numbers
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -217,7 +233,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
-    const int n_tiles = ((args.Mr + kBM - 1) / kBM) * tiles_b;
+    const int tiles_a = (args.Mr + kBM - 1) / kBM;
+    const int n_tiles = tiles_a * tiles_b;
     // the NG products of a tile run one after the other, product g over its own K: k-blocks [0, n_kb0) feed
     // accumulator 0, [n_kb0, n_kb) accumulator 1
     const int n_kb0 = (args.K + BK - 1) / BK;
@@ -257,7 +274,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             uint32_t armed_phase[C::kStages] = {};
             bool ok = true;
             for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
-                const int ta = t / tiles_b, tb = t % tiles_b;
+                int ta, tb;
+                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
                 for (int kb = 0; kb < n_kb; ++kb) {
                     if (!mbar_wait(&empty[stage], phase ^ 1u, args.err, 1)) { ok = false; break; }
                     mbar_arrive_expect_tx(&full[stage], C::kStageBytes);
@@ -331,7 +349,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
         int ab = 0;
         uint32_t aphase = 0;
         for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-            const int ta = t / tiles_b, tb = t % tiles_b;
+            int ta, tb;
+                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
             const int nvalid = min(kBN, args.Nr - tb * kBN);  // columns of this tile inside B
             const bool real_tile = NG == 2 && ta * kBM < args.n_real;  // uniform over the CTA
             __syncwarp();  // every lane is done with the previous tile's slot
@@ -421,7 +440,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
     const bool leader = rank == 0;
     const int cl = static_cast<int>(cluster_id_x()), n_cl = static_cast<int>(cluster_count_x());
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
-    const int n_tiles = ((args.Mr + kPairRows - 1) / kPairRows) * tiles_b;
+    const int tiles_a = (args.Mr + kPairRows - 1) / kPairRows;
+    const int n_tiles = tiles_a * tiles_b;
     const int n_kb0 = (args.K + C::kBK - 1) / C::kBK;
     const int n_kb = n_kb0 + (NG == 2 ? (args.K2 + C::kBK - 1) / C::kBK : 0);
     constexpr uint32_t idesc = idesc_f16_f32(kPairRows, kBN);
@@ -461,7 +481,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
             uint32_t armed_phase[C::kStages] = {};
             bool ok = true;
             for (int t = cl; t < n_tiles && ok; t += n_cl) {
-                const int ta = t / tiles_b, tb = t % tiles_b;
+                int ta, tb;
+                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
                 const int arow = ta * kPairRows + static_cast<int>(rank) * 128;
                 const int brow = tb * kBN + static_cast<int>(rank) * (kBN / 2);
                 for (int kb = 0; kb < n_kb; ++kb) {
@@ -546,7 +567,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
         int ab = 0;
         uint32_t aphase = 0;
         for (int t = cl; t < n_tiles; t += n_cl) {
-            const int ta = t / tiles_b, tb = t % tiles_b;
+            int ta, tb;
+                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
             const int nvalid = min(kBN, args.Nr - tb * kBN);
             const int row0 = ta * kPairRows + static_cast<int>(rank) * 128;
             const bool real_tile = NG == 2 && row0 < args.n_real;  // uniform over the CTA

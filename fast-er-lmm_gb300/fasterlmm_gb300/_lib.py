@@ -61,7 +61,12 @@ SIGNATURES: dict[str, list] = {
     "flmm_bed_decode": [_p, _i64, _i, _i, _p, _i, _i, _p, _i64, _p],
     "flmm_delta_features_f32": [_p, _i, _p, _i64, _i, _p, _p],
     "flmm_delta_mlp_f32": [_p, _i, _p, _p, _p, _p, _p, C.c_float, _d, _d, _p, _p],
-    "flmm_newton_from_proposal": [_p, _i, _p, _i64, _i, _p, _i, _p, _p, _p, _p, _p],
+    "flmm_fit_delta_learned_workspace_bytes": [_i, _i, _i, _psz],
+    "flmm_fit_delta_learned": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _p, _p, C.c_float, _i, _i, _p, _p, _p,
+                               _p, _sz, _p],
+    "flmm_mlp_grad_workspace_bytes": [_i, _psz],
+    "flmm_mlp_grad": [_p, _p, _i64, _i, _p, _p, _i, C.c_float, _i, _p, _p, _p, _sz, _p],
+    "flmm_mlp_adamw": [_p, _p, _p, _p, _i, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _p],
     "flmm_fit_delta_lowrank_f64": [_p, _i, _p, _i64, _p, _i, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
     "flmm_wald_lowrank_f64_workspace_bytes": [_i, _i, _i, _i, _psz],
     "flmm_wald_lowrank_f64": [_p, _i, _p, _i64, _p, _i64, _i, _i, _p, _i, _i, _p, _i64, _p, _i64, _i, _p, _p, _p, _p,

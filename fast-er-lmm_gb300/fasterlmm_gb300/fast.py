@@ -317,9 +317,13 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         s = _spectrum(evals[k_idx], D)
         Ut = Kp[k_idx, D:]
         Us = SplitRows.of(Ut)
+        slot = mark("rotate")
         gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
+        done(slot)
+        slot = mark("delta")
         ld, _ = _fit_delta(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
                                log_delta_max=log_delta_max, refine=refine)
+        done(slot)
         USt = torch.empty((n, ldk), dtype=F32, device=dev)
         gemm_split(ctx, Zs.view(a, n), Us.view(), USt[:, :Neff])
         wald_fast(ctx, ops, s, UYt[:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,

@@ -4,16 +4,17 @@ golden-section search).
 
 A small MLP (65 -> 128 -> 128 -> 1, tanh-GELU) maps cheap features of each rotated column -- the log energy
 fractions of UY^2 over 32 equal-count bins of the ascending spectrum, the log mean eigenvalue per bin, log Neff --
-to a proposed log delta.  The exact refinement then starts there: a proposal inside the FP32 grid argmin's basin
-splits it, the half holding the stationary point is confirmed by one derivative sign, and the fast fit's
-safeguarded Newton iteration runs in that half from the proposal; columns where that fails take the grid
-refinement unchanged (csrc/flmm_delta_learned.cu).  The proposal therefore changes how many evaluations a column
-needs, not the answer: results equal the grid path's to the Newton tolerance.
+to a proposed log delta.  The fit's grid search then collapses to a narrow bracket: each column evaluates the grid
+loss at the 2 HALF_WIDTH + 1 nodes nearest its proposal.  A window argmin on the window's edge sends the column to
+the full grid; a sampled audit (every AUDIT_STRIDE-th column evaluates the full grid) sends every column there if
+a node outside a window wins.  The exact Newton refinement then runs from the chosen node, as in the grid path
+(csrc/flmm_delta_learned.cu), so the proposal saves grid evaluations without moving the answer.
 
 The weights (``delta_mlp.npz`` beside this file) are produced by ``python -m fasterlmm_gb300.learned train`` on a
 GB300: seeded synthetic datasets (N from 300 to 2,000, 1 to 6 covariates, h2 uniform on [0, 0.95], 0 to 100 causal
-variants, each phenotype plus one permuted copy), labels from the exact fit on a 200-point grid, trained in BF16
-with FP32 master weights.
+variants, each phenotype plus one permuted copy), labels from the exact fit on a 200-point grid, trained by the
+library's own kernels (csrc/flmm_mlp_train.cu: minibatch gradient with BF16 operands and FP32 accumulation, AdamW
+on FP32 master weights).
 """
 
 from __future__ import annotations
@@ -72,34 +73,49 @@ def propose_t(feats: Tensor, model: DeltaMLP, lo: float, hi: float) -> Tensor:
     return x
 
 
+# Narrow bracket: grid nodes evaluated on each side of the proposal's nearest node, and the audit rate (every
+# AUDIT_STRIDE-th column also evaluates the full grid; a lost audit sends every column of the call to the full grid).
+HALF_WIDTH = 3
+AUDIT_STRIDE = 64
+
+
 def fit_delta_learned(s: Tensor, UYt: Tensor, *, n_grid: int = 64, log_delta_min: float = -10.0,
                       log_delta_max: float = 10.0, refine: bool = True, model: DeltaMLP | None = None,
-                      stats: dict | None = None) -> tuple[Tensor, Tensor]:
+                      stats: dict | None = None, half_width: int = HALF_WIDTH,
+                      audit_stride: int = AUDIT_STRIDE) -> tuple[Tensor, Tensor]:
     """
-    Fast delta fit with the learned proposal: (log_delta (P,), grid index (P,)), same contract as
-    fast.fit_delta_fast.  ``stats``, if given, receives the number of columns that fell back to the grid path.
+    Fast delta fit with the grid search collapsed to the proposal's bracket (flmm_fit_delta_learned):
+    (log_delta (P,), grid index (P,)), same contract as fast.fit_delta_fast.  ``stats``, if given, receives the
+    device counters (int32[4]: fallback columns, audited columns, audits lost, grid nodes evaluated by the window
+    and audit pass); see :func:`grid_evaluations` for the totals.
     """
     from .fast import fit_delta_fast
     dev = s.device
-    ld_grid, idx = fit_delta_fast(s, UYt, n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max,
-                                  refine=False)
-    if not refine or UYt.shape[1] < 32:
-        if refine:  # too few samples for the features: the grid refinement
-            return fit_delta_fast(s, UYt, n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max)
-        return ld_grid, idx
-    model = model or DeltaMLP.load(dev)
-    st = _stream(dev)
     P, Neff = UYt.shape
-    x = propose_t(features_t(s, UYt), model, log_delta_min, log_delta_max)
-    grid = torch.empty(n_grid, dtype=F64, device=dev)
-    _lib.call("flmm_delta_grid_nodes", float(log_delta_min), float(log_delta_max), n_grid, _ptr(grid), st)
+    if Neff < 32:  # too few samples for the features: the grid path
+        return fit_delta_fast(s, UYt, n_grid=n_grid, log_delta_min=log_delta_min, log_delta_max=log_delta_max,
+                              refine=refine)
+    model = model or DeltaMLP.load(dev)
     ld = torch.empty(P, dtype=F64, device=dev)
-    nfb = torch.zeros(1, dtype=torch.int32, device=dev)
-    _lib.call("flmm_newton_from_proposal", _ptr(s), Neff, _ptr(UYt), UYt.stride(0), P, _ptr(grid), n_grid, _ptr(idx),
-              _ptr(x), _ptr(ld), _ptr(nfb), st)
+    idx = torch.empty(P, dtype=torch.int32, device=dev)
+    cnt = torch.empty(4, dtype=torch.int32, device=dev)
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_fit_delta_learned_workspace_bytes", Neff, n_grid, P))
+    _lib.call("flmm_fit_delta_learned", _ptr(s), Neff, _ptr(UYt), UYt.stride(0), P, n_grid, float(log_delta_min),
+              float(log_delta_max), int(bool(refine)), _ptr(model.W1), _ptr(model.b1), _ptr(model.W2),
+              _ptr(model.b2), _ptr(model.w3), model.b3, int(half_width), int(audit_stride), _ptr(ld), _ptr(idx),
+              _ptr(cnt), w, wb, _stream(dev))
     if stats is not None:
-        stats["fallback"] = nfb
+        stats.update(counters=cnt, P=P, n_grid=n_grid)
     return ld, idx
+
+
+def grid_evaluations(stats: dict) -> dict:
+    """Host summary of a learned fit's counters: grid-node loss evaluations against the full grid's P * n_grid."""
+    fb, audited, lost, window = (int(v) for v in stats["counters"].cpu().tolist())
+    P, G = stats["P"], stats["n_grid"]
+    done = window + fb * G
+    return {"columns": P, "fallback": fb, "fallback_rate": fb / max(P, 1), "audited": audited, "audits_lost": lost,
+            "grid_evaluations": done, "full_grid_evaluations": P * G, "saved_fraction": 1.0 - done / max(P * G, 1)}
 
 
 # ---- training ------------------------------------------------------------------------------------------------
@@ -143,8 +159,82 @@ def make_training_set(n_sets: int, seed: int, dev: torch.device) -> tuple[np.nda
     return np.concatenate(feats), np.concatenate(labels)
 
 
+MLP_PARAMS = 25089  # FLMM_MLP_PARAMS: W1 (128, 65) | b1 (128) | W2 (128, 128) | b2 (128) | w3 (128) | b3
+_LAYOUT = (("W1", (128, N_FEATURES)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)), ("w3", (128,)), ("b3", ()))
+
+
+def init_params(seed: int) -> np.ndarray:
+    """Flat FP32 parameters, each layer U(-1/sqrt(fan_in), 1/sqrt(fan_in)) like a freshly made linear layer."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for name, shape in _LAYOUT:
+        fan_in = N_FEATURES if name in ("W1", "b1") else 128
+        bound = 1.0 / np.sqrt(fan_in)
+        parts.append(rng.uniform(-bound, bound, int(np.prod(shape))))
+    out = np.concatenate(parts).astype(np.float32)
+    assert out.size == MLP_PARAMS
+    return out
+
+
+def unpack_params(flat: np.ndarray) -> dict:
+    out, off = {}, 0
+    for name, shape in _LAYOUT:
+        n = int(np.prod(shape))
+        out[name] = np.asarray(flat[off:off + n], dtype=np.float32).reshape(shape)
+        off += n
+    return out
+
+
+def mlp_grad(params: Tensor, X: Tensor, y: Tensor, rows: Tensor, *, huber_beta: float = 0.1, bf16: bool = True,
+             grad: Tensor | None = None, loss: Tensor | None = None) -> tuple[Tensor, Tensor]:
+    """Gradient of the mean smooth-L1 loss over X[rows] on the device (flmm_mlp_grad): (grad, loss)."""
+    dev = params.device
+    batch = rows.numel()
+    grad = torch.empty(MLP_PARAMS, dtype=F32, device=dev) if grad is None else grad
+    loss = torch.empty(1, dtype=F32, device=dev) if loss is None else loss
+    w, wb = _work.get(dev, _lib.query_bytes("flmm_mlp_grad_workspace_bytes", batch))
+    _lib.call("flmm_mlp_grad", _ptr(params), _ptr(X), X.stride(0), X.shape[0], _ptr(y), _ptr(rows), batch,
+              float(huber_beta), int(bool(bf16)), _ptr(grad), _ptr(loss), w, wb, _stream(dev))
+    return grad, loss
+
+
+def fit_mlp(X: Tensor, y: Tensor, train_rows: np.ndarray, *, steps: int, batch: int = 2048, lr: float = 2e-3,
+            weight_decay: float = 1e-4, huber_beta: float = 0.1, seed: int = 0, bf16: bool = True) -> tuple:
+    """
+    Train the proposal MLP with the library's own kernels: per step a minibatch gradient (flmm_mlp_grad, BF16
+    operands, FP32 accumulation) and an AdamW step on the FP32 master weights (flmm_mlp_adamw), cosine-annealed
+    learning rate.  X (n, 65) FP32 features (already standardised), y (n,) FP32 labels on the device.
+    Returns (FP32 master parameters (MLP_PARAMS,) on the device, per-step minibatch losses as numpy).
+    """
+    dev = X.device
+    rng = np.random.default_rng(seed)
+    params = torch.from_numpy(init_params(seed)).to(dev)
+    m = torch.zeros_like(params)
+    v = torch.zeros_like(params)
+    grad = torch.empty_like(params)
+    losses = torch.empty(steps, dtype=F32, device=dev)
+    picks = rng.integers(0, len(train_rows), (steps, batch))
+    rows = torch.from_numpy(np.asarray(train_rows, dtype=np.int32)[picks]).to(dev)
+    st = _stream(dev)
+    for k in range(steps):
+        mlp_grad(params, X, y, rows[k], huber_beta=huber_beta, bf16=bf16, grad=grad, loss=losses[k:k + 1])
+        lr_k = lr * 0.5 * (1.0 + np.cos(np.pi * k / steps))
+        _lib.call("flmm_mlp_adamw", _ptr(params), _ptr(grad), _ptr(m), _ptr(v), k + 1, float(lr_k), 0.9, 0.999,
+                  1e-8, float(weight_decay), st)
+    return params, losses.cpu().numpy()
+
+
+def export_weights(params: Tensor, mu: np.ndarray, sd: np.ndarray) -> dict:
+    """Inference arrays for flmm_delta_mlp_f32, with the input standardisation (x - mu) / sd folded into layer 1."""
+    p = unpack_params(params.cpu().numpy())
+    W1 = p["W1"] / sd[None, :]
+    b1 = p["b1"] - W1 @ mu
+    return {"W1": W1.astype(np.float32), "b1": b1.astype(np.float32), "W2": p["W2"], "b2": p["b2"], "w3": p["w3"],
+            "b3": np.float32(p["b3"])}
+
+
 def train(out: Path, *, n_sets: int = 48, steps: int = 4000, seed: int = 20240601) -> dict:
-    """Train the proposal MLP (BF16 autocast, FP32 master weights) and write its weights to ``out``."""
+    """Train the proposal MLP on the device with the library's kernels and write its weights to ``out``."""
     dev = torch.device("cuda", torch.cuda.current_device())
     t0 = time.time()
     X, y = make_training_set(n_sets, seed, dev)
@@ -155,36 +245,22 @@ def train(out: Path, *, n_sets: int = 48, steps: int = 4000, seed: int = 2024060
     n_val = max(1, n // 10)
     val, tr = order[:n_val], order[n_val:]
     mu, sd = X[tr].mean(axis=0), X[tr].std(axis=0) + 1e-6
-    Xt = torch.from_numpy((X - mu) / sd).float().to(dev)
-    yt = torch.from_numpy(y).float().to(dev)
-    torch.manual_seed(seed)
-    net = torch.nn.Sequential(torch.nn.Linear(N_FEATURES, 128), torch.nn.GELU(approximate="tanh"),
-                              torch.nn.Linear(128, 128), torch.nn.GELU(approximate="tanh"),
-                              torch.nn.Linear(128, 1)).to(dev)
-    opt = torch.optim.AdamW(net.parameters(), lr=2e-3, weight_decay=1e-4)
-    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
-    tr_t = torch.from_numpy(tr).to(dev)
-    for step in range(steps):
-        b = tr_t[torch.randint(0, tr_t.numel(), (2048,), device=dev)]
-        with torch.autocast("cuda", dtype=torch.bfloat16):
-            pred = net(Xt[b]).squeeze(1)
-        loss = torch.nn.functional.smooth_l1_loss(pred.float(), yt[b], beta=0.1)
-        opt.zero_grad(set_to_none=True)
-        loss.backward()
-        opt.step()
-        sched.step()
-    with torch.no_grad():
-        pv = net(Xt[torch.from_numpy(val).to(dev)]).squeeze(1).float()
-        err = (pv - yt[torch.from_numpy(val).to(dev)]).abs().cpu().numpy()
-    W1 = net[0].weight.detach().float().cpu().numpy() / sd[None, :]  # fold the input standardisation into layer 1
-    b1 = net[0].bias.detach().float().cpu().numpy() - W1 @ mu
-    info = {"samples": int(n), "train_s": time.time() - t0, "data_s": t_data,
+    Xt = torch.from_numpy(((X - mu) / sd).astype(np.float32)).to(dev)
+    yt = torch.from_numpy(y.astype(np.float32)).to(dev)
+    t1 = time.time()
+    params, losses = fit_mlp(Xt, yt, tr, steps=steps, seed=seed)
+    torch.cuda.synchronize()
+    t_fit = time.time() - t1
+    arrays = export_weights(params, mu, sd)
+    model = DeltaMLP(arrays, dev)
+    feats_val = torch.from_numpy(X[val].astype(np.float32)).to(dev)
+    pv = propose_t(feats_val, model, -1e30, 1e30).cpu().numpy()
+    err = np.abs(pv - y[val])
+    info = {"samples": int(n), "train_s": time.time() - t0, "data_s": t_data, "fit_s": t_fit, "steps": steps,
+            "loss_first": float(losses[:50].mean()), "loss_last": float(losses[-50:].mean()),
             "val_abs_err_median": float(np.median(err)), "val_abs_err_p90": float(np.quantile(err, 0.9)),
-            "val_within_0.1": float((err < 0.1).mean())}
-    np.savez(out, W1=W1.astype(np.float32), b1=b1.astype(np.float32),
-             W2=net[2].weight.detach().float().cpu().numpy(), b2=net[2].bias.detach().float().cpu().numpy(),
-             w3=net[4].weight.detach().float().cpu().numpy()[0], b3=np.float32(net[4].bias.item()),
-             info=json.dumps(info))
+            "val_within_0.1": float((err < 0.1).mean()), "trainer": "flmm_mlp_grad + flmm_mlp_adamw (BF16 operands)"}
+    np.savez(out, **arrays, info=json.dumps(info))
     return info
 
 

@@ -115,6 +115,7 @@ int flmm_eigh_batched_f32_workspace_bytes(flmm_context* ctx, int N, int batch, s
 int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* evals, void* work, size_t work_bytes,
                           void* stream);
 
+
 /* One Ogita-Aishima refinement step for the FP32 decomposition of FP64 symmetric A (batch, N, N): U (batch, N, N)
  * FP32 eigenvector rows in, U_out refined rows out (U_out != U), evals (batch, N) FP64 Rayleigh quotients out.  A U
  * is formed in double-FP32 arithmetic; the corrections in FP32.  No counterpart in the reference (its eigh is
@@ -277,18 +278,44 @@ int flmm_bed_decode(const uint8_t* bed, int64_t bytes_per_variant, int n_variant
  * Features of each rotated column, feats (P, 65): log energy fractions of UY^2 over 32 equal-count bins of the
  * ascending spectrum s (Neff >= 32), log mean eigenvalue per bin, log(Neff) / 10.  The MLP 65 -> 128 -> 128 -> 1
  * (tanh-GELU; W1 (128, 65), W2 (128, 128) row-major, w3 (128,)) maps them to a proposed log delta, clamped to
- * [lo, hi].  flmm_newton_from_proposal then refines every column exactly: a proposal inside the FP32 grid argmin's
- * basin [grid[i-1], grid[i+1]] (grid_idx from flmm_fit_delta_fast with refine = 0) splits it, the half holding the
- * sign change of d loss / d log delta is confirmed and the fast fit's safeguarded Newton runs there from the
- * proposal; other columns take the fast fit's grid refinement and are counted in *n_fallback (device int,
- * add-only).  Results equal the grid path's to the Newton noise floor (~1e-7 in log delta). */
+ * [lo, hi]. */
 int flmm_delta_features_f32(const double* s, int Neff, const float* UYt, int64_t ldu, int P, float* feats,
                             void* stream);
 int flmm_delta_mlp_f32(const float* feats, int P, const float* W1, const float* b1, const float* W2, const float* b2,
                        const float* w3, float b3, double lo, double hi, double* x_out, void* stream);
-int flmm_newton_from_proposal(const double* s, int Neff, const float* UYt, int64_t ldu, int P, const double* grid,
-                              int n_grid, const int32_t* grid_idx, const double* x_prop, double* log_delta,
-                              int32_t* n_fallback, void* stream);
+
+/* The fast delta fit (flmm_fit_delta_fast; fasterlmm/core.py:561-595) with the grid search collapsed to a narrow
+ * bracket around the MLP's proposal: each column evaluates the FP32 grid loss at the 2 half_width + 1 nodes nearest
+ * its proposal.  A column whose window argmin is on the window's edge falls back to the full grid; every
+ * audit_stride-th column (0 = none) also evaluates the full grid, and if a node outside its window is lower, every
+ * column falls back.  The exact Newton refinement then runs from the chosen node, so results equal the grid path's
+ * wherever the loss has one minimum near the grid argmin.  stats (device int32[4], zeroed by the call): columns that
+ * fell back, audited columns, audits lost, grid nodes evaluated by the window and audit pass (the full-grid fallback
+ * adds n_grid per fallback column).  Workspace: flmm_fit_delta_learned_workspace_bytes. */
+int flmm_fit_delta_learned_workspace_bytes(int Neff, int n_grid, int P, size_t* bytes);
+int flmm_fit_delta_learned(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid, double lo,
+                           double hi, int refine, const float* W1, const float* b1, const float* W2, const float* b2,
+                           const float* w3, float b3, int half_width, int audit_stride, double* log_delta,
+                           int32_t* grid_idx, int32_t* stats, void* work, size_t work_bytes, void* stream);
+
+/* Training of the proposal MLP on the device (no counterpart in the reference).  The FP32 master parameters are one
+ * flat array of FLMM_MLP_PARAMS floats: W1 (128, 65) | b1 (128) | W2 (128, 128) | b2 (128) | w3 (128) | b3.
+ *
+ * flmm_mlp_grad: grad = d/dparams of the mean smooth-L1 loss (huber_beta) of the network's output against y[rows[r]]
+ * for the feature rows X[rows[r], :65], r < batch, of a feature matrix X (n_x, ldx) and labels y (n_x,); an index
+ * outside [0, n_x) contributes nothing.  bf16 != 0 rounds every matrix operand to BF16 (inputs, weights,
+ * activations, back-propagated gradients) with FP32 accumulation; bf16 == 0 keeps FP32 operands.  *loss (device
+ * float, may be NULL) receives the minibatch loss.  Deterministic: per-CTA partial gradients are added in a fixed
+ * order.  Workspace: flmm_mlp_grad_workspace_bytes(batch).
+ * flmm_mlp_adamw: one AdamW step (decoupled weight decay, bias correction for step >= 1) on the master parameters
+ * with moment arrays m, v (FLMM_MLP_PARAMS floats each, zero before step 1). */
+#define FLMM_MLP_PARAMS 25089
+int flmm_mlp_grad_workspace_bytes(int batch, size_t* bytes);
+int flmm_mlp_grad(const float* params, const float* X, int64_t ldx, int n_x, const float* y, const int32_t* rows,
+                  int batch, float huber_beta, int bf16, float* grad, float* loss, void* work, size_t work_bytes,
+                  void* stream);
+int flmm_mlp_adamw(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1, float beta2,
+                   float eps, float weight_decay, void* stream);
 
 /* ---- low-rank path (fasterlmm/lowrank.py): kinship factor G (N, k), k < N --------------------------------------
  *

@@ -221,29 +221,3 @@ def test_eigh_refinement_brings_fp32_eigenpairs_to_near_fp64():
     orth = (torch.bmm(U.double(), U.double().transpose(1, 2)) - torch.eye(N, device=DEV, dtype=torch.float64)).abs().max()
     assert orth.item() < 1e-5
 
-
-@pytest.mark.skipif(not __import__("pathlib").Path(__file__).resolve().parents[1].joinpath(
-    "fast-er-lmm_gb300", "fasterlmm_gb300", "delta_mlp.npz").exists(), reason="proposal weights not trained")
-def test_learned_delta_proposal_gives_the_grid_paths_answers(golden, monkeypatch):
-    """The learned proposal only changes where the refinement starts: same log delta (1e-6), parity goldens hold."""
-    from fasterlmm_gb300 import core, fast, learned, perms
-    from fasterlmm_gb300.synth import make_dataset
-    d = make_dataset(500, 4000, 1, 3, 200, seed=41, config_id=17, k_lo=0, k_hi=60, h2_lo=0.0, h2_hi=0.95)
-    Zs = orc.standardise_columns(d.Z_float())
-    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
-    spec = core.fastlmm_compat_rotate(t(orc.grm(Zs)), t(d.X), t(d.Y))
-    UYt = spec.UYt.float()
-    ld_grid, _ = fast.fit_delta_fast(spec.s, UYt)
-    stats = {}
-    ld, _ = learned.fit_delta_learned(spec.s, UYt, stats=stats)
-    # both are the FP32 Newton's stationary point, stopped at its noise floor: equal or loss-equivalent
-    s64, UY64 = spec.s.cpu().numpy(), spec.UYt.T.cpu().numpy()
-    assert_log_delta_equivalent(ld.cpu().numpy(), ld_grid.cpu().numpy(), s64, UY64, ld_atol=1e-6, loss_rtol=1e-10)
-    assert int(stats["fallback"].item()) < 0.9 * ld.numel()  # the proposal path is taken by a share of columns
-    monkeypatch.setattr(fast, "DELTA_PROPOSAL", "learned")
-    g = golden("loco_n150_m1500")
-    B = g["f"].shape[1]
-    res, pmf = perms.perm_threshold(_data(g["G"], g["X"], g["Y"], g["chrom"]), list(range(B)), n_perm=int(g["n_perm"]),
-                                    form="fast")
-    assert_scan_close(_np(res), g)
-    assert_scan_close({"perm_max_F": pmf.cpu().numpy()}, g, keys=("perm_max_F",))
