@@ -17,6 +17,7 @@
 
 #include "flmm_common.cuh"
 #include "flmm_delta_eval.cuh"
+#include "flmm_mlp.cuh"
 
 using namespace flmm;
 using namespace flmm::dfit;
@@ -26,10 +27,6 @@ namespace {
 constexpr int kBins = 32;
 constexpr int kIn = 2 * kBins + 1;
 constexpr int kHid = 128;
-
-__device__ __forceinline__ float gelu_tanh(float x) {
-    return 0.5f * x * (1.0f + tanhf(0.7978845608028654f * (x + 0.044715f * x * x * x)));
-}
 
 // Features of one column per warp: feats[p, b] = f_b, feats[p, 32 + b] = g_b, feats[p, 64] = log(Neff) / 10.
 __global__ void k_delta_features(const double* __restrict__ s, int Neff, const float* __restrict__ UYt, int64_t ldu,
@@ -53,47 +50,55 @@ __global__ void k_delta_features(const double* __restrict__ s, int Neff, const f
     if (lane == 0) f[2 * kBins] = logf(static_cast<float>(Neff)) * 0.1f;
 }
 
-// The MLP, one warp per column: lane j holds hidden units j, j + 32, j + 64, j + 96; x = clamp(out, lo, hi).
-__global__ void k_delta_mlp(const float* __restrict__ feats, int P, const float* __restrict__ W1,
-                            const float* __restrict__ b1, const float* __restrict__ W2, const float* __restrict__ b2,
-                            const float* __restrict__ w3, float b3, double lo, double hi, double* __restrict__ x_out) {
-    const int lane = threadIdx.x & 31;
-    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
-    if (p >= P) return;
-    const float* f = feats + p * kIn;
-    const float fb = f[lane], gb = f[kBins + lane], lgn = f[2 * kBins];
-    float h1[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) h1[k] = b1[lane + 32 * k];
-    for (int b = 0; b < kBins; ++b) {
-        const float xf = __shfl_sync(0xffffffffu, fb, b);
-        const float xg = __shfl_sync(0xffffffffu, gb, b);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float* w = W1 + (lane + 32 * k) * kIn;
-            h1[k] = fmaf(w[b], xf, h1[k]);
-            h1[k] = fmaf(w[kBins + b], xg, h1[k]);
+// The MLP over tiles of 16 columns: a persistent CTA holds both weight matrices in shared memory (thread j = hidden
+// unit j, the forward pass of flmm_mlp.cuh in FP32) and writes x = clamp(out, lo, hi).
+__global__ void __launch_bounds__(mlp::kMlpThreads)
+k_delta_mlp(const float* __restrict__ feats, int P, const float* __restrict__ W1, const float* __restrict__ b1,
+            const float* __restrict__ W2, const float* __restrict__ b2, const float* __restrict__ w3, float b3,
+            double lo, double hi, double* __restrict__ x_out) {
+    using namespace flmm::mlp;
+    extern __shared__ float sm[];
+    float* W1s = sm;
+    float* W2s = W1s + kHid * kIn;
+    float* xs = W2s + kHid * kLdW2;
+    float* a1s = xs + kMlpRows * kIn;
+    float* red = a1s + kMlpRows * kHid;
+    auto same = [](float v) { return v; };
+    load_weights(W1, W2, W1s, W2s, same);
+    const int j = threadIdx.x;
+    const float b1j = b1[j], b2j = b2[j], w3j = w3[j];
+    const int n_tiles = (P + kMlpRows - 1) / kMlpRows;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int r0 = tile * kMlpRows;
+        __syncthreads();  // the previous tile is done with xs, a1s and red (and the weights are in place)
+        for (int t = j; t < kMlpRows * kIn; t += kMlpThreads) {
+            const int r = t / kIn;
+            xs[t] = (r0 + r < P) ? feats[static_cast<int64_t>(r0 + r) * kIn + t % kIn] : 0.0f;
         }
+        __syncthreads();
+        float z1[kMlpRows], z2[kMlpRows], a2[kMlpRows];
+        forward_tile(W1s, W2s, xs, a1s, b1j, b2j, z1, z2, a2, same);
+        output_partials(w3j, a2, red);
+        __syncthreads();
+        if (j < kMlpRows && r0 + j < P) x_out[r0 + j] = fmin(fmax(static_cast<double>(row_output(red, j, b3)), lo), hi);
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) h1[k] = gelu_tanh(fmaf(W1[(lane + 32 * k) * kIn + 2 * kBins], lgn, h1[k]));
-    float h2[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) h2[k] = b2[lane + 32 * k];
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-        for (int src = 0; src < 32; ++src) {
-            const float x = __shfl_sync(0xffffffffu, h1[kk], src);
-            const int i = src + 32 * kk;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) h2[k] = fmaf(W2[(lane + 32 * k) * kHid + i], x, h2[k]);
-        }
-    }
-    float o = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) o = fmaf(w3[lane + 32 * k], gelu_tanh(h2[k]), o);
-    o = warp_sum(o) + b3;
-    if (lane == 0) x_out[p] = fmin(fmax(static_cast<double>(o), lo), hi);
+}
+
+constexpr size_t kMlpSmem =
+    sizeof(float) * (static_cast<size_t>(mlp::kHid) * mlp::kIn + static_cast<size_t>(mlp::kHid) * mlp::kLdW2 +
+                     mlp::kMlpRows * mlp::kIn + mlp::kMlpRows * mlp::kHid + 4 * mlp::kMlpRows);
+
+int launch_delta_mlp(const float* feats, int P, const float* W1, const float* b1, const float* W2, const float* b2,
+                     const float* w3, float b3, double lo, double hi, double* x_out, cudaStream_t st) {
+    FLMM_CUDA(cudaFuncSetAttribute(k_delta_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(kMlpSmem)));
+    int dev = 0, sms = 0;
+    FLMM_CUDA(cudaGetDevice(&dev));
+    FLMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int n_tiles = (P + mlp::kMlpRows - 1) / mlp::kMlpRows;
+    const int grid = n_tiles < 2 * sms ? n_tiles : 2 * sms;
+    k_delta_mlp<<<grid, mlp::kMlpThreads, kMlpSmem, st>>>(feats, P, W1, b1, W2, b2, w3, b3, lo, hi, x_out);
+    return check_launch("k_delta_mlp");
 }
 
 // Grid loss of one column at node g (the FP32 grid path's formula): Neff log(sum_n Wg[g, n] u_n^2) + sum_log[g]
@@ -181,9 +186,7 @@ extern "C" int flmm_delta_mlp_f32(const float* feats, int P, const float* W1, co
                                   void* stream) {
     FLMM_REQUIRE(feats && W1 && b1 && W2 && b2 && w3 && x_out && P >= 0, "flmm_delta_mlp_f32: bad arguments");
     if (P == 0) return FLMM_OK;
-    k_delta_mlp<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, as_stream(stream)>>>(feats, P, W1, b1, W2, b2,
-                                                                                            w3, b3, lo, hi, x_out);
-    return check_launch("k_delta_mlp");
+    return launch_delta_mlp(feats, P, W1, b1, W2, b2, w3, b3, lo, hi, x_out, as_stream(stream));
 }
 
 extern "C" int flmm_fit_delta_learned_workspace_bytes(int Neff, int n_grid, int P, size_t* bytes) {
@@ -221,8 +224,7 @@ extern "C" int flmm_fit_delta_learned(const double* s, int Neff, const float* UY
     const unsigned warps_grid = ceil_div(static_cast<int64_t>(P) * 32, 256);
     k_delta_features<<<warps_grid, 256, 0, st>>>(s, Neff, UYt, ldu, P, feats);
     if ((rc = check_launch("k_delta_features"))) return rc;
-    k_delta_mlp<<<warps_grid, 256, 0, st>>>(feats, P, W1, b1, W2, b2, w3, b3, lo, hi, x_prop);
-    if ((rc = check_launch("k_delta_mlp"))) return rc;
+    if ((rc = launch_delta_mlp(feats, P, W1, b1, W2, b2, w3, b3, lo, hi, x_prop, st))) return rc;
     k_delta_window<<<warps_grid, 256, 0, st>>>(w.Wg, w.sum_log, w.grid, n_grid, UYt, ldu, Neff, P, x_prop, half_width,
                                                audit_stride, grid_idx, fb_cols, stats);
     if ((rc = check_launch("k_delta_window"))) return rc;

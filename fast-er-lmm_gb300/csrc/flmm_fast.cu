@@ -18,6 +18,7 @@
 #include <cuda_fp16.h>
 #include <math.h>
 
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -936,7 +937,154 @@ bool use_pair_kernel() {
     return on;
 }
 
+// ---- kernel form and tile order: fixed, forced or autotuned ------------------------------------------------------
+//
+// Every split product (GEMM, NG = 1) and fused Wald launch (NG = 2) picks a kernel form (CTA pair or single CTA) and
+// a tile order (raster group, tile_coords).  Mode 0 uses the default (pair when the device can run pairs, A-major
+// order); mode 2 forces one choice; mode 1 (the default mode) autotunes: the first launch of each product shape
+// (NG, rows, columns, both reduction lengths) times every candidate on the caller's own operands with CUDA events on
+// the caller's stream and keeps the fastest for the rest of the process.  Every candidate computes each output with
+// the same products in the same K order, so all give bit-identical results and re-running one is harmless (the Wald
+// kernel overwrites its detail rows and takes a maximum into max_F).  A GEMM that accumulates into C is not re-run:
+// it takes the default.  Tuning synchronises the calling host thread on its events once per shape, and is skipped
+// while the stream is being captured into a graph.
+
+struct TcChoice {
+    bool pair;
+    int group;
+};
+
+struct TuneRecord {
+    int ng, mr, nr, k, k2;
+    TcChoice choice;
+    float ms, default_ms;
+};
+
+std::mutex g_tune_mu;
+int g_tune_mode = -1;  // -1: not read yet (FLMM_AUTOTUNE=0 in the environment starts in mode 0)
+TcChoice g_forced = {true, 1};
+TuneRecord g_tuned[256];
+int g_n_tuned = 0;
+
+constexpr int kGroups[] = {1, 2, 4, 8};
+
+int tune_mode_locked() {
+    if (g_tune_mode < 0) {
+        const char* e = std::getenv("FLMM_AUTOTUNE");
+        g_tune_mode = (e && e[0] == '0') ? 0 : 1;
+    }
+    return g_tune_mode;
+}
+
+template <int NG>
+int launch_choice(const TcMaps& maps_tc, const TcMaps& maps_pair, TcArgs a, TcChoice c, int n_cl, int sm_count,
+                  cudaStream_t st) {
+    a.group = c.group;
+    if (c.pair && n_cl > 0) return launch_pair<NG>(maps_pair, a, n_cl, st);
+    return launch_tc<NG, kBK>(maps_tc, a, sm_count, st);
+}
+
+template <int NG>
+int time_choice(const TcMaps& maps_tc, const TcMaps& maps_pair, const TcArgs& a, TcChoice c, int n_cl, int sm_count,
+                cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+    int rc = launch_choice<NG>(maps_tc, maps_pair, a, c, n_cl, sm_count, st);  // warm
+    if (rc) return rc;
+    FLMM_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < 2 && !rc; ++r) rc = launch_choice<NG>(maps_tc, maps_pair, a, c, n_cl, sm_count, st);
+    if (rc) return rc;
+    FLMM_CUDA(cudaEventRecord(e1, st));
+    FLMM_CUDA(cudaEventSynchronize(e1));
+    float t = 0.0f;
+    FLMM_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    *ms = 0.5f * t;
+    return FLMM_OK;
+}
+
+// Launch one split product with the configured choice (see above).  maps_pair holds the pair kernel's half-height B
+// maps; n_cl = 0 when the device cannot run the pair kernel.
+template <int NG>
+int launch_product(const TcMaps& maps_tc, const TcMaps& maps_pair, const TcArgs& a, int n_cl, int sm_count,
+                   bool rerunnable, cudaStream_t st) {
+    if (!use_pair_kernel()) n_cl = 0;  // FLMM_TC_PAIR=0: single-CTA kernels only
+    const TcChoice def = {n_cl > 0, 1};
+    TcChoice choice = def;
+    std::unique_lock<std::mutex> lock(g_tune_mu);
+    const int mode = tune_mode_locked();
+    if (mode == 2) {
+        choice = g_forced;
+    } else if (mode == 1 && rerunnable) {
+        bool found = false;
+        for (int i = 0; i < g_n_tuned; ++i) {
+            const TuneRecord& t = g_tuned[i];
+            if (t.ng == NG && t.mr == a.Mr && t.nr == a.Nr && t.k == a.K && t.k2 == a.K2) {
+                choice = t.choice;
+                found = true;
+                break;
+            }
+        }
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        FLMM_CUDA(cudaStreamIsCapturing(st, &cap));
+        if (!found && cap == cudaStreamCaptureStatusNone && g_n_tuned < 256) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            FLMM_CUDA(cudaEventCreate(&e0));
+            if (cudaEventCreate(&e1) != cudaSuccess) {
+                cudaEventDestroy(e0);
+                return fail(FLMM_ERR_CUDA, "autotune: cannot create events");
+            }
+            float best = 0.0f, def_ms = 0.0f;
+            bool have = false;
+            int rc = FLMM_OK;
+            for (int pi = 0; pi < 2 && !rc; ++pi) {
+                const bool pair = pi == 0;
+                if (pair && !(n_cl > 0)) continue;
+                for (int g : kGroups) {
+                    const TcChoice c = {pair, g};
+                    float ms = 0.0f;
+                    if ((rc = time_choice<NG>(maps_tc, maps_pair, a, c, n_cl, sm_count, st, e0, e1, &ms))) break;
+                    if (c.pair == def.pair && c.group == def.group) def_ms = ms;
+                    if (!have || ms < best) {
+                        best = ms;
+                        choice = c;
+                        have = true;
+                    }
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (rc) return rc;
+            g_tuned[g_n_tuned++] = {NG, a.Mr, a.Nr, a.K, a.K2, choice, best, def_ms};
+        }
+    }
+    lock.unlock();
+    return launch_choice<NG>(maps_tc, maps_pair, a, choice, n_cl, sm_count, st);
+}
+
 }  // namespace
+
+extern "C" int flmm_tc_config(int mode, int pair, int group) {
+    FLMM_REQUIRE(mode >= 0 && mode <= 2 && (mode != 2 || group >= 1),
+                 "flmm_tc_config: mode 0 (default), 1 (autotune) or 2 (forced pair / group >= 1)");
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_mode = mode;
+    g_forced = {pair != 0, group};
+    return FLMM_OK;
+}
+
+extern "C" int flmm_autotune_report(char* buf, size_t len, int* n_records) {
+    FLMM_REQUIRE(buf && len > 0 && n_records, "flmm_autotune_report: bad arguments");
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    size_t off = 0;
+    buf[0] = 0;
+    for (int i = 0; i < g_n_tuned && off < len; ++i) {
+        const TuneRecord& t = g_tuned[i];
+        const int w = std::snprintf(buf + off, len - off, "%d %d %d %d %d %d %d %.6f %.6f\n", t.ng, t.mr, t.nr, t.k,
+                                    t.k2, t.choice.pair ? 1 : 0, t.choice.group, t.ms, t.default_ms);
+        if (w < 0) break;
+        off += static_cast<size_t>(w);
+    }
+    *n_records = g_n_tuned;
+    return FLMM_OK;
+}
 
 // ---- C ABI -----------------------------------------------------------------------------------------------------
 
@@ -983,17 +1131,15 @@ extern "C" int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void
     a.C = Cout;
     a.ldc = ldc;
     a.accumulate = accumulate;
-    if (use_pair_kernel()) {
-        int dev = 0;
-        FLMM_CUDA(cudaGetDevice(&dev));
-        const int n_cl = pair_clusters<1>(dev);
-        if (n_cl > 0) {
-            if ((rc = make_map(&maps.m[2], Bh, Nr, K, ldb, kBK, kBN / 2))) return rc;
-            if ((rc = make_map(&maps.m[3], Bl, Nr, K, ldb, kBK, kBN / 2))) return rc;
-            return launch_pair<1>(maps, a, n_cl, as_stream(stream));
-        }
+    int dev = 0;
+    FLMM_CUDA(cudaGetDevice(&dev));
+    const int n_cl = pair_clusters<1>(dev);
+    TcMaps maps_pair = maps;  // the pair kernel loads 64 B rows per CTA: half-height B boxes
+    if (n_cl > 0) {
+        if ((rc = make_map(&maps_pair.m[2], Bh, Nr, K, ldb, kBK, kBN / 2))) return rc;
+        if ((rc = make_map(&maps_pair.m[3], Bl, Nr, K, ldb, kBK, kBN / 2))) return rc;
     }
-    return launch_tc<1, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+    return launch_product<1>(maps, maps_pair, a, n_cl, flmm_ctx_sm_count(ctx), accumulate == 0, as_stream(stream));
 }
 
 extern "C" int flmm_mean_f32(const double* x, int n, float* out, void* stream) {
@@ -1083,18 +1229,15 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sfve = sfve;
     a.ldo = ldo;
     a.max_F = max_F;
-    if (use_pair_kernel()) {
-        int dev = 0;
-        FLMM_CUDA(cudaGetDevice(&dev));
-        const int n_cl = pair_clusters<2>(dev);
-        if (n_cl > 0) {
-            // the pair kernel loads 64 B rows per CTA: variant-side maps with half-height boxes
-            if ((rc = make_map(&maps.m[2], B1h, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
-            if ((rc = make_map(&maps.m[3], B1l, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
-            if ((rc = make_map(&maps.m[6], Fh, Mc, R, ldf, kBK, kBN / 2))) return rc;
-            if ((rc = make_map(&maps.m[7], Fl, Mc, R, ldf, kBK, kBN / 2))) return rc;
-            return launch_pair<2>(maps, a, n_cl, as_stream(stream));
-        }
+    int dev = 0;
+    FLMM_CUDA(cudaGetDevice(&dev));
+    const int n_cl = pair_clusters<2>(dev);
+    TcMaps maps_pair = maps;  // the pair kernel loads 64 B rows per CTA: variant-side maps with half-height boxes
+    if (n_cl > 0) {
+        if ((rc = make_map(&maps_pair.m[2], B1h, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
+        if ((rc = make_map(&maps_pair.m[3], B1l, Mc, Neff, ldb, kBK, kBN / 2))) return rc;
+        if ((rc = make_map(&maps_pair.m[6], Fh, Mc, R, ldf, kBK, kBN / 2))) return rc;
+        if ((rc = make_map(&maps_pair.m[7], Fl, Mc, R, ldf, kBK, kBN / 2))) return rc;
     }
-    return launch_tc<2, kBK>(maps, a, flmm_ctx_sm_count(ctx), as_stream(stream));
+    return launch_product<2>(maps, maps_pair, a, n_cl, flmm_ctx_sm_count(ctx), true, as_stream(stream));
 }

@@ -17,16 +17,17 @@
 // partial gradient; a second kernel adds the partials in a fixed order (deterministic, no atomics).
 //
 // flmm_mlp_adamw: one AdamW step on the master weights (decoupled weight decay, bias-corrected moments).
-#include <cuda_bf16.h>
 #include <math.h>
 
 #include "flmm_common.cuh"
+#include "flmm_mlp.cuh"
 
 using namespace flmm;
+using namespace flmm::mlp;
 
 namespace {
 
-constexpr int kIn = 65, kHid = 128, kRows = 16, kThreads = 128;
+constexpr int kRows = kMlpRows, kThreads = kMlpThreads;
 constexpr int OFF_W1 = 0;
 constexpr int OFF_B1 = OFF_W1 + kHid * kIn;
 constexpr int OFF_W2 = OFF_B1 + kHid;
@@ -36,24 +37,10 @@ constexpr int OFF_B3 = OFF_W3 + kHid;
 constexpr int kParams = OFF_B3 + 1;
 static_assert(kParams == FLMM_MLP_PARAMS, "parameter layout");
 constexpr int kPartialLd = (kParams + 1 + 3) / 4 * 4;  // per-CTA partial: gradient, then the loss
-constexpr int LDW2 = kHid + 1;                         // padded rows: column reads by consecutive threads are conflict-free
+constexpr int LDW2 = kLdW2;
 
 constexpr size_t kSmemFloats = static_cast<size_t>(kHid) * kIn + static_cast<size_t>(kHid) * LDW2 + kRows * kIn +
                                3 * kRows * kHid + kRows + 4 * kRows;
-
-__device__ __forceinline__ float round_bf16(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-
-constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2 / pi)
-constexpr float kGeluA = 0.044715f;
-
-__device__ __forceinline__ float gelu_tanh(float x) {
-    return 0.5f * x * (1.0f + tanhf(kGeluC * (x + kGeluA * x * x * x)));
-}
-
-__device__ __forceinline__ float gelu_tanh_grad(float x) {
-    const float t = tanhf(kGeluC * (x + kGeluA * x * x * x));
-    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluC * (1.0f + 3.0f * kGeluA * x * x);
-}
 
 __global__ void __launch_bounds__(kThreads)
 k_mlp_rows(const float* __restrict__ params, const float* __restrict__ X, int64_t ldx, int n_x,
@@ -69,10 +56,9 @@ k_mlp_rows(const float* __restrict__ params, const float* __restrict__ X, int64_
     float* gos = dz1s + kRows * kHid;       // (kRows,) dloss/do
     float* red = gos + kRows;               // (4, kRows) per-warp partial outputs
 
-    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+    const int j = threadIdx.x;
     auto op = [bf16](float v) { return bf16 ? round_bf16(v) : v; };
-    for (int t = j; t < kHid * kIn; t += kThreads) W1s[t] = op(params[OFF_W1 + t]);
-    for (int t = j; t < kHid * kHid; t += kThreads) W2s[(t / kHid) * LDW2 + t % kHid] = op(params[OFF_W2 + t]);
+    load_weights(params + OFF_W1, params + OFF_W2, W1s, W2s, op);
     const float b1j = params[OFF_B1 + j], b2j = params[OFF_B2 + j], b3 = params[OFF_B3];
     const float w3j = op(params[OFF_W3 + j]);
     const int r0 = blockIdx.x * kRows;
@@ -84,45 +70,16 @@ k_mlp_rows(const float* __restrict__ params, const float* __restrict__ X, int64_
     }
     __syncthreads();
 
-    // layer 1 (unit j over the CTA's rows)
-    float z1[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) z1[r] = b1j;
-    for (int k = 0; k < kIn; ++k) {
-        const float w = W1s[j * kIn + k];
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) z1[r] = fmaf(w, xs[r * kIn + k], z1[r]);
-    }
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) a1s[r * kHid + j] = op(gelu_tanh(z1[r]));
-    __syncthreads();
-
-    // layer 2
-    float z2[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) z2[r] = b2j;
-    for (int i = 0; i < kHid; ++i) {
-        const float w = W2s[j * LDW2 + i];
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) z2[r] = fmaf(w, a1s[r * kHid + i], z2[r]);
-    }
-    float a2[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) a2[r] = op(gelu_tanh(z2[r]));
-
-    // output and loss gradient per row (fixed-order reduction over the four warps)
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-        const float v = warp_sum(w3j * a2[r]);
-        if (lane == 0) red[warp * kRows + r] = v;
-    }
+    float z1[kRows], z2[kRows], a2[kRows];
+    forward_tile(W1s, W2s, xs, a1s, b1j, b2j, z1, z2, a2, op);
+    output_partials(w3j, a2, red);
     __syncthreads();
     float loss = 0.0f;
     if (j < kRows) {
         float g = 0.0f;
         const int row = (j < nr) ? rows[r0 + j] : -1;
         if (row >= 0 && row < n_x) {  // an index outside the feature matrix contributes nothing
-            const float o = ((red[j] + red[kRows + j]) + (red[2 * kRows + j] + red[3 * kRows + j])) + b3;
+            const float o = row_output(red, j, b3);
             const float d = o - y[row];
             const float ad = fabsf(d);
             const float inv_b = 1.0f / static_cast<float>(batch);

@@ -90,8 +90,11 @@ SIGNATURES: dict[str, list] = {
     "flmm_write_column_tsv": [_s, _s, _p, _i64],
     "flmm_fill_rows_host_f64": [_p, _i64, _i64, _p, _i64, _i],
     "flmm_context_check": [_p, _p],
+    "flmm_host_device_pointer": [_p, C.POINTER(_p)],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],
+    "flmm_tc_config": [_i, _i, _i],
+    "flmm_autotune_report": [_p, _sz, C.POINTER(C.c_int)],
     "flmm_fit_delta_fast_workspace_bytes": [_i, _i, _psz],
     "flmm_fit_delta_fast": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p, _sz, _p],
     "flmm_fit_delta_fast_noalloc": [_p, _i, _p, _i64, _i, _i, _d, _d, _i, _p, _p, _p],
@@ -168,6 +171,32 @@ def context(device: int) -> C.c_void_p:
                 raise FlmmError("flmm_context_create", rc, h.flmm_last_error().decode(errors="replace"))
             _contexts[device] = ctx
         return ctx
+
+
+def tc_config(mode: int, pair: int = 1, group: int = 1) -> None:
+    """Kernel form / tile order of the split products: 0 defaults, 1 autotune, 2 forced (pair, group)."""
+    call("flmm_tc_config", int(mode), int(pair), int(group))
+
+
+def autotune_report() -> list[dict]:
+    """Shapes tuned so far in this process, with the chosen kernel form and tile order and their times."""
+    buf = C.create_string_buffer(1 << 16)
+    n = C.c_int(0)
+    call("flmm_autotune_report", C.cast(buf, C.c_void_p), len(buf), C.byref(n))
+    out = []
+    for line in buf.value.decode().splitlines():
+        ng, mr, nr, k, k2, pair, group, ms, dms = line.split()
+        out.append({"kernel": "wald" if ng == "2" else "gemm", "rows": int(mr), "cols": int(nr), "K": int(k),
+                    "K2": int(k2), "pair": bool(int(pair)), "group": int(group), "ms": float(ms),
+                    "default_ms": float(dms)})
+    return out
+
+
+def host_device_pointer(host_ptr: int) -> int | None:
+    """Device address of mapped page-locked host memory, or None if the memory is not such."""
+    out = C.c_void_p()
+    rc = lib().flmm_host_device_pointer(C.c_void_p(host_ptr), C.byref(out))
+    return out.value if rc == 0 else None
 
 
 def kernel_launches() -> int:

@@ -197,6 +197,10 @@ int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double* out, void*
  * Split operands need 16-byte aligned base pointers and a row pitch (in elements) that is a multiple of 8.  These
  * kernels use bounded device-side waits; flmm_context_check reports a wait that gave up. */
 
+/* Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister, mapped), for kernels that write
+ * their results straight into host memory; FLMM_ERR_ARG for pageable or unknown memory.  Host-only query. */
+int flmm_host_device_pointer(const void* host, void** dev_ptr);
+
 /* Synchronise `stream` and return FLMM_ERR_TIMEOUT (clearing the flag) if a kernel of this context gave up a
  * bounded wait since the last check. */
 int flmm_context_check(flmm_context* ctx, void* stream);
@@ -211,6 +215,17 @@ int flmm_split_rows_f16(const void* X, int x_is_f64, int64_t ldx, int rows, int 
 int flmm_gemm_split_f16(flmm_context* ctx, const void* Ah, const void* Al, const float* sa, int64_t lda, int Mr,
                         const void* Bh, const void* Bl, const float* sb, int64_t ldb, int Nr, int K, float* C,
                         int64_t ldc, int accumulate, void* stream);
+
+/* Kernel form and tile order of the split products (flmm_gemm_split_f16, flmm_wald_split_f16); no counterpart in the
+ * reference.  mode 0: defaults (CTA pairs where the device runs them, A-major tile order); mode 1 (the initial mode,
+ * unless FLMM_AUTOTUNE=0 is set in the environment): the first launch of each product shape times every candidate
+ * (pair or single CTA x tile-order groups 1, 2, 4, 8) on the caller's operands and stream, synchronising the calling
+ * thread once, and keeps the fastest for the process; not while the stream is being captured, and not for a GEMM
+ * that accumulates into C; mode 2: force `pair` (0/1) and `group` (>= 1).  All choices give bit-identical results.
+ * flmm_autotune_report writes one line per tuned shape into buf (host memory): "NG rows cols K K2 pair group ms
+ * default_ms", and the number of shapes into *n_records. */
+int flmm_tc_config(int mode, int pair, int group);
+int flmm_autotune_report(char* buf, size_t len, int* n_records);
 
 /* Fast delta fit (fasterlmm/core.py:561-595): FP32 grid argmin, then the stationary point of the loss in the
  * reference's bracket [grid[i-1], grid[i+1]] by a sign-safeguarded Newton iteration on d loss / d log delta with

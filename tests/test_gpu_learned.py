@@ -93,8 +93,10 @@ def test_adamw_step_matches_the_oracle():
     po, mo_, vo = mo.adamw_step(p.astype(np.float32).astype(np.float64), g.astype(np.float32).astype(np.float64),
                                 m.astype(np.float32).astype(np.float64), v.astype(np.float32).astype(np.float64), 7,
                                 lr=1e-3, weight_decay=1e-4)
-    # FP32 update against FP64: a few FP32 roundings per element
-    np.testing.assert_allclose(tp.cpu().numpy(), po, rtol=1e-5, atol=1e-8)
+    # FP32 update against FP64: a few FP32 roundings of the weight and of the step (which can nearly cancel it)
+    p32 = p.astype(np.float32).astype(np.float64)
+    err = np.abs(tp.cpu().numpy() - po)
+    assert np.all(err <= 1e-6 * np.abs(po) + 2e-5 * np.abs(po - p32) + 1e-12), err.max()
     np.testing.assert_allclose(tm.cpu().numpy(), mo_, rtol=1e-5, atol=1e-11)
     np.testing.assert_allclose(tv.cpu().numpy(), vo, rtol=1e-5, atol=1e-13)
 
