@@ -122,21 +122,6 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
 int flmm_ctx_sm_count(flmm_context* ctx) { return ctx->sm_count; }
 int* flmm_ctx_err_flag(flmm_context* ctx) { return ctx->err_flag; }
 
-extern "C" int flmm_host_device_pointer(const void* host, void** dev_ptr) {
-    FLMM_REQUIRE(host && dev_ptr, "flmm_host_device_pointer: NULL argument");
-    *dev_ptr = nullptr;
-    cudaPointerAttributes attr;
-    if (cudaPointerGetAttributes(&attr, host) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(FLMM_ERR_ARG, "flmm_host_device_pointer: %p is not known to the CUDA runtime", host);
-    }
-    if (attr.type != cudaMemoryTypeHost || !attr.devicePointer)
-        return fail(FLMM_ERR_ARG, "flmm_host_device_pointer: %p is not page-locked host memory mapped for the device",
-                    host);
-    *dev_ptr = attr.devicePointer;
-    return FLMM_OK;
-}
-
 extern "C" int flmm_context_check(flmm_context* ctx, void* stream) {
     FLMM_REQUIRE(ctx, "flmm_context_check: NULL context");
     int h = 0;

@@ -90,7 +90,6 @@ SIGNATURES: dict[str, list] = {
     "flmm_write_column_tsv": [_s, _s, _p, _i64],
     "flmm_fill_rows_host_f64": [_p, _i64, _i64, _p, _i64, _i],
     "flmm_context_check": [_p, _p],
-    "flmm_host_device_pointer": [_p, C.POINTER(_p)],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],
     "flmm_tc_config": [_i, _i, _i],
@@ -190,13 +189,6 @@ def autotune_report() -> list[dict]:
                     "K2": int(k2), "pair": bool(int(pair)), "group": int(group), "ms": float(ms),
                     "default_ms": float(dms)})
     return out
-
-
-def host_device_pointer(host_ptr: int) -> int | None:
-    """Device address of mapped page-locked host memory, or None if the memory is not such."""
-    out = C.c_void_p()
-    rc = lib().flmm_host_device_pointer(C.c_void_p(host_ptr), C.byref(out))
-    return out.value if rc == 0 else None
 
 
 def kernel_launches() -> int:

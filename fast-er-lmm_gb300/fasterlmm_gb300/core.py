@@ -328,14 +328,11 @@ def wald_t(s: Tensor, UYt: Tensor, log_delta: Tensor, USt: Tensor, n_real: int, 
     _lib.call("flmm_fill_nullh2", _ptr(log_delta), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, _stream(dev))
 
 
-def _alloc_outputs(M: int, n_real: int, P: int, dev: torch.device, zero: bool = False,
-                   skip=()) -> tuple[dict, Tensor]:
+def _alloc_outputs(M: int, n_real: int, P: int, dev: torch.device, zero: bool = False) -> tuple[dict, Tensor]:
     """(M, n_real) detail outputs and max_F (P,) = -inf.  The scans write every detail element, so the detail is left
-    uninitialised unless ``zero`` (callers whose variant blocks may not cover all M rows); keys in ``skip`` are not
-    allocated (the caller supplies them)."""
+    uninitialised unless ``zero`` (callers whose variant blocks may not cover all M rows)."""
     alloc = torch.zeros if zero else torch.empty
-    out = {k: alloc((M, n_real), dtype=F64, device=dev) for k in ("f", "beta", "se", "sfve", "nullh2")
-           if k not in skip}
+    out = {k: alloc((M, n_real), dtype=F64, device=dev) for k in ("f", "beta", "se", "sfve", "nullh2")}
     max_F = torch.empty(P, dtype=F64, device=dev)
     _lib.call("flmm_fill_f64", _ptr(max_F), P, float("-inf"), _stream(dev))
     return out, max_F

@@ -43,9 +43,6 @@ EIGH_REFINE_STEPS = 2
 # Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
 # fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
 DELTA_PROPOSAL = "grid"
-# With pinned host result tensors (scan_t's host_out), the fused Wald kernel writes f, beta, se and sfve straight into
-# them through their device mapping, instead of into device buffers copied out chromosome by chromosome.
-HOST_DIRECT = True
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -281,9 +278,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
             ev.record()
             slot[1] = ev
 
-    direct = _host_direct_targets(host_out, M, n_real)
-    out, max_F = _alloc_outputs(M, n_real, P, dev, skip=direct)
-    out.update(direct)
+    out, max_F = _alloc_outputs(M, n_real, P, dev)
     basis = CovariateBasis(X)
     Ys = SplitRows.of(basis.regress_out(Yt))
     order, blocks = _chrom_order(chrom)
@@ -291,9 +286,7 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     if host_nullh2:
         del out["nullh2"]  # filled in host memory, chromosome by chromosome
         nullh2_row = torch.zeros(1, dtype=torch.int64, device=dev)
-    sink = None
-    if host_out is not None:
-        sink = _RowSink(out, {k: v for k, v in host_out.items() if k not in direct}, dev, host_nullh2)
+    sink = _RowSink(out, host_out, dev, host_nullh2) if host_out is not None else None
     order_t = None if order is None else torch.from_numpy(order).to(dev)
     Zs = SplitRows.of(Zt if order_t is None else Zt.index_select(0, order_t))
     row_map = torch.arange(M, dtype=torch.int64, device=dev) if order_t is None else order_t.to(torch.int64)
@@ -348,20 +341,6 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     if sink is not None:
         return sink.finish(max_F, log_deltas)
     return ScanResult(max_F=max_F, log_delta=log_deltas, **out)
-
-
-def _host_direct_targets(host_out: dict | None, M: int, n_real: int) -> dict:
-    """The detail tensors of host_out that the Wald kernel can write directly: all of f, beta, se, sfve as pinned,
-    contiguous FP64 (M, n_real) host tensors whose device mapping is their own address (else none of them)."""
-    keys = ("f", "beta", "se", "sfve")
-    if not HOST_DIRECT or host_out is None or n_real == 0:
-        return {}
-    for k in keys:
-        h = host_out.get(k)
-        if (h is None or h.is_cuda or h.dtype != F64 or tuple(h.shape) != (M, n_real) or not h.is_contiguous() or
-                not h.is_pinned() or _lib.host_device_pointer(h.data_ptr()) != h.data_ptr()):
-            return {}
-    return {k: host_out[k] for k in keys}
 
 
 def _eigh_batched_f32(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:

@@ -197,10 +197,6 @@ int flmm_neglog10_pvalue(const double* F, int64_t n, int df2, double* out, void*
  * Split operands need 16-byte aligned base pointers and a row pitch (in elements) that is a multiple of 8.  These
  * kernels use bounded device-side waits; flmm_context_check reports a wait that gave up. */
 
-/* Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister, mapped), for kernels that write
- * their results straight into host memory; FLMM_ERR_ARG for pageable or unknown memory.  Host-only query. */
-int flmm_host_device_pointer(const void* host, void** dev_ptr);
-
 /* Synchronise `stream` and return FLMM_ERR_TIMEOUT (clearing the flag) if a kernel of this context gave up a
  * bounded wait since the last check. */
 int flmm_context_check(flmm_context* ctx, void* stream);
