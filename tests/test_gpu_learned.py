@@ -97,7 +97,9 @@ def test_adamw_step_matches_the_oracle():
     p32 = p.astype(np.float32).astype(np.float64)
     err = np.abs(tp.cpu().numpy() - po)
     assert np.all(err <= 1e-6 * np.abs(po) + 2e-5 * np.abs(po - p32) + 1e-12), err.max()
-    np.testing.assert_allclose(tm.cpu().numpy(), mo_, rtol=1e-5, atol=1e-11)
+    # m = beta1 m + (1 - beta1) g can nearly cancel: bound its error by the terms' magnitudes
+    m32, g32 = m.astype(np.float32).astype(np.float64), g.astype(np.float32).astype(np.float64)
+    assert np.all(np.abs(tm.cpu().numpy() - mo_) <= 1e-6 * (0.9 * np.abs(m32) + 0.1 * np.abs(g32)))
     np.testing.assert_allclose(tv.cpu().numpy(), vo, rtol=1e-5, atol=1e-13)
 
 
