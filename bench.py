@@ -206,6 +206,8 @@ def run_ours(args):
     build()
     if args.delta is not None:
         fast.DELTA_PROPOSAL = args.delta
+    if args.no_pipeline:
+        fast.PIPELINE = False
     d, w = make_inputs(args.B, args.M)
     N, M, B, n_perm = w["N"], w["M"], w["B"], w["n_perm"]
     P = B * (1 + n_perm)
@@ -299,7 +301,7 @@ def run_ours(args):
             "data": "synthetic (seeded: Binomial(2, MAF~U[0.01,0.5]) genotypes, RINT phenotypes, 0-50 causal)",
             "config": {"workload": WORKLOAD, "N": N, "M": M, "B": B, "n_perm": n_perm, "P": P, "chromosomes": w["n_chrom"],
                        "covariates": w["D"], "grid": w["n_grid"], "form": args.form,
-                       "delta_fit": fast.DELTA_PROPOSAL,
+                       "delta_fit": fast.DELTA_PROPOSAL, "pipelined_delta_fit": bool(fast.PIPELINE),
                        "l2": "inputs larger than L2 (Z 0.8 GB FP64, operands >100 MB per chromosome)",
                        "parallelism": f"{world} replica(s), no cross-GPU exchange"},
             "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "rotation_roofline": rotation,
@@ -366,6 +368,8 @@ def main():
     ap.add_argument("--M", type=int, default=None, help="override the variant count (quick runs)")
     ap.add_argument("--delta", choices=["grid", "learned"], default=None,
                     help="fast form's delta fit: full FP32 grid, or the learned proposal's narrow bracket")
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="run each chromosome's delta fit on the main stream instead of one chromosome ahead")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

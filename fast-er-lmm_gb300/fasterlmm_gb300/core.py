@@ -99,6 +99,7 @@ class _Work:
         if b is None or b.numel() < nbytes:
             b = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8, device=dev)
             self.buf[dev] = b
+        b.record_stream(torch.cuda.current_stream(dev))  # freed only after every stream that used it is done
         return C.c_void_p(b.data_ptr()), b.numel()
 
 

@@ -43,6 +43,8 @@ EIGH_REFINE_STEPS = 2
 # Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
 # fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
 DELTA_PROPOSAL = "grid"
+# Run each chromosome's column side (UY rotation, delta fit) on a side stream one chromosome ahead of the Wald scan.
+PIPELINE = True
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -312,22 +314,52 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     else:
         evals = eigh_batched(Kp, mode=EIGH_MODE)
     done(slot)
-    UYt = torch.empty((P, ldk), dtype=F32, device=dev)
+    # Column side of chromosome k (its spectrum, eigenvector split, UY rotation and delta fit) runs on a side stream
+    # one chromosome ahead of the variant side (US rotation, Wald operand prep, fused Wald) on the main stream, so
+    # the delta fit's FP32 work shares the SMs with the tensor-core Wald kernel of the previous chromosome.  Two UY
+    # buffers alternate; the side stream reuses one only after the main stream's Wald prep has read it.
+    main = torch.cuda.current_stream(dev)
+    side = torch.cuda.Stream(device=dev) if PIPELINE else main
+    UY_bufs = [torch.empty((P, ldk), dtype=F32, device=dev) for _ in range(2 if PIPELINE else 1)]
+    buf_free = [None] * len(UY_bufs)
+    start = torch.cuda.Event()
+    start.record(main)
+    side.wait_event(start)
+
+    def column_side(k_idx: int):
+        with torch.cuda.stream(side):
+            s_k = _spectrum(evals[k_idx], D)
+            Us = SplitRows.of(Kp[k_idx, D:])
+            b = k_idx % len(UY_bufs)
+            if buf_free[b] is not None:
+                side.wait_event(buf_free[b])
+            UYt = UY_bufs[b][:, :Neff]
+            slot = mark("rotate")
+            gemm_split(ctx, Ys.view(), Us.view(), UYt)
+            done(slot)
+            slot = mark("delta")
+            ld_k, _ = _fit_delta(s_k, UYt, n_grid=n_grid, log_delta_min=log_delta_min,
+                                 log_delta_max=log_delta_max, refine=refine)
+            done(slot)
+            ready = torch.cuda.Event()
+            ready.record(side)
+        return s_k, Us, b, ld_k, ready
+
+    ahead = column_side(0) if units else None
     for k_idx, (c, a, n) in enumerate(units):
-        s = _spectrum(evals[k_idx], D)
-        Ut = Kp[k_idx, D:]
-        Us = SplitRows.of(Ut)
-        slot = mark("rotate")
-        gemm_split(ctx, Ys.view(), Us.view(), UYt[:, :Neff])
-        done(slot)
-        slot = mark("delta")
-        ld, _ = _fit_delta(s, UYt[:, :Neff], n_grid=n_grid, log_delta_min=log_delta_min,
-                               log_delta_max=log_delta_max, refine=refine)
-        done(slot)
+        s, Us, b, ld, ready = ahead
+        if k_idx + 1 < len(units):
+            ahead = column_side(k_idx + 1)
+        main.wait_event(ready)
+        if side is not main:  # made on the side stream, used on the main stream
+            for t in (s, ld, Us.hi, Us.lo, Us.scale):
+                t.record_stream(main)
         USt = torch.empty((n, ldk), dtype=F32, device=dev)
         gemm_split(ctx, Zs.view(a, n), Us.view(), USt[:, :Neff])
-        wald_fast(ctx, ops, s, UYt[:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,
+        wald_fast(ctx, ops, s, UY_bufs[b][:, :Neff], ld, USt[:, :Neff], n_real, row_map[a:a + n], out, max_F,
                   log_delta_min=log_delta_min, log_delta_max=log_delta_max, mark=mark, done=done)
+        buf_free[b] = torch.cuda.Event()
+        buf_free[b].record(main)
         log_deltas[c if c is not None else 0] = ld
         if sink is not None:
             sink.push(order, a, n)

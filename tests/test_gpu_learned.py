@@ -90,9 +90,11 @@ def test_adamw_step_matches_the_oracle():
     tp, tg, tm, tv = t(p), t(g), t(m), t(v)
     _lib.call("flmm_mlp_adamw", tp.data_ptr(), tg.data_ptr(), tm.data_ptr(), tv.data_ptr(), 7, 1e-3, 0.9, 0.999, 1e-8,
               1e-4, torch.cuda.current_stream().cuda_stream)
+    f32 = lambda x: float(np.float32(x))  # the kernel receives its hyperparameters as FP32 values
     po, mo_, vo = mo.adamw_step(p.astype(np.float32).astype(np.float64), g.astype(np.float32).astype(np.float64),
                                 m.astype(np.float32).astype(np.float64), v.astype(np.float32).astype(np.float64), 7,
-                                lr=1e-3, weight_decay=1e-4)
+                                lr=f32(1e-3), beta1=f32(0.9), beta2=f32(0.999), eps=f32(1e-8),
+                                weight_decay=f32(1e-4))
     # FP32 update against FP64: a few FP32 roundings of the weight and of the step (which can nearly cancel it)
     p32 = p.astype(np.float32).astype(np.float64)
     err = np.abs(tp.cpu().numpy() - po)
