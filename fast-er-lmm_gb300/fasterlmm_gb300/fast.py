@@ -322,6 +322,11 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
     side = torch.cuda.Stream(device=dev) if PIPELINE else main
     UY_bufs = [torch.empty((P, ldk), dtype=F32, device=dev) for _ in range(2 if PIPELINE else 1)]
     buf_free = [None] * len(UY_bufs)
+    # made on the main stream and read on the side stream: their memory is not reused before the side stream's work
+    # is done, also when an error ends the scan early
+    if side is not main:
+        for t in (*UY_bufs, Kp, evals, Ys.hi, Ys.lo, Ys.scale):
+            t.record_stream(side)
     start = torch.cuda.Event()
     start.record(main)
     side.wait_event(start)
