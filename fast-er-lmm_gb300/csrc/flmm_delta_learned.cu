@@ -6,7 +6,7 @@
 //   log(Neff) / 10,
 // 65 inputs -> 128 -> 128 -> 1 with tanh-GELU.  The proposal collapses the fit's grid search to a narrow bracket:
 // each column evaluates the FP32 grid loss only at the 2 h + 1 grid nodes nearest its proposal and takes their
-// argmin.  The full grid stays both the fallback and the judge:
+// argmin.  The full grid stays both the fallback and the check on the proposal:
 //   * a column whose window argmin sits on the window's edge (the minimum may lie outside it) is put on a list whose
 //     columns then get the full grid argmin;
 //   * every audit_stride-th column also evaluates the full grid; if a node outside the window beats the window's
