@@ -79,3 +79,28 @@ def test_host_row_fill(built):
         assert not dst[:10].any() and not dst[10 + rows:].any() and not dst[:, 64:].any()
     with pytest.raises(_lib.FlmmError):
         _lib.call("flmm_fill_rows_host_f64", None, 70, 10, None, 64, 1)
+
+
+def test_new_entry_points_validate_arguments_without_gpu(built):
+    """The training, learned-fit and autotuner entry points reject bad arguments on the host."""
+    from fasterlmm_gb300 import _lib
+    size = ctypes.c_size_t(0)
+    _lib.call("flmm_mlp_grad_workspace_bytes", 2048, ctypes.byref(size))
+    assert size.value == 4 * 25092 * 128  # one padded partial gradient per 16-row CTA
+    with pytest.raises(_lib.FlmmError) as e:  # no parameters / features
+        _lib.call("flmm_mlp_grad", None, None, 65, 10, None, None, 16, 0.1, 1, None, None, None, 0, None)
+    assert e.value.status == 1
+    with pytest.raises(_lib.FlmmError):  # AdamW steps count from 1
+        _lib.call("flmm_mlp_adamw", 8, 8, 8, 8, 0, 1e-3, 0.9, 0.999, 1e-8, 0.0, None)
+    with pytest.raises(_lib.FlmmError, match="Neff must be >= 32"):
+        p = 256
+        _lib.call("flmm_fit_delta_learned", p, 16, p, 16, 10, 64, -10.0, 10.0, 1, p, p, p, p, p, 0.0, 3, 64, p, p, p,
+                  p, 1 << 20, None)
+    _lib.call("flmm_fit_delta_learned_workspace_bytes", 995, 64, 71324, ctypes.byref(size))
+    assert size.value >= 4 * 71324 * 65 + 8 * 71324 + 4 * 71324
+    with pytest.raises(_lib.FlmmError):
+        _lib.call("flmm_tc_config", 3, 1, 1)
+    with pytest.raises(_lib.FlmmError):
+        _lib.call("flmm_tc_config", 2, 1, 0)  # a forced tile order needs group >= 1
+    _lib.tc_config(1)
+    assert isinstance(_lib.autotune_report(), list)
