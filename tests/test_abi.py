@@ -104,3 +104,18 @@ def test_new_entry_points_validate_arguments_without_gpu(built):
         _lib.call("flmm_tc_config", 2, 1, 0)  # a forced tile order needs group >= 1
     _lib.tc_config(1)
     assert isinstance(_lib.autotune_report(), list)
+
+
+def test_dropin_raises_the_references_value_error_before_any_device_work():
+    """A lone Z_kin or chrom_kin is a ValueError, as in the reference (fasterlmm/core.py:694-695), with or without GPU."""
+    import numpy as np
+    import torch
+    from fasterlmm_gb300 import core, gls
+    Z, X, Y = torch.zeros(6, 4, dtype=torch.float64), torch.ones(6, 1, dtype=torch.float64), torch.zeros(6, 2,
+                                                                                                        dtype=torch.float64)
+    chrom = np.array([1, 1, 2, 2])
+    for fn in (core.loco_scan_compat, gls.loco_scan):
+        with pytest.raises(ValueError, match="go together"):
+            fn(Z, X, Y, chrom, Z_kin=Z)
+        with pytest.raises(ValueError, match="go together"):
+            fn(Z, X, Y, chrom, chrom_kin=chrom)
