@@ -840,7 +840,7 @@ int encode_fn(PFN_cuTensorMapEncodeTiled_v12000* out) {
 
 // FP16 matrix (rows, K) with row pitch ld elements -> tiled map with box {BK, box_rows} and the matching swizzle.
 int make_map(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK, int box_rows = 128) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
     int rc = encode_fn(&enc);
     if (rc) return rc;
     if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (ld * 2) % 16 != 0)
