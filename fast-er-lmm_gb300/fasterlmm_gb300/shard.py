@@ -10,7 +10,6 @@ the scan, over any torch.distributed backend: gloo for host tensors, NCCL for de
 
 from __future__ import annotations
 
-import numpy as np
 import torch
 
 from .core import ScanResult

@@ -10,7 +10,6 @@ import socket
 import sys
 from pathlib import Path
 
-import numpy as np
 import pytest
 import torch
 import torch.multiprocessing as mp
