@@ -2,8 +2,8 @@
 The reference's own structural tests of the compat scan, restated against the CPU oracle (CPU only): the drop-D
 shapes of the compat spectrum (reference tests/test_core_compat.py:87-114), the UY identity (:129-142), grid-node
 landing without refinement (:174-186), max_F as the column maximum of F (:214-223), nullh2 = 1 / (1 + delta)
-(:228), the n_real split (:261-282), and a refined fit never worse than its grid node (tests/test_core_plain.py:
-114-127, here for the compat loss).
+(:228), the n_real split (:261-282), a refined fit never worse than its grid node (tests/test_core_plain.py:
+114-127, here for the compat loss), and the permutation seeding rules (tests/test_perms.py:26-36, 98-141).
 """
 from __future__ import annotations
 
@@ -67,3 +67,39 @@ def test_max_f_nullh2_and_n_real_split(case):
     for k in ("f", "beta", "se", "sfve", "nullh2"):
         np.testing.assert_array_equal(part[k], full[k][:, :2])
     np.testing.assert_array_equal(part["max_F"], full["max_F"])  # max_F covers every column
+
+
+@pytest.fixture(scope="module")
+def perm_case():
+    d = make_dataset(60, 240, 3, 2, 5, seed=21, config_id=6, k_lo=1, k_hi=4)
+    return d.Z_float(), d.X, d.Y, d.chrom
+
+
+def _pt(case, cols, **kw):
+    Z, X, Y, chrom = case
+    return orc.perm_threshold(Z, X, Y, chrom, cols, **kw)
+
+
+def test_permutation_seeding_like_the_reference(perm_case):
+    """Reference tests/test_perms.py:26-36, 98-141: same seed identical, other seed differs, a phenotype keeps its
+    permutation null when batched, reordered or scanned as a subset seeded with its full-table column."""
+    r0, p0 = _pt(perm_case, [0, 1], n_perm=4)
+    _, p1 = _pt(perm_case, [0, 1], n_perm=4)
+    np.testing.assert_array_equal(p0, p1)
+    _, p_other = _pt(perm_case, [0, 1], n_perm=4, seed=7)
+    assert not np.array_equal(p0, p_other)
+    # batching stability (same rounding tolerance as the reference's own test)
+    r_solo, p_solo = _pt(perm_case, [0], n_perm=4)
+    np.testing.assert_allclose(p0[0], p_solo[0], rtol=1e-7, atol=1e-9)
+    np.testing.assert_allclose(r0["f"][:, 0], r_solo["f"][:, 0], rtol=1e-7, atol=1e-9)
+    # order independence: rows follow the requested order, each phenotype keeps its own permutations
+    _, p10 = _pt(perm_case, [1, 0], n_perm=4)
+    np.testing.assert_allclose(p10[0], p0[1], rtol=1e-7, atol=1e-9)
+    np.testing.assert_allclose(p10[1], p0[0], rtol=1e-7, atol=1e-9)
+    # seed_idx: a one-column subset seeded with its full-table column gets the same permutations
+    Z, X, Y, chrom = perm_case
+    _, p_plain = orc.perm_threshold(Z, X, Y, chrom, [3], n_perm=3)
+    _, p_sub = orc.perm_threshold(Z, X, Y[:, [3]], chrom, [0], n_perm=3, seed_idx=[3])
+    _, p_unseeded = orc.perm_threshold(Z, X, Y[:, [3]], chrom, [0], n_perm=3)
+    np.testing.assert_allclose(p_sub, p_plain, rtol=1e-7, atol=1e-9)
+    assert not np.allclose(p_unseeded, p_plain)
