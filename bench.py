@@ -7,11 +7,15 @@ Metric: variant-phenotype tests per second, tests = M variants x B phenotypes x 
 phenotypes x 10 permutations (71,324 scan columns), 5 covariate columns, seeded synthetic inputs.
 
 One step = one full permutation scan of that workload through fasterlmm_gb300.perms.perm_threshold: standardise,
-per-chromosome kinship Grams, 20 x (projection, FP64 eigendecomposition, rotations, delta fit, fused Wald scan),
-permutation orders drawn per step.  ``value`` times steps with the inputs already on the device; ``e2e`` times the
-same call with host (pinned) inputs and host outputs, copies included.
+per-chromosome kinship Grams, the batched eigendecomposition of the 20 LOCO kinships, then 20 x (rotations, delta
+fit, fused Wald scan), permutation orders drawn per step.  ``value`` times steps with the inputs already on the
+device; ``e2e`` times the same call with host (pinned) inputs and host outputs, copies included.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast|plain] [--impl ours|reference]
+                  [--delta grid|learned] [--no-pipeline] [--B B] [--M M] [--no-e2e] [--no-cpu-baseline]
+
+``--delta learned`` switches the fast form's delta fit to the learned proposal's narrow bracket; ``--no-pipeline``
+runs each chromosome's delta fit on the main stream instead of one chromosome ahead on a side stream.
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm (oracle/flmm_oracle.py) on the host's
 cores on a bounded sample of the same workload (one chromosome x one 256-phenotype batch per step).
