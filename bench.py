@@ -13,6 +13,12 @@ device; ``e2e`` times the same call with host (pinned) inputs and host outputs, 
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast|plain] [--impl ours|reference]
                   [--delta grid|learned] [--no-pipeline] [--B B] [--M M] [--no-e2e] [--no-cpu-baseline]
+                  [--no-plain] [--plain-chroms C]
+
+Besides ``value`` and ``e2e`` the line carries the metric's own ratio (``chosen_vs_plain``: the plain FP64 form and
+the chosen form timed on the same bounded subset of the workload, its first C chromosomes), the real-only rate,
+the fused Wald kernel's roofline on the tensor pipe and in HBM bytes, the delta fit's FP32 roofline and per-stage
+times of one step with nothing overlapped.
 
 ``--delta learned`` switches the fast form's delta fit to the learned proposal's narrow bracket; ``--no-pipeline``
 runs each chromosome's delta fit on the main stream instead of one chromosome ahead on a side stream.
@@ -185,6 +191,25 @@ def run_reference(args):
         tests.append(n)
     value = sum(tests) / sum(times)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    iso = isolated_stages(args, step, w) if (args.form == "fast" and rank == 0) else None
+    delta_roof = None
+    if iso and iso.get("delta"):
+        # per chromosome: the FP32 grid product (G x Neff) x (Neff x P), 2 flop per term, and the Newton passes,
+        # ~30 FP32 operations per element for each of ~4.5 evaluations of a column
+        d_s = iso["delta"] / w["n_chrom"] / 1e3
+        grid_flop = 2.0 * w["n_grid"] * Neff * P
+        newton_flop = 30.0 * 4.5 * Neff * P
+        fp32_peak = fp32_peak_tflops()
+        delta_roof = {"kernels": "k_grid_argmin_f32 + k_newton_refine (FP32 pipe)", "ms_per_chromosome": 1e3 * d_s,
+                      "algorithmic_flop": grid_flop + newton_flop, "grid_flop": grid_flop,
+                      "achieved_tflops": (grid_flop + newton_flop) / d_s / 1e12, "peak_tflops": fp32_peak,
+                      "frac": (grid_flop + newton_flop) / d_s / 1e12 / fp32_peak,
+                      "peak_source": "nominal FP32 CUDA-core rate: SMs x 128 lanes x 2 flop x max SM clock",
+                      "timed": "one untimed step with the delta fit on the main stream (not overlapped)"}
+    plain = None
+    if rank == 0 and world == 1 and args.form == "fast" and not args.no_plain:
+        plain = plain_comparison(args, d, w, grid_kw)
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
@@ -279,11 +304,20 @@ def run_ours(args):
             for line in tp.read_text().splitlines():
                 if line.startswith("traffic_bytes_per_launch:"):
                     traffic = int(line.split(":")[1])
+        # algorithmic HBM bytes of one launch: the split FP16 hi/lo operands read once (columns: w~ o UY over Neff
+        # and the Lagrange weights over R; variants: US over Neff and the sWs node table over R) and the FP64
+        # detail of the real columns (f, beta, se, sfve) written once
+        ldk, ldr = -(-Neff // 8) * 8, -(-R // 8) * 8
+        alg_bytes = 4.0 * P * (ldk + ldr) + 4.0 * mc_mean * (ldk + ldr) + 32.0 * mc_mean * B
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": "k_pair<2> (fused split-FP16 Wald, tcgen05 CTA pairs)", "launch_ms": 1e3 * mean_s,
                 "algorithmic_flop_per_launch": alg_flop, "executed_flop_per_launch": exec_flop,
                 "executed_tensor_frac": exec_flop / mean_s / 1e12 / peak,
-                "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)"}
+                "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)",
+                "hbm": {"algorithmic_bytes_per_launch": alg_bytes, "achieved_gbs": alg_bytes / mean_s / 1e9,
+                        "measured_gbs": None if traffic is None else traffic / mean_s / 1e9,
+                        "peak_gbs": peaks["hbm_gbs"], "frac": alg_bytes / mean_s / 1e9 / peaks["hbm_gbs"],
+                        "note": "fused: ~1e3 flop per HBM byte, so the tensor pipe binds, not HBM"}}
 
     # the phenotype rotation UY = U_eff^T Y_r per chromosome (split-FP16 tcgen05 GEMM): 2 N Neff P algorithmic flop
     rot_ms = [a.elapsed_time(b) for a, b in timers.get("rotate", []) if b is not None]
@@ -298,6 +332,25 @@ def run_ours(args):
     stages = {k: round(sum(a.elapsed_time(b) for a, b in v if b is not None) / args.steps, 3)
               for k, v in timers.items()}
 
+    iso = isolated_stages(args, step, w) if (args.form == "fast" and rank == 0) else None
+    delta_roof = None
+    if iso and iso.get("delta"):
+        # per chromosome: the FP32 grid product (G x Neff) x (Neff x P), 2 flop per term, and the Newton passes,
+        # ~30 FP32 operations per element for each of ~4.5 evaluations of a column
+        d_s = iso["delta"] / w["n_chrom"] / 1e3
+        grid_flop = 2.0 * w["n_grid"] * Neff * P
+        newton_flop = 30.0 * 4.5 * Neff * P
+        fp32_peak = fp32_peak_tflops()
+        delta_roof = {"kernels": "k_grid_argmin_f32 + k_newton_refine (FP32 pipe)", "ms_per_chromosome": 1e3 * d_s,
+                      "algorithmic_flop": grid_flop + newton_flop, "grid_flop": grid_flop,
+                      "achieved_tflops": (grid_flop + newton_flop) / d_s / 1e12, "peak_tflops": fp32_peak,
+                      "frac": (grid_flop + newton_flop) / d_s / 1e12 / fp32_peak,
+                      "peak_source": "nominal FP32 CUDA-core rate: SMs x 128 lanes x 2 flop x max SM clock",
+                      "timed": "one untimed step with the delta fit on the main stream (not overlapped)"}
+    plain = None
+    if rank == 0 and world == 1 and args.form == "fast" and not args.no_plain:
+        plain = plain_comparison(args, d, w, grid_kw)
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -308,8 +361,10 @@ def run_ours(args):
                        "delta_fit": fast.DELTA_PROPOSAL, "pipelined_delta_fit": bool(fast.PIPELINE),
                        "l2": "inputs larger than L2 (Z 0.8 GB FP64, operands >100 MB per chromosome)",
                        "parallelism": f"{world} replica(s), no cross-GPU exchange"},
+            "real_tests_per_s": value * B / P,
             "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "rotation_roofline": rotation,
-            "stage_ms_per_step": stages, "autotune": _lib.autotune_report(), "clocks": clk}
+            "delta_roofline": delta_roof, "chosen_vs_plain": plain,
+            "stage_ms_per_step": stages, "stage_ms_isolated": iso, "autotune": _lib.autotune_report(), "clocks": clk}
 
     data_dev = None  # the e2e leg starts from host data only
     if host_bufs is not None:
@@ -321,6 +376,64 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def fp32_peak_tflops() -> float:
+    import torch
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    mhz = 2070.0
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        mhz = float(json.loads(p.read_text()).get("sm_max_mhz") or mhz)
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def isolated_stages(args, step, w) -> dict:
+    """Stage times of one untimed step with every stage on the main stream (nothing overlapped), CUDA events."""
+    import torch
+    from fasterlmm_gb300 import fast
+    saved = fast.PIPELINE
+    fast.PIPELINE = False
+    tm: dict = {}
+    try:
+        step(tm)
+        torch.cuda.synchronize()
+    finally:
+        fast.PIPELINE = saved
+    return {k: round(sum(a.elapsed_time(b) for a, b in v if b is not None), 3) for k, v in tm.items()}
+
+
+def plain_comparison(args, d, w, grid_kw) -> dict:
+    """
+    The metric's denominator: the plain FP64 form (FP64 kernels, FP64 eigendecomposition, the reference's golden
+    section) and the chosen form on the same bounded subset of the workload -- its first ``--plain-chroms``
+    chromosomes with every phenotype and permutation -- device-resident inputs, CUDA events, one warm-up step each.
+    """
+    import torch
+    from fasterlmm_gb300 import perms
+    keep = np.isin(d.chrom, sorted(np.unique(d.chrom))[: args.plain_chroms])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    sub = SimpleNamespace(Z=t(d.Z_float()[:, keep]), Y=t(d.Y), X=t(d.X), chrom=d.chrom[keep], Z_kin=None,
+                          chrom_kin=None)
+    B, n_perm = w["B"], w["n_perm"]
+    tests = int(keep.sum()) * B * (1 + n_perm)
+    out = {"subset": f"{args.plain_chroms} of {w['n_chrom']} chromosomes ({int(keep.sum())} variants), all {B} "
+                     f"phenotypes x {n_perm} permutations, LOCO within the subset"}
+    for form, reps in (("plain", 1), ("fast", 3)):
+        perms.perm_threshold(sub, list(range(B)), n_perm=n_perm, form=form, **grid_kw)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            res, pmf = perms.perm_threshold(sub, list(range(B)), n_perm=n_perm, form=form, **grid_kw)
+            del res, pmf
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3 / reps
+        out[form] = {"ms_per_step": 1e3 * sec, "tests_per_s": tests / sec}
+    out["ratio"] = out["fast"]["tests_per_s"] / out["plain"]["tests_per_s"]
+    return out
 
 
 def e2e_buffers(d, w):
@@ -376,6 +489,10 @@ def main():
                     help="run each chromosome's delta fit on the main stream instead of one chromosome ahead")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 form's bounded run (the denominator of the chosen-vs-plain ratio)")
+    ap.add_argument("--plain-chroms", type=int, default=2,
+                    help="chromosomes of the workload that the plain-form comparison scans (default 2 of 20)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

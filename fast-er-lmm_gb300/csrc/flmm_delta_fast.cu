@@ -300,7 +300,8 @@ extern "C" int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, 
 // call overwrites every byte it reads before reading it, so nothing has to start at zero.  Calls whose kernels
 // overlap on the GPU (other streams, other host threads) race on the array: serialise them.
 
-constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;  // 4 MiB: n_grid * Neff up to ~1.04 million
+// 4 MiB: fits every call with fast_ws(Neff, n_grid) <= 4 MiB (n_grid * Neff a little under 2^20)
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
 static __device__ __align__(256) unsigned char g_fit_scratch[kNoAllocScratchBytes];
 
 namespace {
@@ -310,7 +311,9 @@ std::mutex g_scratch_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_fit_scratch on the current device, looked up once per device.  In host code the array's name
-// is only a host-side stand-in, so the address must come from the runtime.
+// is only a host-side stand-in, so the address must come from the runtime.  The kept address belongs to the primary
+// context the first call saw: it does not survive cudaDeviceReset (which reloads the module) and is wrong in a
+// non-primary driver context, so the entry point is documented as not usable there.
 int scratch_address(void** out) {
     int dev = 0;
     FLMM_CUDA(cudaGetDevice(&dev));

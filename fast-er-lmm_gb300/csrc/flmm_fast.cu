@@ -81,6 +81,13 @@ struct TcArgs {
     double* sfve;
     int64_t ldo;
     double* max_F;
+    // FP64-accurate re-evaluation of strong real tests: a real test whose F exceeds f_refine is listed as
+    // (variant index in the chromosome, column) in flags[*flag_count] (up to flag_cap entries) and left out of
+    // max_F, which the re-evaluation (flmm_wald_refine_f32) then updates; flag_count == nullptr turns this off
+    float f_refine;
+    int* flag_count;
+    int2* flags;
+    int flag_cap;
     // tile order of the persistent schedule (see tile_coords); 0 or 1 = A-major
     int group;
 };
@@ -110,7 +117,8 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // [cbeg, cbeg + 64) (variants), TMEM address tl of product 0 for this thread's lane quarter (product 1 lies kBN
 // columns further), the warp's staged scales sc1 / sc2 and output rows rws.
 __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p, bool real_tile, int nvalid,
-                                          int cbeg, const float* sc1, const float* sc2, const int64_t* rws) {
+                                          int cbeg, int mbase, const float* sc1, const float* sc2,
+                                          const int64_t* rws) {
     // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each test needs
     // two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
     //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
@@ -155,7 +163,14 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p
             const float rss = fmaxf(rwr - qv, 1e-30f);
             const bool var_ok = sws > 0.0f;
             const float F = var_ok ? qv * df * rcp_approx(rss) : 0.0f;
-            colmax = fmaxf(colmax, F);
+            bool listed = false;
+            if (real && F > args.f_refine && args.flag_count != nullptr) {
+                // FP32 cancellation in rss grows with F: the re-evaluation recomputes this test and its max
+                const int slot = atomicAdd(args.flag_count, 1);
+                if (slot < args.flag_cap) args.flags[slot] = make_int2(mbase + c0 + j, p);
+                listed = true;  // also when the list is full: the re-evaluation then scans the chromosome
+            }
+            if (!listed) colmax = fmaxf(colmax, F);
             col_nan |= (F != F);
             if (!real) continue;
             const int64_t o = rws[c0 - cbeg + j] * args.ldo + p;
@@ -373,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             if constexpr (NG == 1) {
                 gemm_rows(args, tl, i, tb * kBN, nvalid, cbeg, sc1);
             } else {
-                wald_rows(args, tl, i, real_tile, nvalid, cbeg, sc1, sc2, rws);
+                wald_rows(args, tl, i, real_tile, nvalid, cbeg, tb * kBN, sc1, sc2, rws);
             }
             fence_before_sync();
             mbar_arrive(&acc_empty[ab]);
@@ -592,7 +607,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
             if constexpr (NG == 1)
                 gemm_rows(args, tl, row0 + r, tb * kBN, nvalid, cbeg, sc1);
             else
-                wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, sc1, sc2, rws);
+                wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, tb * kBN, sc1, sc2, rws);
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive_cluster(acc_empty0 + static_cast<uint32_t>(ab * 8));
@@ -980,6 +995,8 @@ template <int NG>
 int launch_choice(const TcMaps& maps_tc, const TcMaps& maps_pair, TcArgs a, TcChoice c, int n_cl, int sm_count,
                   cudaStream_t st) {
     a.group = c.group;
+    // every launch starts a fresh list of strong real tests (autotuning may run the Wald kernel several times)
+    if (NG == 2 && a.flag_count != nullptr) FLMM_CUDA(cudaMemsetAsync(a.flag_count, 0, sizeof(int), st));
     if (c.pair && n_cl > 0) return launch_pair<NG>(maps_pair, a, n_cl, st);
     return launch_tc<NG, kBK>(maps_tc, a, sm_count, st);
 }
@@ -1187,13 +1204,17 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
                                    const float* rWr0, int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1,
                                    const void* Fh, const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff,
                                    int R, const int64_t* rows, double* f, double* beta, double* se, double* sfve,
-                                   int64_t ldo, double* max_F, void* stream) {
+                                   int64_t ldo, double* max_F, float f_refine, int32_t* flag_count,
+                                   int32_t* flags, int flag_cap, void* stream) {
     FLMM_REQUIRE(ctx && A1h && A1l && sa1 && Lh && Ll && sl && rWr && rWr0 && B1h && B1l && sb1 && Fh && Fl && sf && max_F &&
                      Neff > 1 && R > 0 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
                      ldb >= Neff && ldl >= R && ldf >= R,
                  "flmm_wald_split_f16: bad arguments");
     FLMM_REQUIRE(n_real == 0 || Mc == 0 || (rows && f && beta && se && sfve && ldo >= n_real),
                  "flmm_wald_split_f16: real-column outputs missing");
+    FLMM_REQUIRE(flag_count == nullptr || (flag_cap >= 0 && (flags != nullptr || flag_cap == 0)),
+                 "flmm_wald_split_f16: strong-test list without storage");
+    if (flag_count != nullptr) FLMM_CUDA(cudaMemsetAsync(flag_count, 0, sizeof(int32_t), as_stream(stream)));
     if (P == 0 || Mc == 0) return FLMM_OK;
     TcMaps maps;
     std::memset(&maps, 0, sizeof(maps));
@@ -1229,6 +1250,10 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.sfve = sfve;
     a.ldo = ldo;
     a.max_F = max_F;
+    a.f_refine = f_refine;
+    a.flag_count = flag_count;
+    a.flags = reinterpret_cast<int2*>(flags);
+    a.flag_cap = flag_cap;
     int dev = 0;
     FLMM_CUDA(cudaGetDevice(&dev));
     const int n_cl = pair_clusters<2>(dev);

@@ -103,7 +103,9 @@ SIGNATURES: dict[str, list] = {
                                      _p, _p, _p],
     "flmm_wald_split_prep_variants": [_p, _i64, _i, _i, _p, _p, _p, _p, _i64, _p, _p, _p],
     "flmm_wald_split_f16": [_p, _p, _p, _i64, _p, _p, _p, _i64, _p, _p, _p, _i, _i, _p, _p, _i64, _p, _p, _p, _i64, _p,
-                            _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, _p],
+                            _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, C.c_float, _p, _p, _i, _p],
+    "flmm_wald_refine_f32": [_p, _p, _p, _i, C.c_float, _p, _i64, _p, _i64, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p,
+                             _i64, _p, _p],
     "flmm_convert_f64_f32": [_i64, _p, _p, _p],
     "flmm_accumulate_f32_f64": [_i64, _p, _p, _p],
     "flmm_loco_kinship_f32": [_p, _p, _i, _d, _p, _p],

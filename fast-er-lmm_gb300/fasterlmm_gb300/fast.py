@@ -45,6 +45,12 @@ EIGH_REFINE_STEPS = 2
 DELTA_PROPOSAL = "grid"
 # Run each chromosome's column side (UY rotation, delta fit) on a side stream one chromosome ahead of the Wald scan.
 PIPELINE = True
+# Real tests whose FP32 F exceeds this are recomputed without the cancelling rss = rWr - sWy^2 / sWs subtraction
+# (flmm_wald_refine_f32): the FP32 form's -log10 p error grows like F^2 / df, about 1e-5 at F = 30 and N = 1,000.
+# None turns the re-evaluation off.  REFINE_CAP bounds the list of such tests per chromosome (8 bytes each); a
+# chromosome with more is recomputed by scanning its stored F.
+REFINE_F = 30.0
+REFINE_CAP = 1 << 22
 
 
 def _pad(k: int, m: int = 8) -> int:
@@ -188,6 +194,13 @@ class WaldOperands:
         self.dev = dev
         self.cols = None
         self.vars = None
+        self.flags = None
+        self.flag_count = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def _flags(self, n: int) -> Tensor:
+        if self.flags is None or self.flags.shape[0] < n:
+            self.flags = torch.empty((max(n, 1), 2), dtype=torch.int32, device=self.dev)
+        return self.flags
 
     def _cols(self, P: int, ldk: int, ldr: int):
         c = self.cols
@@ -238,13 +251,24 @@ def wald_fast(ctx, ops: WaldOperands, s: Tensor, UYt: Tensor, ld: Tensor, USt: T
     us2 = SplitView(ops, (_ptr(B2h), _ptr(B2l), _ptr(sb2), ldk, Mc, Neff))
     gemm_split(ctx, us2, Ws.view(), F[:, :R])
     Fs = SplitRows.of(F[:, :R])
+    refine = REFINE_F is not None and n_real > 0 and Mc > 0
+    cap = min(Mc * n_real, REFINE_CAP) if refine else 0
+    flags = ops._flags(cap) if refine else None
     slot = mark("wald") if mark else None
     _lib.call("flmm_wald_split_f16", ctx, _ptr(A1h), _ptr(A1l), ldk, _ptr(sa1), _ptr(Lh), _ptr(Ll), ldr, _ptr(sl),
               _ptr(rWr), _ptr(rWr0), P, n_real, _ptr(B1h), _ptr(B1l), ldk, _ptr(sb1), _ptr(Fs.hi), _ptr(Fs.lo), Fs.ld,
               _ptr(Fs.scale), Mc, Neff, R, _ptr(rows), _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]),
-              _ptr(out["sfve"]), n_real, _ptr(max_F), st)
+              _ptr(out["sfve"]), n_real, _ptr(max_F), float(REFINE_F if refine else float("inf")),
+              _ptr(ops.flag_count) if refine else None, _ptr(flags) if refine else None, cap, st)
     if done:
         done(slot)
+    if refine:
+        slot = mark("refine") if mark else None
+        _lib.call("flmm_wald_refine_f32", ctx, _ptr(flags), _ptr(ops.flag_count), cap, float(REFINE_F), _ptr(USt),
+                  USt.stride(0), _ptr(UYt), UYt.stride(0), _ptr(s32), _ptr(ld), Neff, Mc, n_real, _ptr(rows),
+                  _ptr(out["f"]), _ptr(out["beta"]), _ptr(out["se"]), _ptr(out["sfve"]), n_real, _ptr(max_F), st)
+        if done:
+            done(slot)
     if "nullh2" in out:  # (the streamed path fills nullh2 rows in host memory instead)
         _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(rows), Mc, _ptr(out["nullh2"]), n_real, st)
 

@@ -234,10 +234,13 @@ int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu
 /* flmm_fit_delta_fast without caller workspace.  No counterpart in the reference: it exists for callers that cannot
  * give this library device memory -- a host whose device memory is all owned by another pool, or a latency-critical
  * loop that may not call cudaMalloc (it can synchronise the device).  The scratch is a fixed 4 MiB device array in
- * the library (held by every GPU that loads it until exit), so n_grid * Neff is limited to ~1.04 million; larger
- * requests fail with FLMM_ERR_WORKSPACE.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before any stream capture.  All calls share
- * the array: calls whose kernels overlap on the GPU race and must be serialised by the caller.  Allocates nothing. */
+ * the library (held by every GPU that loads it until exit).  A call fits when flmm_fit_delta_fast_workspace_bytes
+ * (Neff, n_grid) <= 4 MiB, i.e. 4 (n_grid Neff + n_grid + 2 Neff + 4) + 8 n_grid + 512 <= 4,194,304 bytes (n_grid * Neff
+ * a little under 1,048,576); larger requests fail with FLMM_ERR_WORKSPACE.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current and keeps it for the process: make that
+ * first call before any stream capture, and do not use this entry point after cudaDeviceReset or from a non-primary
+ * driver context (the kept address belongs to the primary context the first call saw).  All calls share the array:
+ * calls whose kernels overlap on the GPU race and must be serialised by the caller.  Allocates nothing. */
 int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
                                 double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* stream);
 
@@ -262,12 +265,29 @@ int flmm_wald_split_prep_variants(const float* USt, int64_t ldus, int Mc, int Ne
 /* Fused split-precision Wald scan (fasterlmm/core.py:601-671): sWy = A1 B1^T (K = Neff) and sWs~ = L F^T (K = R) on
  * the tensor cores, then in the epilogue beta, var_beta (df Neff - 1), F, SE, SFVE with the reference's clamps (a
  * variant with sWs = 0 gets the FP64 1e-300 clamp); real columns p < n_real write out[rows[m] * ldo + p]; max_F[p]
- * is raised to the column max. */
+ * is raised to the column max.  Strong real tests: with flag_count != NULL, every real test whose F exceeds f_refine
+ * is left out of max_F and listed as (variant index m in [0, Mc), column p) int32 pairs in flags (room for flag_cap
+ * pairs; *flag_count is reset by this call and receives the number of such tests, which may exceed flag_cap), for
+ * flmm_wald_refine_f32 to recompute before the operands are overwritten.  flag_count == NULL: no list, every test
+ * counts into max_F. */
 int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda, const float* sa1,
                         const void* Lh, const void* Ll, int64_t ldl, const float* sl, const float* rWr,
                         const float* rWr0, int P, int n_real, const void* B1h, const void* B1l, int64_t ldb, const float* sb1, const void* Fh,
                         const void* Fl, int64_t ldf, const float* sf, int Mc, int Neff, int R, const int64_t* rows,
-                        double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
+                        double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F, float f_refine,
+                        int32_t* flag_count, int32_t* flags, int flag_cap, void* stream);
+
+/* Re-evaluation of the strong real tests listed by flmm_wald_split_f16 (the reference's Wald formulas,
+ * fasterlmm/core.py:649-667, without the cancelling subtraction rss = rWr - sWy^2 / sWs): from the FP32 rotated
+ * operands USt (Mc, ldus) and UYt (P, lduy) of the same chromosome, the FP32 spectrum s32 and the column log deltas,
+ * each listed test's residual sum of squares is formed around the scan's beta as a sum of positive terms
+ * (compensated FP32 per lane, FP64 across the warp), and f, beta, se, sfve are overwritten in place and max_F[p]
+ * raised to the new F.  When *flag_count > flag_cap every real test of the chromosome whose stored F exceeds f_refine
+ * is recomputed instead.  No counterpart in the reference (which computes in FP64 throughout). */
+int flmm_wald_refine_f32(flmm_context* ctx, const int32_t* flags, const int32_t* flag_count, int flag_cap,
+                         float f_refine, const float* USt, int64_t ldus, const float* UYt, int64_t lduy,
+                         const float* s32, const double* log_delta, int Neff, int Mc, int n_real, const int64_t* rows,
+                         double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
 
 /* Small conversions of the fast form: y[i] = (float)x[i]; y[i] += x[i] (FP32 into FP64); the LOCO kinship from an FP64
  * total and an FP32 chromosome Gram, K = (Gtot - Gc) / m_loco. */

@@ -1,0 +1,78 @@
+"""
+Seeded inputs with strong single-variant associations, drawn so that any numpy reproduces them exactly.
+
+The parity tests of the split-precision scan at large F need inputs that the reference's own FP64 run has been
+made on (tests/golden/make_strong_golden.py writes those outputs) while the inputs themselves are regenerated on
+the test host instead of being stored.  Only ``Generator.random()`` of numpy's PCG64 is used -- the raw 53-bit
+uniform, whose stream numpy keeps fixed -- and everything else is derived from those uniforms by elementary
+transforms: Hardy-Weinberg genotypes by inverse CDF, normals by Box-Muller.  A checksum of the genotypes is stored
+with the golden outputs so a host whose stream differed would fail loudly instead of comparing different data.
+
+Phenotypes follow the reference's simulator recipe (fasterlmm/sim.py:21-28: standardised causal columns, normal
+effects, genetic value rescaled to variance h2, noise of variance 1 - h2), with the causal variants of each
+phenotype on one chosen chromosome, then the Blom rank-inverse-normal transform the CLI applies
+(fasterlmm/normalize.py:21-52).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _normals(rng: np.random.Generator, n: int) -> np.ndarray:
+    u1 = 1.0 - rng.random(n)          # (0, 1]
+    u2 = rng.random(n)
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def _rint(y: np.ndarray, c: float = 3.0 / 8.0) -> np.ndarray:
+    from scipy.stats import norm, rankdata
+    ranks = rankdata(y, method="average")
+    return norm.ppf((ranks - c) / (y.size - 2 * c + 1))
+
+
+def genotype_checksum(G: np.ndarray) -> int:
+    """Order-dependent checksum of an int8 dosage matrix (exact integer arithmetic)."""
+    w = (np.arange(G.shape[1], dtype=np.int64) % 9973) + 1
+    return int(((G.astype(np.int64) * w[None, :]).sum(axis=1) * (np.arange(G.shape[0], dtype=np.int64) % 7919 + 1)).sum())
+
+
+def strong_dataset(N: int, sizes: list[int], D: int, specs: list[tuple[float, int, int]], *, seed: int,
+                   rint: bool = True):
+    """
+    (G (N, M) int8, X (N, D), Y (N, B), chrom (M,)) for phenotypes specs[b] = (h2, k, c): k causal variants on
+    chromosome c (1-based) explaining h2 of the variance (k = 0 or h2 = 0: noise only).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    M = int(sum(sizes))
+    chrom = np.repeat(np.arange(1, len(sizes) + 1), sizes)
+    maf = 0.05 + 0.45 * rng.random(M)
+    G = np.empty((N, M), dtype=np.int8)
+    for j0 in range(0, M, 4096):
+        j1 = min(M, j0 + 4096)
+        p = maf[j0:j1]
+        u = rng.random((N, j1 - j0))
+        G[:, j0:j1] = np.where(u < p * p, 2, np.where(u < 1.0 - (1.0 - p) ** 2, 1, 0)).astype(np.int8)
+    X = np.concatenate([np.ones((N, 1)), _normals(rng, N * (D - 1)).reshape(D - 1, N).T], axis=1)
+    starts = np.concatenate([[0], np.cumsum(sizes)])
+    Y = np.empty((N, len(specs)))
+    for b, (h2, k, c) in enumerate(specs):
+        e = _normals(rng, N) * np.sqrt(1.0 - h2)
+        if k == 0 or h2 == 0.0:
+            Y[:, b] = e
+        else:
+            lo, hi = int(starts[c - 1]), int(starts[c])
+            idx = lo + np.unique((rng.random(4 * k) * (hi - lo)).astype(np.int64))[:k]
+            Zc = G[:, idx].astype(np.float64)
+            Zc = (Zc - Zc.mean(axis=0)) / np.clip(Zc.std(axis=0), 1e-12, None)
+            g = Zc @ _normals(rng, idx.size)
+            Y[:, b] = g / g.std() * np.sqrt(h2) + e
+        if rint:
+            Y[:, b] = _rint(Y[:, b])
+    return G, X, Y, chrom
+
+
+# The N = 5,000 case of the golden fixture strong_n5000: three chromosomes of 3,000 variants (each LOCO kinship has
+# rank 6,000 > N), two covariates, six phenotypes from a single strong variant to pure noise, ten permutations each.
+N5000 = dict(N=5000, sizes=[3000, 3000, 3000], D=3,
+             specs=[(0.95, 1, 1), (0.8, 1, 2), (0.9, 2, 3), (0.5, 10, 1), (0.3, 40, 2), (0.0, 0, 1)],
+             seed=20250611, n_perm=10)

@@ -34,19 +34,19 @@ def _inputs(Neff, P, seed):
     return s, UYt
 
 
-def _fit(lib, s, UYt, n_grid, lo, hi, noalloc):
+def _fit(lib, s, UYt, n_grid, lo, hi, noalloc, refine=1):
     Neff = s.shape[0]
     P = UYt.shape[0]
-    ld = torch.full((P,), float("nan"), dtype=torch.float64, device="cuda")
-    idx = torch.full((P,), -1, dtype=torch.int32, device="cuda")
+    ld = torch.full((max(P, 1),), float("nan"), dtype=torch.float64, device="cuda")
+    idx = torch.full((max(P, 1),), -1, dtype=torch.int32, device="cuda")
     p = lambda t: C.c_void_p(t.data_ptr())
     if noalloc:
-        lib.call("flmm_fit_delta_fast_noalloc", p(s), Neff, p(UYt), UYt.stride(0), P, n_grid, lo, hi, 1, p(ld), p(idx),
-                 None)
+        lib.call("flmm_fit_delta_fast_noalloc", p(s), Neff, p(UYt), UYt.stride(0), P, n_grid, lo, hi, refine, p(ld),
+                 p(idx), None)
     else:
         nbytes = lib.query_bytes("flmm_fit_delta_fast_workspace_bytes", Neff, n_grid)
         work = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-        lib.call("flmm_fit_delta_fast", p(s), Neff, p(UYt), UYt.stride(0), P, n_grid, lo, hi, 1, p(ld), p(idx),
+        lib.call("flmm_fit_delta_fast", p(s), Neff, p(UYt), UYt.stride(0), P, n_grid, lo, hi, refine, p(ld), p(idx),
                  p(work), nbytes, None)
     torch.cuda.synchronize()
     return ld.cpu(), idx.cpu()
@@ -68,3 +68,39 @@ def test_noalloc_rejects_oversized_requests(lib):
     with pytest.raises(lib.FlmmError) as e:
         _fit(lib, s, UYt, 400, -10.0, 10.0, noalloc=True)  # 400 * 5000 floats > 4 MiB
     assert e.value.status == 4 and "fixed" in str(e.value)
+
+
+def test_noalloc_edge_cases_match_workspace_entry(lib):
+    """No columns, grid-only fits, and minima outside the bracket (the edge and binary-search branches)."""
+    s, UYt = _inputs(300, 1, 4)
+    ld = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    idx = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    p = lambda t: C.c_void_p(t.data_ptr())
+    lib.call("flmm_fit_delta_fast_noalloc", p(s), 300, p(UYt), 300, 0, 64, -10.0, 10.0, 1, p(ld), p(idx), None)
+    torch.cuda.synchronize()
+    assert torch.isnan(ld).all() and (idx == -1).all()  # P = 0: nothing written
+    s, UYt = _inputs(300, 129, 5)
+    for refine in (0, 1):
+        a = _fit(lib, s, UYt, 64, -10.0, 10.0, noalloc=False, refine=refine)
+        b = _fit(lib, s, UYt, 64, -10.0, 10.0, noalloc=True, refine=refine)
+        assert torch.equal(a[1], b[1]) and torch.equal(a[0], b[0])
+    # a narrow window [-1, 1]: most columns' minima lie outside it, so the fit ends at a window edge
+    a = _fit(lib, s, UYt, 16, -1.0, 1.0, noalloc=False)
+    b = _fit(lib, s, UYt, 16, -1.0, 1.0, noalloc=True)
+    assert torch.equal(a[1], b[1]) and torch.equal(a[0], b[0])
+    assert ((a[1] == 0) | (a[1] == 15)).any()
+
+
+def test_noalloc_limit_is_the_workspace_size(lib):
+    """The exact limit: calls whose workspace query is at most 4 MiB run, one grid node more is refused."""
+    limit = 4 << 20
+    Neff = 4096
+    fits = [g for g in range(200, 300) if lib.query_bytes("flmm_fit_delta_fast_workspace_bytes", Neff, g) <= limit]
+    g_max = max(fits)
+    s, UYt = _inputs(Neff, 3, 6)
+    a = _fit(lib, s, UYt, g_max, -10.0, 10.0, noalloc=False)
+    b = _fit(lib, s, UYt, g_max, -10.0, 10.0, noalloc=True)
+    assert torch.equal(a[0], b[0])
+    with pytest.raises(lib.FlmmError) as e:
+        _fit(lib, s, UYt, g_max + 1, -10.0, 10.0, noalloc=True)
+    assert e.value.status == 4
