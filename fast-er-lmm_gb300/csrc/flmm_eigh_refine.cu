@@ -118,6 +118,9 @@ __global__ void k_rq_residual(const double* __restrict__ W, const float* __restr
 
 constexpr int FB = 64, FK = 16, FT = 256;
 
+// largest first-order rotation E_ij one refinement step applies to a pair of eigenvectors
+constexpr double kMaxRotation = 0.25;
+
 // FP32 batched products, C[b] = A[b] B[b]^T (NT) or A[b] B[b] (NN), (N, N) each; with ADD the result is added to
 // D[b] and written to C[b].
 template <bool NT, bool ADD>
@@ -179,8 +182,13 @@ k_f32_gemm(const float* __restrict__ A, const float* __restrict__ B, const float
     }
 }
 
-// T[j, i] = E_ij = M[i, j] / (lambda_j - lambda_i) for |lambda_j - lambda_i| > tau, 0 for closer pairs,
-// T[j, j] = (1 - nrm_j) / 2;  M[i, j] = u_i . r_j.  tau = 1e-6 max |lambda| of the matrix.
+// T[j, i] = E_ij = M[i, j] / (lambda_j - lambda_i) where that first-order rotation is small, |E_ij| <= kMaxRotation,
+// and the pair is not closer than tau = 1e-6 max |lambda| of the matrix; 0 otherwise.  T[j, j] = (1 - nrm_j) / 2;
+// M[i, j] = u_i . r_j.  A pair whose coupling is not small against its gap is left as it is for this step: the
+// first-order update is only valid for small rotations (applied to a large one it makes the vectors worse, which is
+// what an FP32 decomposition of a 5,000 x 5,000 kinship gives for its closest pairs), the step's other corrections
+// shrink the residuals, and a later step rotates the pair once its coupling is small.  A pair left unrotated moves
+// the likelihood only by ~ M_ij / (s + delta), whatever the angle.
 __global__ void k_refine_coeffs(const float* __restrict__ M, const double* __restrict__ lam,
                                 const double* __restrict__ nrm, int N, float* __restrict__ T) {
     const int64_t nn = static_cast<int64_t>(N) * N;
@@ -195,8 +203,8 @@ __global__ void k_refine_coeffs(const float* __restrict__ M, const double* __res
         v = static_cast<float>(0.5 * (1.0 - nrm[static_cast<int64_t>(b) * N + j]));
     } else {
         const double gap = lb[j] - lb[i];
-        v = fabs(gap) > tau ? static_cast<float>(static_cast<double>(M[b * nn + static_cast<int64_t>(i) * N + j]) / gap)
-                            : 0.0f;
+        const double m = static_cast<double>(M[b * nn + static_cast<int64_t>(i) * N + j]);
+        v = (fabs(gap) > tau && fabs(m) <= kMaxRotation * fabs(gap)) ? static_cast<float>(m / gap) : 0.0f;
     }
     T[b * nn + t] = v;
 }

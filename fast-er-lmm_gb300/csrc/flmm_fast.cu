@@ -13,7 +13,16 @@
 //           side by side, with beta, var_beta, F, SE, SFVE and the per-column genome max computed in the epilogue.
 // Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, warps 2-9 run the epilogue
 // (warp w reads TMEM lanes 32 (w % 4) .. +31, half of the tile's columns).  Shared memory holds 192 KB of operand
-// stages; tensor memory holds two accumulator sets so the epilogue of one tile overlaps the MMAs of the next.
+// stages.
+//
+// Accumulation in K chunks: the tensor core's FP32 accumulation does not round to nearest -- every MMA step loses
+// about an ulp of the accumulator's magnitude towards zero, so a product over K accumulated in one place carries a
+// relative bias that grows linearly with K (measured on GB300 with positive operands: -7e-6 at K = 1,000, -4e-5 at
+// K = 5,000, -1.7e-4 at K = 20,000).  Each accumulator therefore covers only a chunk of a few k-blocks: tensor
+// memory holds a ring of kSlots chunk accumulators, the MMA issuer starts every chunk afresh in the next free slot,
+// and the epilogue warps drain each finished chunk into FP32 registers with round-to-nearest additions.  The bias is
+// then that of a 128- or 256-long accumulation (~1e-6) whatever K is, and the ring lets the MMAs of the next chunks
+// (and tiles) run while the epilogue drains or finishes a tile.
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 #include <math.h>
@@ -36,6 +45,14 @@ constexpr int kBN = 128;  // B rows per tile (accumulator columns)
 constexpr int kThreads = 320;        // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kEpilogueThreads = 256;
 constexpr int kBK = 64;  // reduction depth of one pipeline stage: 64 gives 3 stages of 64 KB, 32 gives 6 of 32 KB
+constexpr int kSlots = 4;  // tensor-memory chunk accumulators of kBN columns (all 512 columns)
+// k-blocks of 64 per chunk accumulator (TcArgs::chunk_kb; FLMM_CHUNK_KB / FLMM_WALD_CHUNK_KB override): 2 for the
+// GEMMs (Grams and the sWs node table are sums of positive terms); 4 for the Wald product sWy, whose partial sums are
+// small next to sWs except for strong associations, and those are recomputed (flmm_wald_refine_f32).  The Wald
+// kernel's second product (the interpolated sWs, K = R nodes) is always one chunk, read straight from its slot in
+// the epilogue.
+template <int NG>
+constexpr int default_chunk_kb() { return NG == 2 ? 4 : 2; }
 
 template <int NG, int BK>
 struct Cfg {
@@ -44,7 +61,7 @@ struct Cfg {
     static constexpr int kStages = (BK == 32) ? 6 : 3;   // 192 KB of operand stages either way
     static constexpr uint32_t kSwizzle = (BK == 64) ? 2u : 4u;  // 128-byte / 64-byte swizzle
     static constexpr uint32_t kSBO = 8u * BK * 2u;             // bytes between 8-row groups
-    static constexpr int kTmemCols = NG * kBN * 2;
+    static constexpr int kTmemCols = kSlots * kBN;
     static constexpr int kBarBytes = 256;
     // per epilogue warp: the scales of its 64 variants (two products) and their output rows, staged once per tile
     static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
@@ -90,6 +107,8 @@ struct TcArgs {
     int flag_cap;
     // tile order of the persistent schedule (see tile_coords); 0 or 1 = A-major
     int group;
+    // k-blocks per chunk accumulator of product 0 (>= 1)
+    int chunk_kb;
 };
 
 // Tile t of the persistent schedule -> (A block ta, B block tb).  Tiles are visited in groups of `group` A blocks;
@@ -114,11 +133,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
 }
 
 // Wald statistics of one epilogue thread: accumulator row p (a column of the phenotype table) against tile columns
-// [cbeg, cbeg + 64) (variants), TMEM address tl of product 0 for this thread's lane quarter (product 1 lies kBN
-// columns further), the warp's staged scales sc1 / sc2 and output rows rws.
-__device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p, bool real_tile, int nvalid,
-                                          int cbeg, int mbase, const float* sc1, const float* sc2,
-                                          const int64_t* rws) {
+// [cbeg, cbeg + 64) (variants): the sums of product 0 in y[] (drained from its chunk accumulators), product 1 read
+// from its TMEM slot at tl_s (this thread's lane, column cbeg), the warp's staged scales sc1 / sc2 and output rows.
+__device__ __forceinline__ void wald_rows(const TcArgs& args, const float (&y)[64], uint32_t tl_s, int p,
+                                          bool real_tile, int nvalid, int cbeg, int mbase, const float* sc1,
+                                          const float* sc2, const int64_t* rws) {
     // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each test needs
     // two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
     //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
@@ -130,12 +149,20 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p
     const bool real = row_ok && p < args.n_real;
     float colmax = -INFINITY;
     bool col_nan = false;
-    for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-        float vy[16], vs[16];
-        tmem_ld16x2(tl + static_cast<uint32_t>(c0), tl + static_cast<uint32_t>(kBN + c0), vy, vs);
+    // one 16-column quarter per iteration; the loop is kept rolled (the statistics' code is long) and the quarter's
+    // sums are picked from the register array by selects
+#pragma unroll 1
+    for (int qd = 0; qd < 4; ++qd) {
+        const int c0 = cbeg + 16 * qd;
+        float vy[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            vy[j] = qd == 0 ? y[j] : (qd == 1 ? y[16 + j] : (qd == 2 ? y[32 + j] : y[48 + j]));
+        float vs[16];
+        tmem_ld16_wait(tl_s + static_cast<uint32_t>(16 * qd), vs);
         if (!row_ok) continue;
-        const float* s1 = sc1 + (c0 - cbeg);
-        const float* s2 = sc2 + (c0 - cbeg);
+        const float* s1 = sc1 + 16 * qd;
+        const float* s2 = sc2 + 16 * qd;
         if (!real_tile) {
             // permutation columns: F and the column maximum only
 #pragma unroll
@@ -173,7 +200,7 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p
             if (!listed) colmax = fmaxf(colmax, F);
             col_nan |= (F != F);
             if (!real) continue;
-            const int64_t o = rws[c0 - cbeg + j] * args.ldo + p;
+            const int64_t o = rws[16 * qd + j] * args.ldo + p;
             if (var_ok) {
                 args.f[o] = F;
                 args.beta[o] = swy * inv_d;
@@ -193,25 +220,26 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, uint32_t tl, int p
 }
 
 // C = sa sb^T (acc) for one epilogue thread: accumulator row i against tile columns [cbeg, cbeg + 64) starting at
-// column col0 of C, TMEM address tl for this thread's lane quarter, staged column scales sc1.
-__device__ __forceinline__ void gemm_rows(const TcArgs& args, uint32_t tl, int i, int col0, int nvalid, int cbeg,
-                                          const float* sc1) {
+// column col0 of C, with the drained sums v[], staged column scales sc1.
+__device__ __forceinline__ void gemm_rows(const TcArgs& args, const float (&v)[64], int i, int col0, int nvalid,
+                                          int cbeg, const float* sc1) {
     const bool row_ok = i < args.Mr;
-    const float sa = row_ok ? args.sa[i] : 0.0f;
+    if (!row_ok) return;
+    const float sa = args.sa[i];
     float* crow = args.C + static_cast<int64_t>(i) * args.ldc + col0;
-    for (int c0 = cbeg; c0 < cbeg + kBN / 2; c0 += 16) {
-        float v[16];
-        tmem_ld16_wait(tl + static_cast<uint32_t>(c0), v);
-        if (!row_ok) continue;
-        const float* sc = sc1 + (c0 - cbeg);
+#pragma unroll
+    for (int qd = 0; qd < 4; ++qd) {
+        const int c0 = cbeg + 16 * qd;
+        const float* sc = sc1 + 16 * qd;
+        const float* vv = v + 16 * qd;
         float* dst = crow + c0;
         if (c0 + 16 <= nvalid && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
             // a thread owns 16 consecutive outputs of its row: four 16-byte stores
             float4* d4 = reinterpret_cast<float4*>(dst);
 #pragma unroll
             for (int q4 = 0; q4 < 4; ++q4) {
-                float4 x = make_float4(v[4 * q4] * sa * sc[4 * q4], v[4 * q4 + 1] * sa * sc[4 * q4 + 1],
-                                       v[4 * q4 + 2] * sa * sc[4 * q4 + 2], v[4 * q4 + 3] * sa * sc[4 * q4 + 3]);
+                float4 x = make_float4(vv[4 * q4] * sa * sc[4 * q4], vv[4 * q4 + 1] * sa * sc[4 * q4 + 1],
+                                       vv[4 * q4 + 2] * sa * sc[4 * q4 + 2], vv[4 * q4 + 3] * sa * sc[4 * q4 + 3]);
                 if (args.accumulate) {
                     const float4 o = d4[q4];
                     x.x += o.x;
@@ -226,11 +254,38 @@ __device__ __forceinline__ void gemm_rows(const TcArgs& args, uint32_t tl, int i
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             if (c0 + j < nvalid) {
-                const float x = v[j] * sa * sc[j];
+                const float x = vv[j] * sa * sc[j];
                 dst[j] = args.accumulate ? dst[j] + x : x;
             }
         }
     }
+}
+
+// Add the 64 accumulator columns at TMEM address tl (this thread's lane) into acc[] (FP32, round to nearest): four
+// loads in flight, one wait.
+__device__ __forceinline__ void drain64(uint32_t tl, float (&acc)[64]) {
+    uint32_t v[64];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, "
+        "[%65];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, "
+        "[%66];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, "
+        "[%67];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
+          "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]),
+          "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]),
+          "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+          "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+        : "r"(tl), "r"(tl + 16u), "r"(tl + 32u), "r"(tl + 48u)
+        : "memory");
+#pragma unroll
+    for (int j = 0; j < 64; ++j) acc[j] += __uint_as_float(v[j]);
 }
 
 template <int NG, int BK>
@@ -239,11 +294,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kStageBytes);
-    uint64_t* full = bars;                  // [kStages]
-    uint64_t* empty = bars + C::kStages;    // [kStages]
-    uint64_t* acc_full = bars + 2 * C::kStages;      // [2]
-    uint64_t* acc_empty = acc_full + 2;              // [2]
-    uint64_t* final_bar = acc_empty + 2;             // [1]
+    uint64_t* full = bars;                          // [kStages]
+    uint64_t* empty = bars + C::kStages;            // [kStages]
+    uint64_t* slot_full = bars + 2 * C::kStages;    // [kSlots] chunk accumulated (MMA -> epilogue)
+    uint64_t* slot_empty = slot_full + kSlots;      // [kSlots] chunk drained (epilogue -> MMA)
+    uint64_t* final_bar = slot_empty + kSlots;      // [1]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(final_bar + 1);
     uint8_t* epi_smem = smem + C::kStages * C::kStageBytes + C::kBarBytes;  // [8][kEpiWarpBytes]
 
@@ -251,8 +306,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     const int tiles_b = (args.Nr + kBN - 1) / kBN;
     const int tiles_a = (args.Mr + kBM - 1) / kBM;
     const int n_tiles = tiles_a * tiles_b;
-    // the NG products of a tile run one after the other, product g over its own K: k-blocks [0, n_kb0) feed
-    // accumulator 0, [n_kb0, n_kb) accumulator 1
+    // the NG products of a tile run one after the other, product g over its own K: k-blocks [0, n_kb0) belong to
+    // product 0, [n_kb0, n_kb) to product 1; product 0 is accumulated in chunks of args.chunk_kb k-blocks, product
+    // 1 in one chunk
     const int n_kb0 = (args.K + BK - 1) / BK;
     const int n_kb = n_kb0 + (NG == 2 ? (args.K2 + BK - 1) / BK : 0);
     constexpr uint32_t idesc = idesc_f16_f32(kBM, kBN);
@@ -262,9 +318,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], kEpilogueThreads);
+        for (int b = 0; b < kSlots; ++b) {
+            mbar_init(&slot_full[b], 1);
+            mbar_init(&slot_empty[b], kEpilogueThreads);
         }
         mbar_init(final_bar, 1);
         fence_barrier_init();
@@ -312,40 +368,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
                 if (armed[s]) mbar_drain(&full[s], armed_phase[s]);
         }
     } else if (warp == 1) {
-        // ---- MMA issuer ----
+        // ---- MMA issuer: every chunk starts afresh in the next slot of the ring ----
         if (lane == 0) {
             int stage = 0;
             uint32_t phase = 0;
-            int ab = 0;
-            uint32_t aphase = 0;
+            int slot = 0;
+            uint32_t sphase = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
-                if (!mbar_wait(&acc_empty[ab], aphase ^ 1u, args.err, 2)) break;
-                fence_after_sync();
-                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * NG * kBN);
-                for (int kb = 0; kb < n_kb; ++kb) {
-                    if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                for (int kc = 0, kc_end = 0; kc < n_kb && ok; kc = kc_end) {
+                    kc_end = kc < n_kb0 ? min(kc + args.chunk_kb, n_kb0) : n_kb;
+                    if (!mbar_wait(&slot_empty[slot], sphase ^ 1u, args.err, 2)) { ok = false; break; }
                     fence_after_sync();
-                    const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
-                    const int g = kb < n_kb0 ? 0 : 1;
-                    const int kb_g = kb - g * n_kb0;
-                    const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
+                    const uint32_t d = tmem_base + static_cast<uint32_t>(slot * kBN);
+                    for (int kb = kc; kb < kc_end; ++kb) {
+                        if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                        fence_after_sync();
+                        const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; ++kk) {
-                        const uint64_t ah = smem_desc(sbase + 0 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t al = smem_desc(sbase + 1 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t bh = smem_desc(sbase + 2 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t bl = smem_desc(sbase + 3 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        mma_f16(d, ah, bh, idesc, (kb_g | kk) ? 1u : 0u);
-                        mma_f16(d, ah, bl, idesc, 1u);
-                        mma_f16(d, al, bh, idesc, 1u);
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            const uint64_t ah = smem_desc(sbase + 0 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t al = smem_desc(sbase + 1 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bh = smem_desc(sbase + 2 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bl = smem_desc(sbase + 3 * C::kTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            mma_f16(d, ah, bh, idesc, (kb != kc || kk) ? 1u : 0u);
+                            mma_f16(d, ah, bl, idesc, 1u);
+                            mma_f16(d, al, bh, idesc, 1u);
+                        }
+                        mma_commit(&empty[stage]);
+                        if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
                     }
-                    mma_commit(&empty[stage]);
-                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                    if (!ok) break;
+                    mma_commit(&slot_full[slot]);
+                    if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
                 }
-                if (!ok) break;
-                mma_commit(&acc_full[ab]);
-                if (++ab == 2) { ab = 0; aphase ^= 1u; }
             }
             // every MMA this thread issued has completed before tensor memory is released
             mma_commit(final_bar);
@@ -354,45 +410,62 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
     } else {
         // ---- epilogue: warps 2..9.  Warp w reads TMEM lanes 32 (w % 4) .. +31 (thread = one accumulator row) and
         // half (w - 2) / 4 of the tile's columns, so two warps share each lane quarter.  Each warp stages the scales
-        // (and output rows) of its 64 variants in its own shared-memory slot before waiting for the accumulator,
-        // so those loads overlap the MMAs instead of stalling the epilogue.
+        // (and output rows) of its 64 variants in its own shared-memory slot before draining the chunks, so those
+        // loads overlap the MMAs instead of stalling the epilogue.
         const int q = warp & 3;
         const int cbeg = ((warp - 2) >> 2) * (kBN / 2);
         const int r = q * 32 + lane;
         float* sc1 = reinterpret_cast<float*>(epi_smem + (warp - 2) * C::kEpiWarpBytes);  // [64]
         float* sc2 = sc1 + 64;                                                           // [64]
         int64_t* rws = reinterpret_cast<int64_t*>(sc2 + 64);                             // [64]
-        int ab = 0;
-        uint32_t aphase = 0;
-        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const uint32_t tl0 = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(cbeg);
+        int slot = 0;
+        uint32_t sphase = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
             int ta, tb;
-                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
+            tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
             const int nvalid = min(kBN, args.Nr - tb * kBN);  // columns of this tile inside B
             const bool real_tile = NG == 2 && ta * kBM < args.n_real;  // uniform over the CTA
             __syncwarp();  // every lane is done with the previous tile's slot
             for (int k = lane; k < kBN / 2; k += 32) {
                 const int c = cbeg + k;
                 const int m = tb * kBN + c;
-                const bool ok = c < nvalid;
-                sc1[k] = ok ? args.sb[m] : 0.0f;
+                const bool okc = c < nvalid;
+                sc1[k] = okc ? args.sb[m] : 0.0f;
                 if constexpr (NG == 2) {
-                    sc2[k] = ok ? args.sb2[m] : 0.0f;
-                    if (real_tile) rws[k] = ok ? args.rows[m] : 0;
+                    sc2[k] = okc ? args.sb2[m] : 0.0f;
+                    if (real_tile) rws[k] = okc ? args.rows[m] : 0;
                 }
             }
             __syncwarp();
-            if (!mbar_wait(&acc_full[ab], aphase, args.err, 4)) break;
-            fence_after_sync();
-            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
+            float acc0[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) acc0[j] = 0.0f;
+            // product 0: drain every chunk into acc0 and hand its slot back
+            for (int kc = 0, kc_end = 0; kc < n_kb0; kc = kc_end) {
+                kc_end = min(kc + args.chunk_kb, n_kb0);
+                if (!mbar_wait(&slot_full[slot], sphase, args.err, 4)) { ok = false; break; }
+                fence_after_sync();
+                drain64(tl0 + static_cast<uint32_t>(slot * kBN), acc0);
+                fence_before_sync();
+                mbar_arrive(&slot_empty[slot]);
+                if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
+            }
+            if (!ok) break;
             const int i = ta * kBM + r;  // A row
             if constexpr (NG == 1) {
-                gemm_rows(args, tl, i, tb * kBN, nvalid, cbeg, sc1);
+                gemm_rows(args, acc0, i, tb * kBN, nvalid, cbeg, sc1);
             } else {
-                wald_rows(args, tl, i, real_tile, nvalid, cbeg, tb * kBN, sc1, sc2, rws);
+                // product 1 (one chunk) is read from its slot by the statistics, then the slot is handed back
+                if (!mbar_wait(&slot_full[slot], sphase, args.err, 4)) { ok = false; break; }
+                fence_after_sync();
+                wald_rows(args, acc0, tl0 + static_cast<uint32_t>(slot * kBN), i, real_tile, nvalid, cbeg, tb * kBN,
+                          sc1, sc2, rws);
+                fence_before_sync();
+                mbar_arrive(&slot_empty[slot]);
+                if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
             }
-            fence_before_sync();
-            mbar_arrive(&acc_empty[ab]);
-            if (++ab == 2) { ab = 0; aphase ^= 1u; }
         }
     }
 
@@ -414,9 +487,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc(const __grid_constant__ TcMa
 // memory bandwidth is what bounds the single-CTA form.
 //
 // Synchronisation: both CTAs' TMA loads of a stage complete on the even CTA's full[stage] (its producer expects the
-// pair's bytes); the MMA issuer's commits arrive on empty[stage], acc_full[] and the final barrier of both CTAs
-// (multicast); the epilogue warps of both CTAs arrive on the even CTA's acc_empty[] (16 warps).  Every wait is
-// bounded as in the single-CTA kernel.
+// pair's bytes); the MMA issuer's commits arrive on empty[stage], slot_full[] and the final barrier of both CTAs
+// (multicast); the epilogue warps of both CTAs arrive on the even CTA's slot_empty[] (16 warps) once they have
+// drained a chunk.  Every wait is bounded as in the single-CTA kernel.
 template <int NG>
 struct PairCfg {
     static constexpr int kBK = 64;
@@ -426,7 +499,7 @@ struct PairCfg {
     static constexpr int kStages = 4;
     static constexpr uint32_t kSwizzle = 2u;   // 128-byte
     static constexpr uint32_t kSBO = 1024u;    // bytes between 8-row groups
-    static constexpr int kTmemCols = NG * 2 * kBN;  // NG products, double-buffered
+    static constexpr int kTmemCols = kSlots * kBN;  // the ring of chunk accumulators
     static constexpr int kBarBytes = 256;
     static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
     static constexpr int kEpiBytes = 8 * kEpiWarpBytes;
@@ -443,11 +516,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::kStages * C::kStageBytes);
-    uint64_t* full = bars;                        // [kStages], used in the even CTA
-    uint64_t* empty = bars + C::kStages;          // [kStages]
-    uint64_t* acc_full = bars + 2 * C::kStages;   // [2]
-    uint64_t* acc_empty = acc_full + 2;           // [2], used in the even CTA
-    uint64_t* final_bar = acc_empty + 2;          // [1]
+    uint64_t* full = bars;                          // [kStages], used in the even CTA
+    uint64_t* empty = bars + C::kStages;            // [kStages]
+    uint64_t* slot_full = bars + 2 * C::kStages;    // [kSlots] chunk accumulated (MMA -> both CTAs' epilogues)
+    uint64_t* slot_empty = slot_full + kSlots;      // [kSlots] chunk drained by both CTAs, used in the even CTA
+    uint64_t* final_bar = slot_empty + kSlots;      // [1]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(final_bar + 1);
     uint8_t* epi_smem = smem + C::kStages * C::kStageBytes + C::kBarBytes;
 
@@ -467,9 +540,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 2 * (kEpilogueThreads / 32));
+        for (int b = 0; b < kSlots; ++b) {
+            mbar_init(&slot_full[b], 1);
+            mbar_init(&slot_empty[b], 2 * (kEpilogueThreads / 32));
         }
         mbar_init(final_bar, 1);
         fence_barrier_init();
@@ -530,40 +603,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
         }
     } else if (warp == 1) {
         if (leader && lane == 0) {
-            // ---- MMA issuer (even CTA) ----
+            // ---- MMA issuer (even CTA): every chunk starts afresh in the next slot of the ring ----
             int stage = 0;
             uint32_t phase = 0;
-            int ab = 0;
-            uint32_t aphase = 0;
+            int slot = 0;
+            uint32_t sphase = 0;
             bool ok = true;
             for (int t = cl; t < n_tiles && ok; t += n_cl) {
-                if (!mbar_wait_cluster(&acc_empty[ab], aphase ^ 1u, args.err, 2)) break;
-                fence_after_sync();
-                const uint32_t d0 = tmem_base + static_cast<uint32_t>(ab * NG * kBN);
-                for (int kb = 0; kb < n_kb; ++kb) {
-                    if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                for (int kc = 0, kc_end = 0; kc < n_kb && ok; kc = kc_end) {
+                    kc_end = kc < n_kb0 ? min(kc + args.chunk_kb, n_kb0) : n_kb;
+                    if (!mbar_wait_cluster(&slot_empty[slot], sphase ^ 1u, args.err, 2)) { ok = false; break; }
                     fence_after_sync();
-                    const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
-                    const int g = kb < n_kb0 ? 0 : 1;
-                    const int kb_g = kb - g * n_kb0;
-                    const uint32_t d = d0 + static_cast<uint32_t>(g * kBN);
+                    const uint32_t d = tmem_base + static_cast<uint32_t>(slot * kBN);
+                    for (int kb = kc; kb < kc_end; ++kb) {
+                        if (!mbar_wait(&full[stage], phase, args.err, 3)) { ok = false; break; }
+                        fence_after_sync();
+                        const uint32_t sbase = smem_u32(smem + stage * C::kStageBytes);
 #pragma unroll
-                    for (int kk = 0; kk < C::kBK / 16; ++kk) {
-                        const uint64_t ah = smem_desc(sbase, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t al = smem_desc(sbase + C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t bh = smem_desc(sbase + 2 * C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        const uint64_t bl =
-                            smem_desc(sbase + 2 * C::kATileBytes + C::kBTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
-                        mma_f16_pair(d, ah, bh, idesc, (kb_g | kk) ? 1u : 0u);
-                        mma_f16_pair(d, ah, bl, idesc, 1u);
-                        mma_f16_pair(d, al, bh, idesc, 1u);
+                        for (int kk = 0; kk < C::kBK / 16; ++kk) {
+                            const uint64_t ah = smem_desc(sbase, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t al = smem_desc(sbase + C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bh = smem_desc(sbase + 2 * C::kATileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            const uint64_t bl =
+                                smem_desc(sbase + 2 * C::kATileBytes + C::kBTileBytes, C::kSBO, C::kSwizzle) + 2u * kk;
+                            mma_f16_pair(d, ah, bh, idesc, (kb != kc || kk) ? 1u : 0u);
+                            mma_f16_pair(d, ah, bl, idesc, 1u);
+                            mma_f16_pair(d, al, bh, idesc, 1u);
+                        }
+                        mma_commit_pair(&empty[stage], 3);
+                        if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
                     }
-                    mma_commit_pair(&empty[stage], 3);
-                    if (++stage == C::kStages) { stage = 0; phase ^= 1u; }
+                    if (!ok) break;
+                    mma_commit_pair(&slot_full[slot], 3);
+                    if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
                 }
-                if (!ok) break;
-                mma_commit_pair(&acc_full[ab], 3);
-                if (++ab == 2) { ab = 0; aphase ^= 1u; }
             }
             mma_commit_pair(final_bar, 3);
             mbar_drain(final_bar, 0);
@@ -579,12 +652,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
         float* sc1 = reinterpret_cast<float*>(epi_smem + (warp - 2) * C::kEpiWarpBytes);
         float* sc2 = sc1 + 64;
         int64_t* rws = reinterpret_cast<int64_t*>(sc2 + 64);
-        const uint32_t acc_empty0 = map_to_rank(smem_u32(acc_empty), 0);
-        int ab = 0;
-        uint32_t aphase = 0;
-        for (int t = cl; t < n_tiles; t += n_cl) {
+        const uint32_t slot_empty0 = map_to_rank(smem_u32(slot_empty), 0);
+        const uint32_t tl0 = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(cbeg);
+        int slot = 0;
+        uint32_t sphase = 0;
+        bool ok = true;
+        for (int t = cl; t < n_tiles && ok; t += n_cl) {
             int ta, tb;
-                tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
+            tile_coords(t, tiles_a, tiles_b, args.group, ta, tb);
             const int nvalid = min(kBN, args.Nr - tb * kBN);
             const int row0 = ta * kPairRows + static_cast<int>(rank) * 128;
             const bool real_tile = NG == 2 && row0 < args.n_real;  // uniform over the CTA
@@ -600,18 +675,36 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
                 }
             }
             __syncwarp();
-            const bool ok = mbar_wait(&acc_full[ab], aphase, args.err, 4);
-            if (!__all_sync(0xffffffffu, ok)) break;
-            fence_after_sync();
-            const uint32_t tl = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(ab * NG * kBN);
-            if constexpr (NG == 1)
-                gemm_rows(args, tl, row0 + r, tb * kBN, nvalid, cbeg, sc1);
-            else
-                wald_rows(args, tl, row0 + r, real_tile, nvalid, cbeg, tb * kBN, sc1, sc2, rws);
-            fence_before_sync();
-            __syncwarp();
-            if (lane == 0) mbar_arrive_cluster(acc_empty0 + static_cast<uint32_t>(ab * 8));
-            if (++ab == 2) { ab = 0; aphase ^= 1u; }
+            float acc0[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) acc0[j] = 0.0f;
+            // product 0: drain every chunk into acc0 and hand its slot back
+            for (int kc = 0, kc_end = 0; kc < n_kb0; kc = kc_end) {
+                kc_end = min(kc + args.chunk_kb, n_kb0);
+                const bool got = mbar_wait(&slot_full[slot], sphase, args.err, 4);
+                if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
+                fence_after_sync();
+                drain64(tl0 + static_cast<uint32_t>(slot * kBN), acc0);
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive_cluster(slot_empty0 + static_cast<uint32_t>(slot * 8));
+                if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
+            }
+            if (!ok) break;
+            if constexpr (NG == 1) {
+                gemm_rows(args, acc0, row0 + r, tb * kBN, nvalid, cbeg, sc1);
+            } else {
+                // product 1 (one chunk) is read from its slot by the statistics, then the slot is handed back
+                const bool got = mbar_wait(&slot_full[slot], sphase, args.err, 4);
+                if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
+                fence_after_sync();
+                wald_rows(args, acc0, tl0 + static_cast<uint32_t>(slot * kBN), row0 + r, real_tile, nvalid, cbeg,
+                          tb * kBN, sc1, sc2, rws);
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive_cluster(slot_empty0 + static_cast<uint32_t>(slot * 8));
+                if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
+            }
         }
     }
 
@@ -943,6 +1036,17 @@ int launch_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max, cuda
     return check_launch(NG == 1 ? "k_pair<gemm>" : "k_pair<wald>");
 }
 
+// k-blocks per chunk accumulator: the default, or FLMM_CHUNK_KB (GEMMs) / FLMM_WALD_CHUNK_KB (Wald) from the environment
+template <int NG>
+int chunk_kb_for() {
+    static const int v = [] {
+        const char* e = std::getenv(NG == 2 ? "FLMM_WALD_CHUNK_KB" : "FLMM_CHUNK_KB");
+        const int x = e ? std::atoi(e) : 0;
+        return x >= 1 ? x : default_chunk_kb<NG>();
+    }();
+    return v;
+}
+
 // tcgen05 kernel form: CTA pairs unless FLMM_TC_PAIR=0 asks for the single-CTA kernels (kept for cross-checks)
 bool use_pair_kernel() {
     static const bool on = [] {
@@ -995,6 +1099,7 @@ template <int NG>
 int launch_choice(const TcMaps& maps_tc, const TcMaps& maps_pair, TcArgs a, TcChoice c, int n_cl, int sm_count,
                   cudaStream_t st) {
     a.group = c.group;
+    a.chunk_kb = chunk_kb_for<NG>();
     // every launch starts a fresh list of strong real tests (autotuning may run the Wald kernel several times)
     if (NG == 2 && a.flag_count != nullptr) FLMM_CUDA(cudaMemsetAsync(a.flag_count, 0, sizeof(int), st));
     if (c.pair && n_cl > 0) return launch_pair<NG>(maps_pair, a, n_cl, st);

@@ -39,7 +39,15 @@ F32 = torch.float32
 #   "f64": the FP64 batched call (EIGH_MODE: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on worker streams).
 EIGH_PRECISION = "f32r"
 EIGH_MODE = 1
-EIGH_REFINE_STEPS = 2
+# Refinement steps of "f32r": None picks by size -- 2 up to N = 2,000, 3 above (the FP32 decomposition's error grows
+# with N: at N = 5,000 two steps leave beta of ~1 % of the tests outside 1e-5 of the FP64 result, three match it).
+EIGH_REFINE_STEPS = None
+
+
+def refine_steps(N: int) -> int:
+    if EIGH_REFINE_STEPS is not None:
+        return max(1, int(EIGH_REFINE_STEPS))
+    return 2 if N <= 2000 else 3
 # Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
 # fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
 DELTA_PROPOSAL = "grid"
@@ -426,7 +434,7 @@ def _eigh_batched_f32_refined(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
     U_ref = torch.empty_like(U)
     evals = torch.empty((batch, N), dtype=F64, device=dev)
     w, wb = _work.get(dev, _lib.query_bytes("flmm_eigh_refine_workspace_bytes", N, batch))
-    for _ in range(max(1, EIGH_REFINE_STEPS)):
+    for _ in range(refine_steps(N)):
         _lib.call("flmm_eigh_refine_f32", _ptr(Kp), _ptr(U), _ptr(U_ref), _ptr(evals), N, batch, w, wb,
                   _stream(dev))
         U, U_ref = U_ref, U
