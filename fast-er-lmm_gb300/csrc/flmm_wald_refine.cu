@@ -166,7 +166,11 @@ extern "C" int flmm_wald_refine_f32(flmm_context* ctx, const int32_t* flags, con
     a.max_F = max_F;
     a.f_refine = f_refine;
     cudaStream_t st = as_stream(stream);
-    const unsigned grid = static_cast<unsigned>(4 * flmm_ctx_sm_count(ctx));
+    // A small grid: the launch usually finds few or no strong tests, and it must get onto the SMs quickly while the
+    // next chromosome's delta fit runs beside it on another stream (a grid of several CTAs per SM waited there for
+    // whole waves of that fit and held the Wald stream back ~1 ms per chromosome).
+    const int sms = flmm_ctx_sm_count(ctx);
+    const unsigned grid = static_cast<unsigned>(sms < 32 ? sms : 32);
     if (flag_cap > 0) {
         k_wald_refine_list<<<grid, 256, 0, st>>>(reinterpret_cast<const int2*>(flags), flag_count, flag_cap, a);
         int rc = check_launch("k_wald_refine_list");

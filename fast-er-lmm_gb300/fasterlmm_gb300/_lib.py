@@ -106,11 +106,25 @@ SIGNATURES: dict[str, list] = {
                             _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, C.c_float, _p, _p, _i, _p],
     "flmm_wald_refine_f32": [_p, _p, _p, _i, C.c_float, _p, _i64, _p, _i64, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p,
                              _i64, _p, _p],
+    "flmm_scan_opts_default": [_p],
+    "flmm_scan_create": [_i, _i, _i, _p, C.POINTER(_p)],
+    "flmm_scan_destroy": [_p],
+    "flmm_scan_group_prepare": [_p, _p, _p, _i64, _i, _p, _p, _i, _p],
+    "flmm_scan_rotate_phenos": [_p, _p, _i64, _i, _p],
+    "flmm_scan_fit_delta": [_p, _i, _p, _p],
+    "flmm_scan_wald": [_p, _i, _p, _i64, _i, _p, _i, _p, _p, _p, _p, _p, _i64, _p, _p],
+    "flmm_scan_run": [_p, _p, _i64, _i, _p, _i, _p, _p, _p, _p, _p, _i64, _p, _p, _p],
     "flmm_convert_f64_f32": [_i64, _p, _p, _p],
     "flmm_accumulate_f32_f64": [_i64, _p, _p, _p],
     "flmm_loco_kinship_f32": [_p, _p, _i, _d, _p, _p],
 }
 _RESTYPE = {"flmm_status_string": C.c_char_p, "flmm_last_error": C.c_char_p, "flmm_kernel_launches": C.c_uint64}
+
+
+class ScanOpts(C.Structure):
+    """flmm_scan_opts of include/fasterlmm_gb300.h."""
+    _fields_ = [("n_grid", C.c_int), ("log_delta_min", C.c_double), ("log_delta_max", C.c_double),
+                ("refine", C.c_int), ("eigh_refine_steps", C.c_int), ("f_refine", C.c_double), ("pipeline", C.c_int)]
 
 
 class FlmmError(RuntimeError):

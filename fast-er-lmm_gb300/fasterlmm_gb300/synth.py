@@ -96,14 +96,20 @@ def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19
         G[miss] = MISSING
     X = np.concatenate([np.ones((N, 1)), rng.standard_normal((N, D - 1))], axis=1)
 
-    # per-variant stats over observed calls, used only to standardise the causal columns
-    Gf = G.astype(np.float64)
+    # per-variant stats over observed calls, used only to standardise the causal columns (in column blocks, so the
+    # FP64 copy never holds more than `step` columns)
     obs = G != MISSING
-    n_obs = np.maximum(obs.sum(axis=0), 1)
-    mu = np.where(obs, Gf, 0.0).sum(axis=0) / n_obs
-    sd = np.sqrt(np.where(obs, (Gf - mu) ** 2, 0.0).sum(axis=0) / n_obs)
+    mu = np.empty(M)
+    sd = np.empty(M)
+    for j0 in range(0, M, step):
+        j1 = min(M, j0 + step)
+        Gf = G[:, j0:j1].astype(np.float64)
+        ob = obs[:, j0:j1]
+        n_obs = np.maximum(ob.sum(axis=0), 1)
+        m = np.where(ob, Gf, 0.0).sum(axis=0) / n_obs
+        mu[j0:j1] = m
+        sd[j0:j1] = np.sqrt(np.where(ob, (Gf - m) ** 2, 0.0).sum(axis=0) / n_obs)
     sd = np.clip(sd, 1e-12, None)
-    del Gf
 
     h2 = rng.uniform(h2_lo, h2_hi, size=B)
     n_causal = rng.integers(k_lo, k_hi + 1, size=B)
@@ -142,6 +148,13 @@ WORKLOADS = {
     "n1000_m100k_b6484_perm10": dict(N=1000, M=100_000, n_chrom=20, D=5, B=6484, n_perm=10, n_grid=64,
                                      log_delta_min=-10.0, log_delta_max=10.0,
                                      gen=dict(maf_lo=0.01, h2_lo=0.0, h2_hi=0.9, k_lo=0, k_hi=50, config_id=2)),
+    # uneven batching: 5,000 samples x 500,000 variants over 22 chromosomes sized like the human autosomes, 2,000
+    # phenotypes in 12 missingness patterns (each pattern but the first drops up to 40 % of the samples, so groups
+    # have 3,000-5,000 samples); the first 50 phenotypes get 1,000 permutations (n_perm_hi), the rest 10
+    "n5000_m500k_b2000_na12": dict(N=5000, M=500_000, n_chrom=22, D=5, B=2000, n_perm=10, n_grid=64,
+                                   log_delta_min=-10.0, log_delta_max=10.0, B_hi=50, n_perm_hi=1000, human=True,
+                                   gen=dict(maf_lo=0.01, h2_lo=0.0, h2_hi=0.9, k_lo=0, k_hi=50, config_id=3,
+                                            pheno_na_patterns=12, na_frac_hi=0.4)),
 }
 
 
@@ -153,5 +166,7 @@ def make_workload(name: str, *, seed: int = 19930909, B: int | None = None, M: i
         w["B"] = B
     if M is not None:
         w["M"] = M
+    if w.get("human"):
+        gen["chrom_sizes"] = chrom_sizes_human(w["M"], w["n_chrom"])
     data = make_dataset(w["N"], w["M"], w["n_chrom"], w["D"], w["B"], seed=seed, **gen)
     return data, w

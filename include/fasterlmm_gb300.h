@@ -295,6 +295,60 @@ int flmm_convert_f64_f32(int64_t n, const double* x, float* y, void* stream);
 int flmm_accumulate_f32_f64(int64_t n, const float* x, double* y, void* stream);
 int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_loco, double* K, void* stream);
 
+/* ---- scan-level entry points (fasterlmm/perms.py:21-68 -> fasterlmm/core.py:677-726) -----------------------------
+ *
+ * The whole fast-form LOCO scan behind a handful of calls, for callers that bind the library directly (the reference
+ * binds the Python functions by name; these are what an FFI binding of that path would call).  A scan object is
+ * bound to one device and owns its working buffers; inputs and outputs are caller-owned device pointers, every call
+ * takes a stream (0 = the legacy default stream) and returns a status.  Order: create, group_prepare (once per
+ * sample group: covariates and kinship panel), rotate_phenos (once per batch of scan columns), then either run (every
+ * chromosome, pipelined) or fit_delta(k) followed by wald(k) per chromosome; destroy.
+ *
+ * flmm_scan_opts: delta grid (n_grid points on [log_delta_min, log_delta_max], refine != 0: exact refinement of the
+ * grid argmin; fasterlmm/core.py:561-595), eigh_refine_steps (0: 2 up to N = 2,000, 3 above), f_refine (real tests
+ * with F above it are recomputed without the FP32 cancellation; <= 0: off), pipeline (!= 0: the column side of
+ * chromosome k + 1 runs on a second stream beside the variant side of chromosome k). */
+typedef struct flmm_scan flmm_scan;
+typedef struct flmm_scan_opts {
+    int n_grid;
+    double log_delta_min;
+    double log_delta_max;
+    int refine;
+    int eigh_refine_steps;
+    double f_refine;
+    int pipeline;
+} flmm_scan_opts;
+int flmm_scan_opts_default(flmm_scan_opts* opts);
+int flmm_scan_create(int device, int N, int D, const flmm_scan_opts* opts, flmm_scan** out);
+int flmm_scan_destroy(flmm_scan* scan);
+/* Covariates X (N, D) row-major and the kinship panel Zt_kin (M_kin, ldz) standardised, variant-major, with host
+ * chromosome labels chrom_kin (M_kin,); loco_chroms (host, n_units) lists the chromosomes to scan, each with the
+ * kinship of the panel without that chromosome (fasterlmm/core.py:707-713); n_units = 0 prepares one unit with the
+ * whole panel's kinship (single-K, fasterlmm/core.py:729-740).  Forms the covariate basis, the per-chromosome Grams,
+ * the projected LOCO kinships and their refined eigendecompositions; returns after the device work is done. */
+int flmm_scan_group_prepare(flmm_scan* scan, const double* X, const double* Zt_kin, int64_t ldz, int M_kin,
+                            const int32_t* chrom_kin, const int32_t* loco_chroms, int n_units, void* stream);
+/* Scan columns Yt (P, ldy) row-major (the real phenotypes first, then their permutations; fasterlmm/perms.py:56-59),
+ * regressed off the covariates and split for the tensor cores.  Returns after the device work is done. */
+int flmm_scan_rotate_phenos(flmm_scan* scan, const double* Yt, int64_t ldy, int P, void* stream);
+/* Column side of unit k (the k-th prepared chromosome): UY = U_eff^T Y_r and the fast delta fit; log_delta_out (P,)
+ * device, may be NULL.  Must precede flmm_scan_wald(k); units k and k + 2 share buffers. */
+int flmm_scan_fit_delta(flmm_scan* scan, int unit, double* log_delta_out, void* stream);
+/* Variant side of unit k: the chromosome's standardised variants Zt_c (Mc, ldz), their output rows rows (Mc,) int64
+ * device; fused Wald scan into f, beta, se, sfve, nullh2 (nullh2 may be NULL) at out[rows[m] * ldo + p] for the
+ * n_real real columns, max_F (P,) raised to the column maxima (fasterlmm/core.py:601-671). */
+int flmm_scan_wald(flmm_scan* scan, int unit, const double* Zt_c, int64_t ldz, int Mc, const int64_t* rows,
+                   int n_real, double* f, double* beta, double* se, double* sfve, double* nullh2, int64_t ldo,
+                   double* max_F, void* stream);
+/* Every unit: tested variants Zt (M, ldz) standardised, variant-major, with host chromosome labels chrom (M,); unit k
+ * scans the variants of its chromosome (all variants for a single-K unit); outputs (M, n_real) at ldo, max_F (P,)
+ * (set to -inf first), log_delta_out (n_units, P) device or NULL.  The column side of unit k + 1 runs on the scan's
+ * second stream while the variant side of unit k runs on `stream` (opts.pipeline).  Returns after the device work
+ * is done, FLMM_ERR_TIMEOUT if a bounded device wait gave up. */
+int flmm_scan_run(flmm_scan* scan, const double* Zt, int64_t ldz, int M, const int32_t* chrom, int n_real,
+                  double* f, double* beta, double* se, double* sfve, double* nullh2, int64_t ldo, double* max_F,
+                  double* log_delta_out, void* stream);
+
 /* ---- PLINK .bed input (fasterlmm/io.py:54-67, fasterlmm/io_stream.py:60-71) ------------------------------------
  *
  * Decode n_variants SNP-major .bed records (each bytes_per_variant = ceil(n_fam / 4) bytes, header stripped) into
