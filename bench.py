@@ -191,25 +191,6 @@ def run_reference(args):
         tests.append(n)
     value = sum(tests) / sum(times)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    iso = isolated_stages(args, step, w) if (args.form == "fast" and rank == 0) else None
-    delta_roof = None
-    if iso and iso.get("delta"):
-        # per chromosome: the FP32 grid product (G x Neff) x (Neff x P), 2 flop per term, and the Newton passes,
-        # ~30 FP32 operations per element for each of ~4.5 evaluations of a column
-        d_s = iso["delta"] / w["n_chrom"] / 1e3
-        grid_flop = 2.0 * w["n_grid"] * Neff * P
-        newton_flop = 30.0 * 4.5 * Neff * P
-        fp32_peak = fp32_peak_tflops()
-        delta_roof = {"kernels": "k_grid_argmin_f32 + k_newton_refine (FP32 pipe)", "ms_per_chromosome": 1e3 * d_s,
-                      "algorithmic_flop": grid_flop + newton_flop, "grid_flop": grid_flop,
-                      "achieved_tflops": (grid_flop + newton_flop) / d_s / 1e12, "peak_tflops": fp32_peak,
-                      "frac": (grid_flop + newton_flop) / d_s / 1e12 / fp32_peak,
-                      "peak_source": "nominal FP32 CUDA-core rate: SMs x 128 lanes x 2 flop x max SM clock",
-                      "timed": "one untimed step with the delta fit on the main stream (not overlapped)"}
-    plain = None
-    if rank == 0 and world == 1 and args.form == "fast" and not args.no_plain:
-        plain = plain_comparison(args, d, w, grid_kw)
-
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
