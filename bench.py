@@ -13,7 +13,7 @@ device; ``e2e`` times the same call with host (pinned) inputs and host outputs, 
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast|plain] [--impl ours|reference]
                   [--delta grid|learned] [--no-pipeline] [--B B] [--M M] [--no-e2e] [--no-cpu-baseline]
-                  [--no-plain] [--plain-chroms C]
+                  [--no-plain] [--plain-chroms C] [--workload headline|c3]
 
 Besides ``value`` and ``e2e`` the line carries the metric's own ratio (``chosen_vs_plain``: the plain FP64 form and
 the chosen form timed on the same bounded subset of the workload, its first C chromosomes), the real-only rate,
@@ -22,6 +22,10 @@ times of one step with nothing overlapped.
 
 ``--delta learned`` switches the fast form's delta fit to the learned proposal's narrow bracket; ``--no-pipeline``
 runs each chromosome's delta fit on the main stream instead of one chromosome ahead on a side stream.
+
+``--workload c3`` runs the uneven-batching shape instead: 5,000 samples x 500,000 variants over 22 chromosomes of
+human proportions, 2,000 phenotypes in 12 missingness patterns (groups of 3,000-5,000 samples), 1,000 permutations
+for 50 phenotypes and 10 for the rest, every group on its own strain subset (fasterlmm_gb300.groups).
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm (oracle/flmm_oracle.py) on the host's
 cores on a bounded sample of the same workload (one chromosome x one 256-phenotype batch per step).
@@ -133,9 +137,15 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "tensor_tflops": 1900.0, "tensor_tflops_sustained": 1700.0, "source": "fallback"}
 
 
-def make_inputs(B: int | None, M: int | None):
+# --workload: the headline shape, or the uneven-batching shape (5,000 samples x 500,000 variants over 22
+# human-sized chromosomes, 2,000 phenotypes in 12 missingness patterns, 1,000 permutations for 50 of them and 10
+# for the rest)
+WORKLOADS = {"headline": WORKLOAD, "c3": "n5000_m500k_b2000_na12"}
+
+
+def make_inputs(B: int | None, M: int | None, name: str = WORKLOAD):
     from fasterlmm_gb300.synth import make_workload
-    d, w = make_workload(WORKLOAD, B=B, M=M)
+    d, w = make_workload(name, B=B, M=M)
     return d, w
 
 
@@ -359,6 +369,106 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_grouped(args):
+    """
+    The uneven-batching workload: every missingness group scanned on its own strain subset through
+    fasterlmm_gb300.groups.perm_threshold_grouped, each group's two permutation counts in one joint scan.  One step =
+    the whole grouped permutation scan; inputs on the device (int8 dosages uploaded and widened there once).
+    """
+    import torch
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from fasterlmm_gb300 import _lib, build, fast
+    from fasterlmm_gb300.groups import group_by_na, perm_threshold_grouped
+    build()
+    if args.no_pipeline:
+        fast.PIPELINE = False
+    name = WORKLOADS[args.workload]
+    t_gen = time.perf_counter()
+    d, w = make_inputs(args.B, args.M, name)
+    t_gen = time.perf_counter() - t_gen
+    N, M, B, n_perm, D = w["N"], w["M"], w["B"], w["n_perm"], w["D"]
+    n_perm_of = {b: w["n_perm_hi"] for b in range(min(w.get("B_hi", 0), B))}
+    groups = [(keep, cols) for keep, cols in group_by_na(d.Y, range(B)) if len(keep) - D - 1 >= 1]
+    P_of = [sum(1 + n_perm_of.get(b, n_perm) for b in cols) for _, cols in groups]
+    tests_per_step = M * sum(P_of)
+    grid_kw = dict(n_grid=w["n_grid"], log_delta_min=w["log_delta_min"], log_delta_max=w["log_delta_max"])
+    G = torch.from_numpy(d.G).to(dev)
+    Z = G.to(torch.float64)
+    Z[G < 0] = float("nan")
+    del G
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    data_dev = SimpleNamespace(Z=Z, Y=t(d.Y), X=t(d.X), chrom=d.chrom, Z_kin=None, chrom_kin=None)
+
+    def step(tm=None):
+        return perm_threshold_grouped(data_dev, list(range(B)), n_perm=n_perm, n_perm_of=n_perm_of, form=args.form,
+                                      timers=tm, **grid_kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    launches0 = _lib.kernel_launches()
+    timers: dict = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = step(timers)
+        del out
+    ev1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    launches = _lib.kernel_launches() - launches0
+    clk = clocks.stop()
+    elapsed = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    value = world * tests_per_step * args.steps / elapsed
+    stages = {k: round(sum(a.elapsed_time(b) for a, b in v if b is not None) / args.steps, 3)
+              for k, v in timers.items()}
+    # the fused Wald launches of a step: 4 Neff_g P_g Mc algorithmic flop each, summed over groups and chromosomes
+    peaks = measured_peaks()
+    wald_s = sum(a.elapsed_time(b) for a, b in timers.get("wald", []) if b is not None) / 1e3 / args.steps
+    wald_flop = sum(4.0 * (len(keep) - D) * Pg * M for (keep, _), Pg in zip(groups, P_of))
+    roof = None
+    if wald_s > 0:
+        ach = wald_flop / wald_s / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peaks["tensor_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["tensor_tflops"], "traffic": None,
+                "kernel": "k_pair<2> (fused split-FP16 Wald, tcgen05 CTA pairs), all launches of a step",
+                "wald_ms_per_step": 1e3 * wald_s, "algorithmic_flop_per_step": wald_flop,
+                "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp16x2-split tensor (FP32 acc) + f64" if args.form == "fast" else "f64",
+            "data": "synthetic (seeded: Binomial(2, MAF~U[0.01,0.5]) genotypes, RINT phenotypes, 0-50 causal, "
+                    f"{len(groups)} missingness patterns)",
+            "config": {"workload": name, "N": N, "M": M, "B": B, "n_perm": n_perm,
+                       "n_perm_hi": w.get("n_perm_hi"), "B_hi": len(n_perm_of), "chromosomes": w["n_chrom"],
+                       "covariates": D, "grid": w["n_grid"], "form": args.form,
+                       "groups": [{"samples": len(keep), "phenotypes": len(cols), "columns": Pg}
+                                  for (keep, cols), Pg in zip(groups, P_of)],
+                       "columns": sum(P_of), "pipelined_delta_fit": bool(fast.PIPELINE),
+                       "l2": "inputs larger than L2 (Z 20 GB FP64)",
+                       "parallelism": f"{world} replica(s), no cross-GPU exchange"},
+            "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "stage_ms_per_step": stages,
+            "generate_s": round(t_gen, 1), "e2e": None, "cpu_baseline": None,
+            "notes": "device-resident inputs; no e2e leg and no CPU sample for this shape (one N=5,000 LOCO GRM "
+                     "alone is ~2e13 flop on the host)",
+            "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def fp32_peak_tflops() -> float:
     import torch
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
@@ -474,9 +584,13 @@ def main():
                     help="skip the plain FP64 form's bounded run (the denominator of the chosen-vs-plain ratio)")
     ap.add_argument("--plain-chroms", type=int, default=2,
                     help="chromosomes of the workload that the plain-form comparison scans (default 2 of 20)")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
+                    help="headline: 1,000 x 100,000 x 6,484 phenotypes; c3: the uneven-batching shape")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "headline":
+        run_grouped(args)
     else:
         run_ours(args)
 

@@ -56,6 +56,32 @@ def rint_columns(Y: np.ndarray, c: float = 3.0 / 8.0) -> np.ndarray:
     return out
 
 
+def _for_blocks(fn, starts, threads: int) -> None:
+    """fn(j0) for every block start, on ``threads`` host threads (numpy releases the GIL in the block work)."""
+    starts = list(starts)
+    if threads <= 1:
+        for j0 in starts:
+            fn(j0)
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(fn, starts))
+
+
+def _bernoulli_pair_blocks(G: np.ndarray, maf: np.ndarray, step: int, key: tuple, threads: int) -> None:
+    N, M = G.shape
+
+    def draw(j0):
+        j1 = min(M, j0 + step)
+        r = np.random.Generator(np.random.PCG64(np.random.SeedSequence([*key, 1, j0 // step])))
+        p = maf[j0:j1]
+        blk = (r.random((N, j1 - j0)) < p).astype(np.int8)
+        blk += (r.random((N, j1 - j0)) < p).astype(np.int8)
+        G[:, j0:j1] = blk
+
+    _for_blocks(draw, range(0, M, step), threads)
+
+
 def chrom_sizes_even(M: int, n_chrom: int) -> list[int]:
     base, extra = divmod(M, n_chrom)
     return [base + (1 if i < extra else 0) for i in range(n_chrom)]
@@ -71,11 +97,15 @@ def chrom_sizes_human(M: int, n_chrom: int = 22) -> list[int]:
 def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19930909, config_id: int = 0,
                  maf_lo: float = 0.05, h2_lo: float = 0.1, h2_hi: float = 0.8, k_lo: int = 5, k_hi: int = 5,
                  chrom_sizes: list[int] | None = None, geno_missing_rate: float = 0.0,
-                 pheno_na_patterns: int = 0, na_frac_hi: float = 0.4, rint: bool = True) -> SynthData:
+                 pheno_na_patterns: int = 0, na_frac_hi: float = 0.4, rint: bool = True,
+                 block_threads: int = 0) -> SynthData:
     """
     Draw one synthetic dataset.
 
     Genotypes: Binomial(2, p_j) with p_j ~ U[maf_lo, 0.5]; optional missing calls at ``geno_missing_rate``.
+    ``block_threads`` > 0 draws them instead as two Bernoulli(p_j) uniforms per call, each block of 8,192 variants
+    from its own PCG64 stream (SeedSequence [seed, config_id, 1, block]) on that many host threads -- the same
+    distribution, ~50x faster for the 2.5e9-call workload, independent of the thread count.
     Covariates: intercept plus D - 1 standard normals.  Phenotypes: k ~ U{k_lo..k_hi} causal variants, effects
     N(0, 1), genetic value rescaled to variance h2 (h2 ~ U[h2_lo, h2_hi]; k = 0 or h2 = 0 gives no genetic part),
     noise N(0, 1 - h2), then RINT.  ``pheno_na_patterns`` > 0 assigns each phenotype one of that many missingness
@@ -88,9 +118,12 @@ def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19
     maf = rng.uniform(maf_lo, 0.5, size=M)
     G = np.empty((N, M), dtype=np.int8)
     step = 8192
-    for j0 in range(0, M, step):
-        j1 = min(M, j0 + step)
-        G[:, j0:j1] = rng.binomial(2, maf[j0:j1], size=(N, j1 - j0)).astype(np.int8)
+    if block_threads > 0:
+        _bernoulli_pair_blocks(G, maf, step, (seed, config_id), block_threads)
+    else:
+        for j0 in range(0, M, step):
+            j1 = min(M, j0 + step)
+            G[:, j0:j1] = rng.binomial(2, maf[j0:j1], size=(N, j1 - j0)).astype(np.int8)
     if geno_missing_rate > 0:
         miss = rng.random((N, M)) < geno_missing_rate
         G[miss] = MISSING
@@ -101,7 +134,8 @@ def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19
     obs = G != MISSING
     mu = np.empty(M)
     sd = np.empty(M)
-    for j0 in range(0, M, step):
+
+    def stats(j0):
         j1 = min(M, j0 + step)
         Gf = G[:, j0:j1].astype(np.float64)
         ob = obs[:, j0:j1]
@@ -109,6 +143,8 @@ def make_dataset(N: int, M: int, n_chrom: int, D: int, B: int, *, seed: int = 19
         m = np.where(ob, Gf, 0.0).sum(axis=0) / n_obs
         mu[j0:j1] = m
         sd[j0:j1] = np.sqrt(np.where(ob, (Gf - m) ** 2, 0.0).sum(axis=0) / n_obs)
+
+    _for_blocks(stats, range(0, M, step), block_threads)
     sd = np.clip(sd, 1e-12, None)
 
     h2 = rng.uniform(h2_lo, h2_hi, size=B)
@@ -154,7 +190,7 @@ WORKLOADS = {
     "n5000_m500k_b2000_na12": dict(N=5000, M=500_000, n_chrom=22, D=5, B=2000, n_perm=10, n_grid=64,
                                    log_delta_min=-10.0, log_delta_max=10.0, B_hi=50, n_perm_hi=1000, human=True,
                                    gen=dict(maf_lo=0.01, h2_lo=0.0, h2_hi=0.9, k_lo=0, k_hi=50, config_id=3,
-                                            pheno_na_patterns=12, na_frac_hi=0.4)),
+                                            pheno_na_patterns=12, na_frac_hi=0.4, block_threads=16)),
 }
 
 

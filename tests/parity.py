@@ -16,6 +16,8 @@ import numpy as np
 
 DETAIL = ("f", "beta", "se", "sfve", "nullh2")
 RTOL = 1e-5
+# the -log10 p gate of the strong-signal and NaN-group tests: half of the 1e-3 parity bound
+GATE = 5e-4
 ATOL = {"f": 1e-5, "beta": 1e-6, "se": 1e-6, "sfve": 1e-6, "nullh2": 1e-6, "max_F": 1e-5, "perm_max_F": 1e-5}
 
 
@@ -78,3 +80,45 @@ def assert_log_delta_equivalent_gls(ld, ld_ref, s, X_rot, Y_rot, *, reml: bool =
     bad = ~(close | (La <= Lb + loss_rtol * np.abs(Lb)))
     assert not bad.any(), (f"{bad.sum()} log delta values neither close nor loss-equivalent; got {ld[bad][:5]}, "
                            f"ref {ld_ref[bad][:5]}, dloss {(La - Lb)[bad][:5]}")
+
+
+def neg_log10_p_gpu(F, df2):
+    """-log10 p of F statistics by the library's own kernel (the scan's p-value path)."""
+    import torch
+    from fasterlmm_gb300.post import neg_log10_pvalue
+    return neg_log10_pvalue(torch.from_numpy(np.ascontiguousarray(F)).cuda(), df2).cpu().numpy()
+
+
+def check_gates(got: dict, want: dict, df2: int, label: str, gate: float = None) -> float:
+    """
+    The strong-signal gates: beta and SE within rtol 1e-5 / atol 1e-6, |d(-log10 p)| <= gate on every real test,
+    each column's ten strongest variants in the same order (a swap is a tie within the gate), permutation maxima
+    within 1e-4 in -log10 p, the 0.05-quantile permutation threshold (fasterlmm/cli.py:128) within 1e-4, and the same
+    significance calls except within the gate of the threshold.  Returns the largest |d(-log10 p)|.
+    """
+    gate = GATE if gate is None else gate
+    for k in ("beta", "se"):
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-5, atol=1e-6, err_msg=f"{label} {k}")
+    gp, wp = neg_log10_p_gpu(got["f"], df2), neg_log10_p_gpu(want["f"], df2)
+    err = np.abs(gp - wp)
+    worst = np.unravel_index(np.argmax(err), err.shape)
+    assert err.max() <= gate, f"{label}: |d(-log10 p)| {err.max():.3e} at F = {want['f'][worst]:.1f}"
+    # each phenotype's ten strongest variants, in order (a swap is a tie: the reference's values within the gate)
+    for j in range(gp.shape[1]):
+        tg = np.argsort(-gp[:, j], kind="stable")[:10]
+        tw = np.argsort(-wp[:, j], kind="stable")[:10]
+        d = tg != tw
+        assert np.all(np.abs(wp[tg[d], j] - wp[tw[d], j]) <= gate), (label, j)
+    # permutation thresholds and significance calls
+    gq, wq = neg_log10_p_gpu(got["perm_max_F"], df2), neg_log10_p_gpu(want["perm_max_F"], df2)
+    assert np.abs(gq - wq).max() <= 1e-4, label
+    for j in range(gp.shape[1]):
+        tg = -np.log10(np.quantile(10.0 ** -gq[j], 0.05))
+        tw = -np.log10(np.quantile(10.0 ** -wq[j], 0.05))
+        assert abs(tg - tw) <= 1e-4, (label, j, tg, tw)
+        sg, sw = gp[:, j] > tg, wp[:, j] > tw
+        d = sg != sw
+        assert np.all(np.abs(wp[d, j] - tw) <= gate), (label, j, int(d.sum()))
+    rb = np.abs(got["beta"] - want["beta"]) / np.maximum(np.abs(want["beta"]), 1e-6)
+    print(f"{label}: max F {want['f'].max():.0f}, max |d(-log10 p)| {err.max():.2e}, max rel d(beta) {rb.max():.2e}")
+    return float(err.max())

@@ -76,3 +76,36 @@ def strong_dataset(N: int, sizes: list[int], D: int, specs: list[tuple[float, in
 N5000 = dict(N=5000, sizes=[3000, 3000, 3000], D=3,
              specs=[(0.95, 1, 1), (0.8, 1, 2), (0.9, 2, 3), (0.5, 10, 1), (0.3, 40, 2), (0.0, 0, 1)],
              seed=20250611, n_perm=10)
+
+
+def na_patterns(N: int, B: int, n_patterns: int, *, frac_lo: float, frac_hi: float, seed: int) -> np.ndarray:
+    """
+    (B, N) bool missingness of each phenotype: pattern b % n_patterns, pattern 0 complete, pattern p > 0 drops each
+    sample with a probability drawn from U[frac_lo, frac_hi] (raw uniforms of its own PCG64 stream).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    masks = [np.zeros(N, dtype=bool)]
+    for _ in range(n_patterns - 1):
+        frac = frac_lo + (frac_hi - frac_lo) * rng.random()
+        masks.append(rng.random(N) < frac)
+    return np.stack([masks[b % n_patterns] for b in range(B)])
+
+
+# The NaN-group case of the golden fixture na_groups_n1600: 1,600 samples in four missingness patterns (groups of
+# about 1,000 to 1,600 samples), four chromosomes of 600-1,200 variants, twelve phenotypes, five permutations each
+# except three phenotypes with forty (the uneven permutation counts of a mixed batch).
+NA1600 = dict(N=1600, sizes=[1200, 1000, 800, 600], D=3,
+              specs=[(0.9, 1, 1), (0.6, 3, 2), (0.5, 10, 3), (0.3, 20, 4), (0.8, 1, 2), (0.2, 5, 1),
+                     (0.0, 0, 3), (0.7, 2, 4), (0.4, 8, 1), (0.5, 1, 3), (0.6, 15, 2), (0.1, 3, 4)],
+              seed=16001600, na_seed=7700, n_patterns=4, frac_lo=0.1, frac_hi=0.35, n_perm=5,
+              n_perm_of={0: 40, 5: 40, 10: 40})
+
+
+def na_dataset(c: dict = NA1600):
+    """(G, X, Y with NaN, chrom) of a NaN-group case."""
+    G, X, Y, chrom = strong_dataset(c["N"], c["sizes"], c["D"], c["specs"], seed=c["seed"])
+    miss = na_patterns(c["N"], Y.shape[1], c["n_patterns"], frac_lo=c["frac_lo"], frac_hi=c["frac_hi"],
+                       seed=c["na_seed"])
+    Y = Y.copy()
+    Y[miss.T] = np.nan
+    return G, X, Y, chrom

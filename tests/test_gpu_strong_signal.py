@@ -27,11 +27,11 @@ import torch
 
 import flmm_oracle as orc
 from conftest import GOLDEN
+from parity import GATE, check_gates, neg_log10_p_gpu
 from strong_inputs import N5000, genotype_checksum, strong_dataset
 
 pytestmark = pytest.mark.gpu
 
-GATE = 5e-4
 SPECS_1000 = [(0.95, 1, 1), (0.9, 1, 2), (0.8, 1, 3), (0.95, 2, 1), (0.6, 3, 2), (0.5, 10, 3), (0.3, 40, 1),
               (0.0, 0, 2)]
 
@@ -45,39 +45,6 @@ def _run_fast(G, X, Y, chrom, n_perm):
     out = {k: getattr(res, k).cpu().numpy() for k in ("f", "beta", "se", "sfve", "max_F")}
     out["perm_max_F"] = pmf.cpu().numpy()
     return out
-
-
-def _nl10(F, df2):
-    from fasterlmm_gb300.post import neg_log10_pvalue
-    return neg_log10_pvalue(torch.from_numpy(np.ascontiguousarray(F)).cuda(), df2).cpu().numpy()
-
-
-def _check(got, want, df2, label):
-    for k in ("beta", "se"):
-        np.testing.assert_allclose(got[k], want[k], rtol=1e-5, atol=1e-6, err_msg=f"{label} {k}")
-    gp, wp = _nl10(got["f"], df2), _nl10(want["f"], df2)
-    err = np.abs(gp - wp)
-    worst = np.unravel_index(np.argmax(err), err.shape)
-    assert err.max() <= GATE, f"{label}: |d(-log10 p)| {err.max():.3e} at F = {want['f'][worst]:.1f}"
-    # each phenotype's ten strongest variants, in order (a swap is a tie: the reference's values within the gate)
-    for j in range(gp.shape[1]):
-        tg = np.argsort(-gp[:, j], kind="stable")[:10]
-        tw = np.argsort(-wp[:, j], kind="stable")[:10]
-        d = tg != tw
-        assert np.all(np.abs(wp[tg[d], j] - wp[tw[d], j]) <= GATE), (label, j)
-    # permutation thresholds and significance calls
-    gq, wq = _nl10(got["perm_max_F"], df2), _nl10(want["perm_max_F"], df2)
-    assert np.abs(gq - wq).max() <= 1e-4, label
-    for j in range(gp.shape[1]):
-        tg = -np.log10(np.quantile(10.0 ** -gq[j], 0.05))
-        tw = -np.log10(np.quantile(10.0 ** -wq[j], 0.05))
-        assert abs(tg - tw) <= 1e-4, (label, j, tg, tw)
-        sg, sw = gp[:, j] > tg, wp[:, j] > tw
-        d = sg != sw
-        assert np.all(np.abs(wp[d, j] - tw) <= GATE), (label, j, int(d.sum()))
-    rb = np.abs(got["beta"] - want["beta"]) / np.maximum(np.abs(want["beta"]), 1e-6)
-    print(f"{label}: max F {want['f'].max():.0f}, max |d(-log10 p)| {err.max():.2e}, max rel d(beta) {rb.max():.2e}")
-    return float(err.max())
 
 
 def _case_1000(rint: bool):
@@ -102,13 +69,13 @@ def case_raw():
 def test_strong_single_variant_n1000_rint(case_rint):
     *_, got, ref = case_rint
     assert ref["f"].max() > 2000  # the case does reach the tight end of the gate
-    _check(got, ref, 1000 - 5 - 1, "N=1000 RINT")
+    check_gates(got, ref, 1000 - 5 - 1, "N=1000 RINT")
 
 
 def test_strong_single_variant_n1000_raw(case_raw):
     *_, got, ref = case_raw
     assert ref["f"].max() > 10000
-    _check(got, ref, 1000 - 5 - 1, "N=1000 raw")
+    check_gates(got, ref, 1000 - 5 - 1, "N=1000 raw")
 
 
 def test_reevaluation_is_what_closes_the_gate(case_raw):
@@ -122,8 +89,8 @@ def test_reevaluation_is_what_closes_the_gate(case_raw):
     finally:
         fast.REFINE_F = saved
     df2 = 1000 - 5 - 1
-    e_with = np.abs(_nl10(got["f"], df2) - _nl10(ref["f"], df2)).max()
-    e_without = np.abs(_nl10(plain["f"], df2) - _nl10(ref["f"], df2)).max()
+    e_with = np.abs(neg_log10_p_gpu(got["f"], df2) - neg_log10_p_gpu(ref["f"], df2)).max()
+    e_without = np.abs(neg_log10_p_gpu(plain["f"], df2) - neg_log10_p_gpu(ref["f"], df2)).max()
     print(f"max |d(-log10 p)|: {e_without:.3e} without the re-evaluation, {e_with:.3e} with it")
     assert e_with < e_without and e_without > GATE
 
@@ -152,4 +119,4 @@ def test_strong_signals_n5000_against_reference_golden():
     np.testing.assert_allclose(Y, want["Y"], rtol=0, atol=1e-12)
     got = _run_fast(G, X, Y, chrom, c["n_perm"])
     assert want["f"].max() > 5000
-    _check(got, want, c["N"] - c["D"] - 1, "N=5000")
+    check_gates(got, want, c["N"] - c["D"] - 1, "N=5000")
