@@ -21,6 +21,11 @@ int check_cuda(const char* what);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// The library's own batched FP32 eigensolver (csrc/flmm_eigh_own.cu): A (batch, N, N) symmetric in, one eigenvector
+// per row out, evals (batch, N) ascending; work of eigh_own_workspace_bytes(N, batch) bytes.
+size_t eigh_own_workspace_bytes(int N, int batch);
+int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStream_t st);
+
 inline unsigned ceil_div(int64_t a, int64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 
 #define FLMM_REQUIRE(cond, ...)                                                       \

@@ -181,6 +181,7 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
     const EvalPoint pb = eval_point(grid[inner ? i + 1 : i], sbar);
     EvalSums t, ta, tb;
     float uh = 0.f, uc = 0.f;
+#pragma unroll 4
     for (int n = lane; n < Neff; n += 32) {
         const float un = u[n];
         const float uu = un * un;

@@ -1,0 +1,576 @@
+// Batched FP32 symmetric eigendecomposition of the projected LOCO kinships (N up to kOwnMaxN), the fast form's
+// replacement for the library's batched eigensolver.  The reference decomposes each kinship in FP64
+// (fasterlmm/core.py:54-77, torch.linalg.eigh); the fast form takes an FP32 decomposition and refines it
+// (flmm_eigh_refine_f32), so only FP32-quality eigenpairs are needed here.
+//
+// Four stages, all matrices of the batch side by side:
+//
+// 1. k_sytrd_cluster: Householder tridiagonalisation A = Q T Q^T, one thread-block cluster of kClusterCtas CTAs per
+//    matrix.  The FP32 matrix stays in global memory (L2-resident for the batch sizes used), rows dealt round-robin
+//    to the cluster's CTAs.  Column k's reflector is formed redundantly by every CTA from row k, each CTA computes
+//    p = tau W v for its rows, and the cluster exchanges p and the partial p^T v through distributed shared memory.
+//    The symmetric rank-2 update W -= v w^T + w v^T is applied lazily: row k+1 (the next pivot row) right away by its
+//    owner, every other row in the same pass that forms the next step's W v, so the trailing matrix is read and
+//    written once per column.  Both products of an update term are rounded before the add, so W stays exactly
+//    symmetric.  Two cluster barriers per column.
+// 2. k_tridiag_bisect: each eigenvalue of T by bisection on FP32 Sturm counts (ascending, by index).
+// 3. k_tridiag_invit: each eigenvector of T by inverse iteration in FP64 (LDL^T of T - lambda I with a pivot floor,
+//    five solves from a fixed pseudo-random start); eigenvalues closer than kClusterTol * ||T|| form a cluster whose
+//    vectors one thread computes in turn, each orthogonalised against the cluster's earlier vectors.
+// 4. k_wy_factors + k_backtransform: the reflectors in blocks of kWy as I - V T V^T (forward, columnwise), applied to
+//    column tiles of the eigenvector matrix of T held in shared memory, last block first; the result is written as
+//    one eigenvector per row.
+//
+// Every loop is bounded by N and fixed iteration counts; the only waits are cluster barriers that every CTA of the
+// cluster reaches on the same trip count.
+#include <math.h>
+#include <stdint.h>
+
+#include "flmm_common.cuh"
+
+using namespace flmm;
+
+namespace {
+
+constexpr int kClusterCtas = 8;
+constexpr int kSytrdThreads = 256;
+constexpr int kWy = 16;            // reflectors per WY block
+constexpr int kTile = 16;          // eigenvectors per back-transform CTA
+constexpr int kBtThreads = 256;
+constexpr int kChunk = 128;        // rows of a V block staged at a time in the back-transform
+constexpr int kInvitSolves = 5;
+constexpr double kClusterTol = 1e-5;
+constexpr int kBisectSteps = 48;
+
+__device__ __forceinline__ uint32_t cta_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_index() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// FP32 load from the shared memory of the cluster's CTA `rank` at the address of `p` in this CTA
+__device__ __forceinline__ float ld_remote(const float* p, uint32_t rank) {
+    uint32_t a;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_addr(p)), "r"(rank));
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+    return v;
+}
+
+// block-wide FP32 sum (all threads get it); red holds >= 32 floats
+__device__ float block_sum(float v, float* red) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    float t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0f;
+    if (wid == 0) t = warp_sum(t);
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    return red[0];
+}
+
+// W (batch, N, N) FP32 symmetric, full storage, overwritten: row k holds the reflector v_k on columns k+1..N-1
+// (v_k[k+1] = 1).  d (batch, N), e (batch, N), tau (batch, N): T's diagonal, off-diagonal (e[k] = T[k][k+1]) and the
+// reflector scalars (tau[N-2] = tau[N-1] = 0).
+__global__ void __launch_bounds__(kSytrdThreads)
+k_sytrd_cluster(float* __restrict__ W, int N, float* __restrict__ d_out, float* __restrict__ e_out,
+                float* __restrict__ tau_out) {
+    extern __shared__ float sm[];
+    const int Np = (N + 3) & ~3;
+    float* vbuf[2] = {sm, sm + Np};
+    float* wbuf[2] = {sm + 2 * Np, sm + 3 * Np};
+    float* pbuf[2] = {sm + 4 * Np, sm + 5 * Np};
+    float* red = sm + 6 * Np;        // 32 floats
+    float* part = red + 32;          // partial p^T v, one per parity
+    const int b = static_cast<int>(cluster_index());
+    const int r = static_cast<int>(cta_rank());
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = kSytrdThreads >> 5;
+    float* Wb = W + static_cast<int64_t>(b) * N * N;
+    for (int k = 0; k + 2 < N; ++k) {
+        const int cur = k & 1;
+        float* vc = vbuf[cur];
+        float* wc = wbuf[cur];
+        const float* vp = vbuf[cur ^ 1];
+        const float* wp = wbuf[cur ^ 1];
+        float* pb = pbuf[cur];
+        // (A) reflector of row k, which its owner brought up to date before the last barrier (read past L1: the row
+        // was written by another CTA)
+        const float* rowk = Wb + static_cast<int64_t>(k) * N;
+        float ss = 0.0f;
+        for (int j = k + 2 + threadIdx.x; j < N; j += kSytrdThreads) {
+            const float x = __ldcg(rowk + j);
+            vc[j] = x;
+            ss = fmaf(x, x, ss);
+        }
+        const float sigma = block_sum(ss, red);
+        const float alpha = __ldcg(rowk + k + 1);
+        const float dk = __ldcg(rowk + k);
+        float tau = 0.0f, beta = alpha, scal = 0.0f;
+        if (sigma > 0.0f) {
+            beta = -copysignf(sqrtf(fmaf(alpha, alpha, sigma)), alpha);
+            tau = (beta - alpha) / beta;
+            scal = 1.0f / (alpha - beta);
+        }
+        for (int j = k + 2 + threadIdx.x; j < N; j += kSytrdThreads) vc[j] *= scal;
+        if (threadIdx.x == 0) vc[k + 1] = 1.0f;
+        __syncthreads();
+        // (B) rows i > k of this CTA: the previous column's update (lazy), then p_i = tau * W[i, k+1:] . v
+        float dot = 0.0f;
+        int first = k + 1 + ((r - (k + 1)) % kClusterCtas + kClusterCtas) % kClusterCtas;
+        for (int i = first + wid * kClusterCtas; i < N; i += nw * kClusterCtas) {
+            float* row = Wb + static_cast<int64_t>(i) * N;
+            float acc = 0.0f;
+            if (k > 0) {
+                const float vi = vp[i], wi = wp[i];
+#pragma unroll 4
+                for (int j = k + 1 + lane; j < N; j += 32) {
+                    const float x = row[j] - (__fmul_rn(vi, wp[j]) + __fmul_rn(wi, vp[j]));
+                    row[j] = x;
+                    acc = fmaf(x, vc[j], acc);
+                }
+            } else {
+#pragma unroll 4
+                for (int j = k + 1 + lane; j < N; j += 32) acc = fmaf(row[j], vc[j], acc);
+            }
+            acc = warp_sum(acc);
+            const float pi = tau * acc;
+            if (lane == 0) pb[i] = pi;
+            dot = fmaf(pi, vc[i], dot);
+        }
+        // lanes of a warp hold the same dot (lane 0's rows are the warp's rows); sum one lane per warp
+        const float dsum = block_sum(lane == 0 ? dot : 0.0f, red);
+        if (threadIdx.x == 0) part[cur] = dsum;
+        cluster_barrier();  // B1: every CTA's p and partial p^T v are visible
+        // (C) w = p - (tau / 2) (p^T v) v over the whole trailing range
+        float s = 0.0f;
+        for (int q = 0; q < kClusterCtas; ++q) s += ld_remote(&part[cur], q);
+        const float c = -0.5f * tau * s;
+        for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads)
+            wc[j] = fmaf(c, vc[j], ld_remote(&pb[j], static_cast<uint32_t>(j % kClusterCtas)));
+        __syncthreads();
+        if ((k + 1) % kClusterCtas == r) {  // the next pivot row, updated now
+            float* row = Wb + static_cast<int64_t>(k + 1) * N;
+            const float vi = vc[k + 1], wi = wc[k + 1];
+            for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads)
+                row[j] -= __fmul_rn(vi, wc[j]) + __fmul_rn(wi, vc[j]);
+        }
+        if (r == 0) {  // row k is read by nobody after B1: it keeps the reflector
+            float* rowv = Wb + static_cast<int64_t>(k) * N;
+            for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads) rowv[j] = vc[j];
+            if (threadIdx.x == 0) {
+                d_out[static_cast<int64_t>(b) * N + k] = dk;
+                e_out[static_cast<int64_t>(b) * N + k] = beta;
+                tau_out[static_cast<int64_t>(b) * N + k] = tau;
+            }
+        }
+        cluster_barrier();  // B2: row k + 1 is visible; nobody reads this step's p any more
+    }
+    // the last column's update of row N-1 (rows <= N-2 are final), then the trailing 2 x 2 (or 1 x 1) block
+    if (N >= 3) {
+        const int last = (N - 3) & 1;
+        const float* vp = vbuf[last];
+        const float* wp = wbuf[last];
+        if ((N - 1) % kClusterCtas == r && threadIdx.x < 2) {
+            const int j = N - 2 + threadIdx.x;
+            float* row = Wb + static_cast<int64_t>(N - 1) * N;
+            row[j] -= __fmul_rn(vp[N - 1], wp[j]) + __fmul_rn(wp[N - 1], vp[j]);
+        }
+    }
+    cluster_barrier();
+    if (r == 0 && threadIdx.x == 0) {
+        float* d = d_out + static_cast<int64_t>(b) * N;
+        float* e = e_out + static_cast<int64_t>(b) * N;
+        float* t = tau_out + static_cast<int64_t>(b) * N;
+        if (N >= 2) {
+            d[N - 2] = __ldcg(Wb + static_cast<int64_t>(N - 2) * N + (N - 2));
+            e[N - 2] = __ldcg(Wb + static_cast<int64_t>(N - 2) * N + (N - 1));
+            t[N - 2] = 0.0f;
+        }
+        d[N - 1] = __ldcg(Wb + static_cast<int64_t>(N - 1) * N + (N - 1));
+        e[N - 1] = 0.0f;
+        t[N - 1] = 0.0f;
+    }
+    cluster_barrier();  // no CTA leaves while another may still read its shared memory
+}
+
+// ---- eigenvalues of T: bisection on Sturm counts ---------------------------------------------------------------
+
+// number of eigenvalues of T below x (FP32, pivots floored at pivmin in magnitude)
+__device__ __forceinline__ int sturm_count(const float* d, const float* e2, int N, float x, float pivmin) {
+    int cnt = 0;
+    float q = d[0] - x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    cnt += q < 0.0f;
+    for (int i = 1; i < N; ++i) {
+        q = (d[i] - x) - e2[i - 1] / q;
+        if (fabsf(q) < pivmin) q = -pivmin;
+        cnt += q < 0.0f;
+    }
+    return cnt;
+}
+
+// grid (ceil(N / 256), batch): eigenvalue j of matrix b into evals[b][j], ascending
+__global__ void __launch_bounds__(256)
+k_tridiag_bisect(const float* __restrict__ d_all, const float* __restrict__ e_all, int N, float* __restrict__ evals,
+                 float* __restrict__ tnorm_out) {
+    extern __shared__ float sm[];
+    float* d = sm;
+    float* e2 = sm + N;
+    __shared__ float red[34];
+    const int b = blockIdx.y;
+    const float* db = d_all + static_cast<int64_t>(b) * N;
+    const float* eb = e_all + static_cast<int64_t>(b) * N;
+    float lo = INFINITY, hi = -INFINITY;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float di = db[i];
+        const float el = i > 0 ? fabsf(eb[i - 1]) : 0.0f;
+        const float er = i + 1 < N ? fabsf(eb[i]) : 0.0f;
+        d[i] = di;
+        if (i + 1 < N) e2[i] = eb[i] * eb[i];
+        lo = fminf(lo, di - el - er);
+        hi = fmaxf(hi, di + el + er);
+    }
+    // block min / max through warp shuffles
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = lo;
+        red[16 + (threadIdx.x >> 5)] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float l = red[0], h = red[16];
+        for (int w = 1; w < (blockDim.x >> 5); ++w) {
+            l = fminf(l, red[w]);
+            h = fmaxf(h, red[16 + w]);
+        }
+        red[32] = l;
+        red[33] = h;
+    }
+    __syncthreads();
+    const float gl = red[32], gu = red[33];
+    const float tnorm = fmaxf(fabsf(gl), fabsf(gu));
+    if (blockIdx.x == 0 && threadIdx.x == 0) tnorm_out[b] = tnorm;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const float pivmin = fmaxf(1e-30f, 1.2e-7f * 1e-6f * tnorm);
+    float a = gl - 1e-6f * tnorm - 1e-30f, z = gu + 1e-6f * tnorm + 1e-30f;
+    // the interval [a, z) holds the (j+1)-th smallest eigenvalue: count(a) <= j < count(z)
+    for (int it = 0; it < kBisectSteps; ++it) {
+        const float m = 0.5f * (a + z);
+        if (m <= a || m >= z) break;
+        if (sturm_count(d, e2, N, m, pivmin) > j) z = m; else a = m;
+    }
+    evals[static_cast<int64_t>(b) * N + j] = 0.5f * (a + z);
+}
+
+// ---- eigenvectors of T: inverse iteration in FP64 -------------------------------------------------------------
+
+__device__ __forceinline__ double start_value(int i, int j) {
+    uint32_t h = static_cast<uint32_t>(i) * 0x9E3779B1u ^ (static_cast<uint32_t>(j) + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return 0.5 + static_cast<double>(h & 0xFFFFFF) * (1.0 / 16777216.0);  // in [0.5, 1.5)
+}
+
+// grid (ceil(N / 128), batch), one thread per eigenvalue index j.  Scratch S (batch, 3, N, N) FP64: S[0] the
+// reciprocal LDL^T pivots 1 / D, S[1] the multipliers L, S[2] the iterate x, element i of thread j at [i * N + j] (coalesced over a
+// warp's consecutive j).  Z (batch, N, N) FP32: eigenvector j of T in column j.
+__global__ void __launch_bounds__(128)
+k_tridiag_invit(const float* __restrict__ d_all, const float* __restrict__ e_all, const float* __restrict__ evals,
+                const float* __restrict__ tnorm_all, int N, double* __restrict__ S, float* __restrict__ Z) {
+    const int b = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const float* db = d_all + static_cast<int64_t>(b) * N;
+    const float* eb = e_all + static_cast<int64_t>(b) * N;
+    const float* lam = evals + static_cast<int64_t>(b) * N;
+    const double tnorm = static_cast<double>(tnorm_all[b]);
+    const double tol = kClusterTol * tnorm;
+    // j runs the cluster that starts at j; a thread whose eigenvalue continues a cluster has nothing to do
+    if (j > 0 && static_cast<double>(lam[j]) - static_cast<double>(lam[j - 1]) < tol) return;
+    int jend = j + 1;
+    while (jend < N && static_cast<double>(lam[jend]) - static_cast<double>(lam[jend - 1]) < tol) ++jend;
+    const int64_t NN = static_cast<int64_t>(N) * N;
+    double* D = S + (static_cast<int64_t>(b) * 3 + 0) * NN;
+    double* L = S + (static_cast<int64_t>(b) * 3 + 1) * NN;
+    double* X = S + (static_cast<int64_t>(b) * 3 + 2) * NN;
+    float* Zb = Z + static_cast<int64_t>(b) * NN;
+    const double pivmin = 1e-14 * tnorm + 1e-300;
+    for (int m = j; m < jend; ++m) {
+        // members of a cluster get slightly separated shifts so that their LDL^T factors differ
+        const double lm = static_cast<double>(lam[m]) + (m - j) * 1e-3 * tol;
+        // LDL^T of T - lm I, kept as the multipliers L and the reciprocal pivots 1 / D (in the column of thread j,
+        // reused by the cluster's members in turn): one FP64 division per row, none in the solves
+        double dcur = static_cast<double>(db[0]) - lm;
+        if (fabs(dcur) < pivmin) dcur = -pivmin;
+        double inv = 1.0 / dcur;
+        D[j] = inv;
+        for (int i = 1; i < N; ++i) {
+            const double ei = static_cast<double>(eb[i - 1]);
+            const double l = ei * inv;
+            dcur = (static_cast<double>(db[i]) - lm) - l * ei;
+            if (fabs(dcur) < pivmin) dcur = -pivmin;
+            inv = 1.0 / dcur;
+            L[static_cast<int64_t>(i - 1) * N + j] = l;
+            D[static_cast<int64_t>(i) * N + j] = inv;
+        }
+        for (int i = 0; i < N; ++i) X[static_cast<int64_t>(i) * N + j] = start_value(i, m);
+        for (int it = 0; it < kInvitSolves; ++it) {
+            // forward: z_i = x_i - L_{i-1} z_{i-1}; backward: y_i = z_i / D_i - L_i y_{i+1}
+            double z = X[j];
+            for (int i = 1; i < N; ++i) {
+                z = X[static_cast<int64_t>(i) * N + j] - L[static_cast<int64_t>(i - 1) * N + j] * z;
+                X[static_cast<int64_t>(i) * N + j] = z;
+            }
+            double y = X[static_cast<int64_t>(N - 1) * N + j] * D[static_cast<int64_t>(N - 1) * N + j];
+            X[static_cast<int64_t>(N - 1) * N + j] = y;
+            double nrm = y * y;
+            for (int i = N - 2; i >= 0; --i) {
+                y = X[static_cast<int64_t>(i) * N + j] * D[static_cast<int64_t>(i) * N + j] -
+                    L[static_cast<int64_t>(i) * N + j] * y;
+                X[static_cast<int64_t>(i) * N + j] = y;
+                nrm = fma(y, y, nrm);
+            }
+            // orthogonalise against the cluster's earlier vectors (already written to Z), then normalise
+            for (int q = j; q < m; ++q) {
+                double pr = 0.0;
+                for (int i = 0; i < N; ++i)
+                    pr = fma(static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]), X[static_cast<int64_t>(i) * N + j], pr);
+                nrm = 0.0;
+                for (int i = 0; i < N; ++i) {
+                    const double v = X[static_cast<int64_t>(i) * N + j] - pr * static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]);
+                    X[static_cast<int64_t>(i) * N + j] = v;
+                    nrm = fma(v, v, nrm);
+                }
+            }
+            const double sc = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+            for (int i = 0; i < N; ++i) X[static_cast<int64_t>(i) * N + j] *= sc;
+        }
+        for (int i = 0; i < N; ++i)
+            Zb[static_cast<int64_t>(i) * N + m] = static_cast<float>(X[static_cast<int64_t>(i) * N + j]);
+    }
+}
+
+// ---- back-transformation: U = Q Z with Q = H_0 ... H_{N-3} in WY blocks ---------------------------------------
+
+// grid (nblocks, batch), kWy * kWy threads: T_q of block q (upper triangular, I - V T V^T = H_{k0} ... H_{k0+15}),
+// from G = V^T V and tau (LAPACK larft, forward / columnwise)
+__global__ void __launch_bounds__(kWy * kWy)
+k_wy_factors(const float* __restrict__ W, const float* __restrict__ tau_all, int N, int n_refl,
+             float* __restrict__ Tq) {
+    __shared__ float G[kWy][kWy + 1];
+    __shared__ float T[kWy][kWy + 1];
+    const int b = blockIdx.y, q = blockIdx.x;
+    const int k0 = q * kWy;
+    const int a = threadIdx.x / kWy, c = threadIdx.x % kWy;
+    const float* Wb = W + static_cast<int64_t>(b) * N * N;
+    const float* tau = tau_all + static_cast<int64_t>(b) * N;
+    const int ka = k0 + a, kc = k0 + c;
+    float g = 0.0f;
+    if (a < c && kc < n_refl) {  // v_a . v_c over rows > kc (v_c is zero above row kc + 1, where it is 1)
+        const float* va = Wb + static_cast<int64_t>(ka) * N;
+        const float* vc = Wb + static_cast<int64_t>(kc) * N;
+        g = va[kc + 1];
+        for (int i = kc + 2; i < N; ++i) g = fmaf(va[i], vc[i], g);
+    }
+    G[a][c] = g;
+    T[a][c] = 0.0f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kWy; ++i) {
+            const float ti = (k0 + i < n_refl) ? tau[k0 + i] : 0.0f;
+            // T[0:i, i] = -ti * T[0:i, 0:i] G[0:i, i]
+            for (int rr = 0; rr < i; ++rr) {
+                float s = 0.0f;
+                for (int m = rr; m < i; ++m) s = fmaf(T[rr][m], G[m][i], s);
+                T[rr][i] = -ti * s;
+            }
+            T[i][i] = ti;
+        }
+    }
+    __syncthreads();
+    Tq[((static_cast<int64_t>(b) * gridDim.x + q) * kWy + a) * kWy + c] = T[a][c];
+}
+
+// grid (ceil(N / kTile), batch): columns c0 .. c0+15 of Z (eigenvectors of T) to eigenvector rows of A in U
+__global__ void __launch_bounds__(kBtThreads)
+k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, const float* __restrict__ Z, int N,
+                int n_refl, int nblocks, float* __restrict__ U) {
+    extern __shared__ float sm[];
+    float* Zt = sm;                          // N x kTile
+    float* Vc = Zt + N * kTile;              // kChunk x kWy
+    __shared__ float Sm[kWy][kTile + 1];
+    __shared__ float Sp[kWy][kTile + 1];
+    __shared__ float Tm[kWy][kWy + 1];
+    const int b = blockIdx.y;
+    const int c0 = blockIdx.x * kTile;
+    const int64_t NN = static_cast<int64_t>(N) * N;
+    const float* Wb = W + b * NN;
+    const float* Zb = Z + b * NN;
+    const int ncols = min(kTile, N - c0);
+    for (int t = threadIdx.x; t < N * kTile; t += kBtThreads) {
+        const int i = t / kTile, c = t % kTile;
+        Zt[t] = c < ncols ? Zb[static_cast<int64_t>(i) * N + c0 + c] : 0.0f;
+    }
+    const int a = threadIdx.x / kTile, cc = threadIdx.x % kTile;  // one (reflector, column) pair per thread
+    for (int q = nblocks - 1; q >= 0; --q) {
+        const int k0 = q * kWy;
+        const int r0 = k0 + 1;  // first row any reflector of the block touches
+        if (threadIdx.x < kWy * kWy)
+            Tm[threadIdx.x / kWy][threadIdx.x % kWy] = Tq_all[(static_cast<int64_t>(b) * nblocks + q) * kWy * kWy + threadIdx.x];
+        float s = 0.0f;
+        // S = V^T Z over the block's rows, V staged kChunk rows at a time (V[i][a] = v_{k0+a}[i])
+        for (int i0 = r0; i0 < N; i0 += kChunk) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {
+                const int ii = t / kWy, aa = t % kWy, i = i0 + ii, k = k0 + aa;
+                float v = 0.0f;
+                if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
+                Vc[t] = v;
+            }
+            __syncthreads();
+            const int iend = min(kChunk, N - i0);
+            for (int ii = 0; ii < iend; ++ii) s = fmaf(Vc[ii * kWy + a], Zt[(i0 + ii) * kTile + cc], s);
+        }
+        Sm[a][cc] = s;
+        __syncthreads();
+        // S' = T S
+        float sp = 0.0f;
+        for (int m = a; m < kWy; ++m) sp = fmaf(Tm[a][m], Sm[m][cc], sp);
+        Sp[a][cc] = sp;
+        __syncthreads();
+        // Z -= V S'
+        for (int i0 = r0; i0 < N; i0 += kChunk) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {
+                const int ii = t / kWy, aa = t % kWy, i = i0 + ii, k = k0 + aa;
+                float v = 0.0f;
+                if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
+                Vc[t] = v;
+            }
+            __syncthreads();
+            const int iend = min(kChunk, N - i0);
+            for (int t = threadIdx.x; t < iend * kTile; t += kBtThreads) {
+                const int ii = t / kTile, c = t % kTile;
+                float acc = Zt[(i0 + ii) * kTile + c];
+#pragma unroll
+                for (int m = 0; m < kWy; ++m) acc = fmaf(-Vc[ii * kWy + m], Sp[m][c], acc);
+                Zt[(i0 + ii) * kTile + c] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    // eigenvector c0 + c is column c of the tile: one row of U each
+    for (int c = 0; c < ncols; ++c)
+        for (int i = threadIdx.x; i < N; i += kBtThreads)
+            U[b * NN + static_cast<int64_t>(c0 + c) * N + i] = Zt[i * kTile + c];
+}
+
+struct OwnLayout {
+    size_t W, Z, S, d, e, tau, ev, tn, T, total;
+    int nblocks;
+};
+
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+OwnLayout own_layout(int N, int batch) {
+    OwnLayout L;
+    const size_t NN = static_cast<size_t>(N) * N * batch;
+    const int n_refl = N > 2 ? N - 2 : 0;
+    L.nblocks = n_refl > 0 ? (n_refl + kWy - 1) / kWy : 0;
+    size_t o = 0;
+    L.W = o; o += up256(4 * NN);
+    L.Z = o; o += up256(4 * NN);
+    L.S = o; o += up256(8 * 3 * NN);
+    L.d = o; o += up256(4 * static_cast<size_t>(N) * batch);
+    L.e = o; o += up256(4 * static_cast<size_t>(N) * batch);
+    L.tau = o; o += up256(4 * static_cast<size_t>(N) * batch);
+    L.ev = o; o += up256(4 * static_cast<size_t>(N) * batch);
+    L.tn = o; o += up256(4 * static_cast<size_t>(batch));
+    L.T = o; o += up256(4 * static_cast<size_t>(L.nblocks > 0 ? L.nblocks : 1) * kWy * kWy * batch);
+    L.total = o;
+    return L;
+}
+
+}  // namespace
+
+namespace flmm {
+
+size_t eigh_own_workspace_bytes(int N, int batch) { return own_layout(N, batch).total; }
+
+// A (batch, N, N) FP32 symmetric in, eigenvector rows out (ascending eigenvalues into evals (batch, N) FP32)
+int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStream_t st) {
+    const OwnLayout L = own_layout(N, batch);
+    char* base = static_cast<char*>(work);
+    float* W = reinterpret_cast<float*>(base + L.W);
+    float* Z = reinterpret_cast<float*>(base + L.Z);
+    double* S = reinterpret_cast<double*>(base + L.S);
+    float* d = reinterpret_cast<float*>(base + L.d);
+    float* e = reinterpret_cast<float*>(base + L.e);
+    float* tau = reinterpret_cast<float*>(base + L.tau);
+    float* tn = reinterpret_cast<float*>(base + L.tn);
+    float* Tq = reinterpret_cast<float*>(base + L.T);
+    const size_t NN = static_cast<size_t>(N) * N;
+    FLMM_CUDA(cudaMemcpyAsync(W, A, 4 * NN * batch, cudaMemcpyDeviceToDevice, st));
+    // 1. tridiagonalisation, one cluster per matrix
+    const int Np = (N + 3) & ~3;
+    const size_t smem1 = sizeof(float) * (6 * static_cast<size_t>(Np) + 34);
+    // (per device, so set on every call; the call is cheap)
+    FLMM_CUDA(cudaFuncSetAttribute(k_sytrd_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    FLMM_CUDA(cudaFuncSetAttribute(k_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(kClusterCtas * batch), 1, 1);
+    cfg.blockDim = dim3(kSytrdThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem1;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FLMM_CUDA(cudaLaunchKernelEx(&cfg, k_sytrd_cluster, W, N, d, e, tau));
+    int rc = check_launch("k_sytrd_cluster");
+    if (rc) return rc;
+    // 2. eigenvalues
+    k_tridiag_bisect<<<dim3(ceil_div(N, 256), batch), 256, sizeof(float) * 2 * static_cast<size_t>(N), st>>>(
+        d, e, N, evals, tn);
+    if ((rc = check_launch("k_tridiag_bisect"))) return rc;
+    // 3. eigenvectors of T
+    k_tridiag_invit<<<dim3(ceil_div(N, 128), batch), 128, 0, st>>>(d, e, evals, tn, N, S, Z);
+    if ((rc = check_launch("k_tridiag_invit"))) return rc;
+    // 4. back-transformation into A
+    const int n_refl = N > 2 ? N - 2 : 0;
+    if (L.nblocks > 0) {
+        k_wy_factors<<<dim3(L.nblocks, batch), kWy * kWy, 0, st>>>(W, tau, N, n_refl, Tq);
+        if ((rc = check_launch("k_wy_factors"))) return rc;
+    }
+    const size_t smem4 = sizeof(float) * (static_cast<size_t>(N) * kTile + kChunk * kWy);
+    k_backtransform<<<dim3(ceil_div(N, kTile), batch), kBtThreads, smem4, st>>>(W, Tq, Z, N, n_refl, L.nblocks, A);
+    return check_launch("k_backtransform");
+}
+
+}  // namespace flmm

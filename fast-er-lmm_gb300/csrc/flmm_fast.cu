@@ -831,13 +831,22 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
     float av[kPrepCache];
     const bool cached = Neff <= 32 * kPrepCache;
     if (cached) {
+        // every load of the column first, so they are in flight together (the division's branches would otherwise
+        // hold each load back until the previous element is done)
+        float uv[kPrepCache], sv[kPrepCache];
+#pragma unroll
+        for (int i = 0; i < kPrepCache; ++i) {
+            const int n = lane + 32 * i;
+            uv[i] = n < Neff ? u[n] : 0.0f;
+            sv[i] = n < Neff ? s32[n] : 0.0f;
+        }
 #pragma unroll
         for (int i = 0; i < kPrepCache; ++i) {
             const int n = lane + 32 * i;
             av[i] = 0.0f;
             if (n < Neff) {
-                const float un = u[n];
-                const float a = (num / (s32[n] + delta)) * un;
+                const float un = uv[i];
+                const float a = (num / (sv[i] + delta)) * un;
                 av[i] = a;
                 m1 = fmaxf(m1, fabsf(a));
                 neumaier(acc, comp, a * un);
@@ -911,11 +920,13 @@ __global__ void k_wald_prep_variants(const float* __restrict__ USt, int64_t ldus
     if (m >= Mc) return;
     const float* u = USt + m * ldus;
     float m1 = 0.0f;
+#pragma unroll 4
     for (int n = lane; n < Neff; n += 32) m1 = fmaxf(m1, fabsf(u[n]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
     int e1, e2;
     const float mul1 = row_scale_exp(m1, &e1), mul2 = row_scale_exp(m1 * m1, &e2);
+#pragma unroll 4
     for (int n = lane; n < Neff; n += 32) {
         const float x = u[n];
         split_store(x, mul1, B1h, B1l, m * ldb + n);

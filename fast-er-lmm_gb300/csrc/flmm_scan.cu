@@ -145,7 +145,7 @@ int interp_R(double lo, double hi, double* x0) {
 
 int refine_steps(const flmm_scan& s) {
     if (s.opts.eigh_refine_steps > 0) return s.opts.eigh_refine_steps;
-    return s.N <= 2000 ? 2 : 3;
+    return s.N <= 1024 ? 2 : 3;
 }
 
 // Column side of unit u into slot b: U_eff split, UY rotation, delta fit (stream st).

@@ -39,15 +39,16 @@ F32 = torch.float32
 #   "f64": the FP64 batched call (EIGH_MODE: 1 = cusolverDnXsyevBatched, 2 = syevd side by side on worker streams).
 EIGH_PRECISION = "f32r"
 EIGH_MODE = 1
-# Refinement steps of "f32r": None picks by size -- 2 up to N = 2,000, 3 above (the FP32 decomposition's error grows
-# with N: at N = 5,000 two steps leave beta of ~1 % of the tests outside 1e-5 of the FP64 result, three match it).
+# Refinement steps of "f32r": None picks by size -- 2 up to N = 1,024, 3 above (the FP32 decomposition's error grows
+# with N: at N = 1,294 two steps left beta of a few hundred tests of a missingness group outside 1e-5 of the
+# reference's FP64 result and at N = 5,000 ~1 % of them; three steps match it in both).
 EIGH_REFINE_STEPS = None
 
 
 def refine_steps(N: int) -> int:
     if EIGH_REFINE_STEPS is not None:
         return max(1, int(EIGH_REFINE_STEPS))
-    return 2 if N <= 2000 else 3
+    return 2 if N <= 1024 else 3
 # Where the exact delta refinement starts: "grid" (the FP32 grid argmin's bracket) or "learned" (the MLP proposal of
 # fasterlmm_gb300.learned, bracketed inside the grid argmin's basin; same answers, fewer evaluations per column).
 DELTA_PROPOSAL = "grid"

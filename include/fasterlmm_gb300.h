@@ -110,7 +110,9 @@ int flmm_eigh_batched(flmm_context* ctx, double* A, int N, int batch, double* ev
 
 /* FP32 twin of flmm_eigh_batched (mode 1, main handle) for the split-precision form, whose eigenbasis is used at
  * ~2^-22 relative precision: an FP32 eigendecomposition's backward error (~1e-7 of the projected kinship) is below
- * that.  Same layout: eigenvectors one per row of each A[b], evals ascending. */
+ * that.  Same layout: eigenvectors one per row of each A[b], evals ascending.  Below N = 2,500 the library's own
+ * batched solver runs (FLMM_EIGH_F32=cusolver selects cuSOLVER's batched call instead); from there on batches of up to
+ * 4 matrices go one at a time through cusolverDnSsyevd and larger ones through the batched call. */
 int flmm_eigh_batched_f32_workspace_bytes(flmm_context* ctx, int N, int batch, size_t* bytes);
 int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* evals, void* work, size_t work_bytes,
                           void* stream);
@@ -305,7 +307,7 @@ int flmm_loco_kinship_f32(const double* Gtot, const float* Gc, int N, double m_l
  * chromosome, pipelined) or fit_delta(k) followed by wald(k) per chromosome; destroy.
  *
  * flmm_scan_opts: delta grid (n_grid points on [log_delta_min, log_delta_max], refine != 0: exact refinement of the
- * grid argmin; fasterlmm/core.py:561-595), eigh_refine_steps (0: 2 up to N = 2,000, 3 above), f_refine (real tests
+ * grid argmin; fasterlmm/core.py:561-595), eigh_refine_steps (0: 2 up to N = 1,024, 3 above), f_refine (real tests
  * with F above it are recomputed without the FP32 cancellation; <= 0: off), pipeline (!= 0: the column side of
  * chromosome k + 1 runs on a second stream beside the variant side of chromosome k). */
 typedef struct flmm_scan flmm_scan;
