@@ -1,29 +1,34 @@
-// Batched FP32 symmetric eigendecomposition of the projected LOCO kinships (N up to kOwnMaxN), the fast form's
+// Batched FP32 symmetric eigendecomposition of the projected LOCO kinships (N below 2,500), the fast form's
 // replacement for the library's batched eigensolver.  The reference decomposes each kinship in FP64
 // (fasterlmm/core.py:54-77, torch.linalg.eigh); the fast form takes an FP32 decomposition and refines it
 // (flmm_eigh_refine_f32), so only FP32-quality eigenpairs are needed here.
 //
-// Four stages, all matrices of the batch side by side:
+// Five stages, all matrices of the batch side by side:
 //
-// 1. k_sytrd_cluster: Householder tridiagonalisation A = Q T Q^T, one thread-block cluster of kClusterCtas CTAs per
-//    matrix.  The FP32 matrix stays in global memory (L2-resident for the batch sizes used), rows dealt round-robin
-//    to the cluster's CTAs.  Column k's reflector is formed redundantly by every CTA from row k, each CTA computes
-//    p = tau W v for its rows, and the cluster exchanges p and the partial p^T v through distributed shared memory.
-//    The symmetric rank-2 update W -= v w^T + w v^T is applied lazily: row k+1 (the next pivot row) right away by its
-//    owner, every other row in the same pass that forms the next step's W v, so the trailing matrix is read and
-//    written once per column.  Both products of an update term are rounded before the add, so W stays exactly
-//    symmetric.  Two cluster barriers per column.
+// 1. k_sytrd_cluster: Householder tridiagonalisation A = Q T Q^T, one thread-block cluster of 2 to 8 CTAs per
+//    matrix (one CTA per SM).  The FP32 matrix stays in global memory (L2-resident for the batch sizes used), rows
+//    dealt round-robin to the cluster's CTAs.  Column k's reflector is formed redundantly by every CTA, each CTA
+//    computes p = tau W v for its rows and stores it, with its partial p^T v, into every CTA's shared memory
+//    (distributed shared memory), so after the barrier each CTA reads only its own.  The symmetric rank-2 update
+//    W -= v w^T + w v^T is applied lazily, in the same pass that forms the next column's W v, so the trailing
+//    matrix is read and written once per column; the next pivot row gets its last update in registers in every
+//    CTA, which forms the next reflector from it.  Both products of an update term are rounded before the add, so
+//    W stays exactly symmetric.  One cluster barrier per column.
 // 2. k_tridiag_bisect: each eigenvalue of T by bisection on FP32 Sturm counts (ascending, by index).
 // 3. k_tridiag_invit: each eigenvector of T by inverse iteration in FP64 (LDL^T of T - lambda I with a pivot floor,
-//    five solves from a fixed pseudo-random start); eigenvalues closer than kClusterTol * ||T|| form a cluster whose
-//    vectors one thread computes in turn, each orthogonalised against the cluster's earlier vectors.
-// 4. k_wy_factors + k_backtransform: the reflectors in blocks of kWy as I - V T V^T (forward, columnwise), applied to
+//    three solves from a fixed pseudo-random start, the first fused with the factorisation), one thread each.
+// 4. k_cluster_orth: eigenvalues closer than kClusterTol * ||T|| form a cluster; one warp orthonormalises its
+//    vectors (modified Gram-Schmidt in FP64).  Each vector of a cluster has converged into the cluster's invariant
+//    subspace from its own start, so the result is an orthonormal basis of that subspace.
+// 5. k_wy_factors + k_backtransform: the reflectors in blocks of kWy as I - V T V^T (forward, columnwise), applied to
 //    column tiles of the eigenvector matrix of T held in shared memory, last block first; the result is written as
 //    one eigenvector per row.
 //
 // Every loop is bounded by N and fixed iteration counts; the only waits are cluster barriers that every CTA of the
 // cluster reaches on the same trip count.
 #include <math.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include "flmm_common.cuh"
@@ -32,13 +37,18 @@ using namespace flmm;
 
 namespace {
 
-constexpr int kClusterCtas = 8;
-constexpr int kSytrdThreads = 256;
+constexpr int kMaxClusterCtas = 8;
+constexpr int kSytrdThreads = 512;
+constexpr int kRowsPerWarp = 4;    // rows a warp of the tridiagonalisation works on at once
+constexpr int kLoadsPerRow = 8;    // loads of each of them a lane has in flight
 constexpr int kWy = 16;            // reflectors per WY block
 constexpr int kTile = 16;          // eigenvectors per back-transform CTA
 constexpr int kBtThreads = 256;
 constexpr int kChunk = 128;        // rows of a V block staged at a time in the back-transform
-constexpr int kInvitSolves = 5;
+// the FP32 shift is within ~1e-7 ||T|| of its eigenvalue: at the cluster cut (a gap of 1e-5 ||T||) each solve shrinks
+// the neighbour by ~1e-2, so three solves leave ~1e-6 of it (two left pairs near the cut ~1e-4 from orthogonal)
+constexpr int kInvitSolves = 3;
+constexpr int kInvitBlock = 16;     // elements whose loads a recurrence pass issues ahead
 constexpr double kClusterTol = 1e-5;
 constexpr int kBisectSteps = 48;
 
@@ -62,13 +72,12 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// FP32 load from the shared memory of the cluster's CTA `rank` at the address of `p` in this CTA
-__device__ __forceinline__ float ld_remote(const float* p, uint32_t rank) {
+// FP32 store into the shared memory of the cluster's CTA `rank` at the address of `p` in this CTA (made visible to it
+// by the next cluster barrier)
+__device__ __forceinline__ void st_remote(float* p, uint32_t rank, float v) {
     uint32_t a;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_addr(p)), "r"(rank));
-    float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
-    return v;
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
 // block-wide FP32 sum (all threads get it); red holds >= 32 floats
@@ -87,8 +96,41 @@ __device__ float block_sum(float v, float* red) {
 
 // W (batch, N, N) FP32 symmetric, full storage, overwritten: row k holds the reflector v_k on columns k+1..N-1
 // (v_k[k+1] = 1).  d (batch, N), e (batch, N), tau (batch, N): T's diagonal, off-diagonal (e[k] = T[k][k+1]) and the
-// reflector scalars (tau[N-2] = tau[N-1] = 0).
-__global__ void __launch_bounds__(kSytrdThreads)
+// reflector scalars (tau[N-2] = tau[N-1] = 0).  The cluster size C is the launch's (%cluster_nctarank); CTA r owns
+// the rows i with i % C == r.
+//
+// Step k: (B) each CTA brings its rows i > k up to date with column k-1's update and forms p_i = tau_k W[i, k+1:] v_k;
+// one cluster barrier; (C) every CTA gathers p and p^T v from the cluster, forms w_k, reads row k+1 (stored by its
+// owner in (B), so it already carries every update but column k's), applies column k's update to it in registers and
+// forms the next reflector v_{k+1} -- redundantly in every CTA, so no second barrier is needed.
+__device__ __forceinline__ uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
+struct Reflector {
+    float d, beta, tau;
+};
+
+// From x = row entries x[k .. N-1] in xs[] (xs[j] for j >= k + 1; d passed in): the reflector of column k into v[]
+// (v[k+1] = 1, v[j] = x_j / (alpha - beta) for j >= k + 2), as LAPACK's larfg.  Every thread of the CTA calls it.
+__device__ Reflector make_reflector(float d, float alpha, float ss_partial, float* v, int k, int N, float* red) {
+    const float sigma = block_sum(ss_partial, red);
+    Reflector R{d, alpha, 0.0f};
+    float scal = 0.0f;
+    if (sigma > 0.0f) {
+        R.beta = -copysignf(sqrtf(fmaf(alpha, alpha, sigma)), alpha);
+        R.tau = (R.beta - alpha) / R.beta;
+        scal = 1.0f / (alpha - R.beta);
+    }
+    for (int j = k + 2 + threadIdx.x; j < N; j += blockDim.x) v[j] *= scal;
+    if (threadIdx.x == 0) v[k + 1] = 1.0f;
+    __syncthreads();
+    return R;
+}
+
+__global__ void __launch_bounds__(kSytrdThreads, 1)
 k_sytrd_cluster(float* __restrict__ W, int N, float* __restrict__ d_out, float* __restrict__ e_out,
                 float* __restrict__ tau_out) {
     extern __shared__ float sm[];
@@ -97,114 +139,161 @@ k_sytrd_cluster(float* __restrict__ W, int N, float* __restrict__ d_out, float* 
     float* wbuf[2] = {sm + 2 * Np, sm + 3 * Np};
     float* pbuf[2] = {sm + 4 * Np, sm + 5 * Np};
     float* red = sm + 6 * Np;        // 32 floats
-    float* part = red + 32;          // partial p^T v, one per parity
+    float* part = red + 32;          // partial p^T v of every CTA of the cluster, [parity][rank]
+    float* scal2 = part + 2 * kMaxClusterCtas;  // d and alpha of the next reflector
+    const int C = static_cast<int>(cluster_size());
     const int b = static_cast<int>(cluster_index());
     const int r = static_cast<int>(cta_rank());
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = kSytrdThreads >> 5;
     float* Wb = W + static_cast<int64_t>(b) * N * N;
+    float* db = d_out + static_cast<int64_t>(b) * N;
+    float* eb = e_out + static_cast<int64_t>(b) * N;
+    float* tb = tau_out + static_cast<int64_t>(b) * N;
+    Reflector R{0.0f, 0.0f, 0.0f};
+    if (N >= 3) {  // reflector of column 0 from the untouched row 0
+        float ss = 0.0f;
+        for (int j = 2 + threadIdx.x; j < N; j += kSytrdThreads) {
+            const float x = Wb[j];
+            vbuf[0][j] = x;
+            ss = fmaf(x, x, ss);
+        }
+        R = make_reflector(Wb[0], Wb[1], ss, vbuf[0], 0, N, red);
+    }
     for (int k = 0; k + 2 < N; ++k) {
         const int cur = k & 1;
         float* vc = vbuf[cur];
         float* wc = wbuf[cur];
-        const float* vp = vbuf[cur ^ 1];
-        const float* wp = wbuf[cur ^ 1];
+        float* vn = vbuf[cur ^ 1];        // v_{k-1} until (B) is done, then v_{k+1}
+        const float* wp = wbuf[cur ^ 1];  // w_{k-1}
         float* pb = pbuf[cur];
-        // (A) reflector of row k, which its owner brought up to date before the last barrier (read past L1: the row
-        // was written by another CTA)
-        const float* rowk = Wb + static_cast<int64_t>(k) * N;
-        float ss = 0.0f;
-        for (int j = k + 2 + threadIdx.x; j < N; j += kSytrdThreads) {
-            const float x = __ldcg(rowk + j);
-            vc[j] = x;
-            ss = fmaf(x, x, ss);
-        }
-        const float sigma = block_sum(ss, red);
-        const float alpha = __ldcg(rowk + k + 1);
-        const float dk = __ldcg(rowk + k);
-        float tau = 0.0f, beta = alpha, scal = 0.0f;
-        if (sigma > 0.0f) {
-            beta = -copysignf(sqrtf(fmaf(alpha, alpha, sigma)), alpha);
-            tau = (beta - alpha) / beta;
-            scal = 1.0f / (alpha - beta);
-        }
-        for (int j = k + 2 + threadIdx.x; j < N; j += kSytrdThreads) vc[j] *= scal;
-        if (threadIdx.x == 0) vc[k + 1] = 1.0f;
-        __syncthreads();
-        // (B) rows i > k of this CTA: the previous column's update (lazy), then p_i = tau * W[i, k+1:] . v
+        const float tau = R.tau;
+        // (B) rows i > k of this CTA: column k-1's update (lazy), then p_i = tau W[i, k+1:] . v.  A warp takes
+        // kRowsPerWarp rows at a time and a lane issues kLoadsPerRow loads of each before using any, so the pass
+        // keeps enough L2 reads in flight to run at bandwidth rather than at L2 latency.
         float dot = 0.0f;
-        int first = k + 1 + ((r - (k + 1)) % kClusterCtas + kClusterCtas) % kClusterCtas;
-        for (int i = first + wid * kClusterCtas; i < N; i += nw * kClusterCtas) {
-            float* row = Wb + static_cast<int64_t>(i) * N;
-            float acc = 0.0f;
-            if (k > 0) {
-                const float vi = vp[i], wi = wp[i];
-#pragma unroll 4
-                for (int j = k + 1 + lane; j < N; j += 32) {
-                    const float x = row[j] - (__fmul_rn(vi, wp[j]) + __fmul_rn(wi, vp[j]));
-                    row[j] = x;
-                    acc = fmaf(x, vc[j], acc);
-                }
-            } else {
-#pragma unroll 4
-                for (int j = k + 1 + lane; j < N; j += 32) acc = fmaf(row[j], vc[j], acc);
+        const int first = k + 1 + ((r - (k + 1)) % C + C) % C;
+        const int n_own = first < N ? (N - 1 - first) / C + 1 : 0;
+        const bool lazy = k > 0;
+        for (int t0 = wid * kRowsPerWarp; t0 < n_own; t0 += nw * kRowsPerWarp) {
+            float* rows[kRowsPerWarp];
+            float vi[kRowsPerWarp], wi[kRowsPerWarp], acc[kRowsPerWarp];
+#pragma unroll
+            for (int q = 0; q < kRowsPerWarp; ++q) {
+                const int t = t0 + q;
+                const int i = first + t * C;
+                rows[q] = t < n_own ? Wb + static_cast<int64_t>(i) * N : nullptr;
+                vi[q] = (t < n_own && lazy) ? vn[i] : 0.0f;
+                wi[q] = (t < n_own && lazy) ? wp[i] : 0.0f;
+                acc[q] = 0.0f;
             }
-            acc = warp_sum(acc);
-            const float pi = tau * acc;
-            if (lane == 0) pb[i] = pi;
-            dot = fmaf(pi, vc[i], dot);
+            for (int j0 = k + 1; j0 < N; j0 += 32 * kLoadsPerRow) {
+                float x[kRowsPerWarp][kLoadsPerRow];
+#pragma unroll
+                for (int q = 0; q < kRowsPerWarp; ++q)
+#pragma unroll
+                    for (int u = 0; u < kLoadsPerRow; ++u) {
+                        const int j = j0 + lane + 32 * u;
+                        x[q][u] = (rows[q] != nullptr && j < N) ? rows[q][j] : 0.0f;
+                    }
+#pragma unroll
+                for (int u = 0; u < kLoadsPerRow; ++u) {
+                    const int j = j0 + lane + 32 * u;
+                    if (j < N) {
+                        const float vj = vc[j];
+                        const float vpj = lazy ? vn[j] : 0.0f, wpj = lazy ? wp[j] : 0.0f;
+#pragma unroll
+                        for (int q = 0; q < kRowsPerWarp; ++q) {
+                            if (rows[q] == nullptr) continue;
+                            float xv = x[q][u];
+                            if (lazy) {
+                                xv -= __fmul_rn(vi[q], wpj) + __fmul_rn(wi[q], vpj);
+                                rows[q][j] = xv;
+                            }
+                            acc[q] = fmaf(xv, vj, acc[q]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kRowsPerWarp; ++q) {
+                const float a = warp_sum(acc[q]);
+                if (rows[q] != nullptr) {
+                    const int i = first + (t0 + q) * C;
+                    const float pi = tau * a;
+                    // p_i into every CTA's copy of p (lane l to CTA l): after the barrier all of p is local
+                    if (lane < C) st_remote(&pb[i], static_cast<uint32_t>(lane), pi);
+                    dot = fmaf(pi, vc[i], dot);
+                }
+            }
         }
-        // lanes of a warp hold the same dot (lane 0's rows are the warp's rows); sum one lane per warp
+        // lanes of a warp hold the same dot; sum one lane per warp
         const float dsum = block_sum(lane == 0 ? dot : 0.0f, red);
-        if (threadIdx.x == 0) part[cur] = dsum;
-        cluster_barrier();  // B1: every CTA's p and partial p^T v are visible
-        // (C) w = p - (tau / 2) (p^T v) v over the whole trailing range
+        if (threadIdx.x < static_cast<unsigned>(C))
+            st_remote(&part[cur * kMaxClusterCtas + r], threadIdx.x, dsum);
+        cluster_barrier();  // every CTA's p, p^T v and updated rows are visible
+        // (C) w = p - (tau / 2) (p^T v) v over the whole trailing range (p^T v summed in rank order)
         float s = 0.0f;
-        for (int q = 0; q < kClusterCtas; ++q) s += ld_remote(&part[cur], q);
+        for (int q = 0; q < C; ++q) s += part[cur * kMaxClusterCtas + q];
         const float c = -0.5f * tau * s;
-        for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads)
-            wc[j] = fmaf(c, vc[j], ld_remote(&pb[j], static_cast<uint32_t>(j % kClusterCtas)));
+        for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads) wc[j] = fmaf(c, vc[j], pb[j]);
         __syncthreads();
-        if ((k + 1) % kClusterCtas == r) {  // the next pivot row, updated now
-            float* row = Wb + static_cast<int64_t>(k + 1) * N;
-            const float vi = vc[k + 1], wi = wc[k + 1];
-            for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads)
-                row[j] -= __fmul_rn(vi, wc[j]) + __fmul_rn(wi, vc[j]);
-        }
-        if (r == 0) {  // row k is read by nobody after B1: it keeps the reflector
+        if (r == 0) {  // row k is read by nobody any more: it keeps the reflector
             float* rowv = Wb + static_cast<int64_t>(k) * N;
             for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads) rowv[j] = vc[j];
             if (threadIdx.x == 0) {
-                d_out[static_cast<int64_t>(b) * N + k] = dk;
-                e_out[static_cast<int64_t>(b) * N + k] = beta;
-                tau_out[static_cast<int64_t>(b) * N + k] = tau;
+                db[k] = R.d;
+                eb[k] = R.beta;
+                tb[k] = tau;
             }
         }
-        cluster_barrier();  // B2: row k + 1 is visible; nobody reads this step's p any more
-    }
-    // the last column's update of row N-1 (rows <= N-2 are final), then the trailing 2 x 2 (or 1 x 1) block
-    if (N >= 3) {
-        const int last = (N - 3) & 1;
-        const float* vp = vbuf[last];
-        const float* wp = wbuf[last];
-        if ((N - 1) % kClusterCtas == r && threadIdx.x < 2) {
-            const int j = N - 2 + threadIdx.x;
-            float* row = Wb + static_cast<int64_t>(N - 1) * N;
-            row[j] -= __fmul_rn(vp[N - 1], wp[j]) + __fmul_rn(wp[N - 1], vp[j]);
+        // row k + 1 with column k's update, in registers: the next reflector (or, after the last one, T's trailing
+        // 2 x 2 block)
+        const float* rown = Wb + static_cast<int64_t>(k + 1) * N;
+        const float vk1 = vc[k + 1], wk1 = wc[k + 1];
+        if (k + 3 < N) {
+            float ss = 0.0f;
+            for (int j = k + 1 + threadIdx.x; j < N; j += kSytrdThreads) {
+                const float x = __ldcg(rown + j) - (__fmul_rn(vk1, wc[j]) + __fmul_rn(wk1, vc[j]));
+                if (j == k + 1) scal2[0] = x;
+                else if (j == k + 2) scal2[1] = x;
+                else {
+                    vn[j] = x;
+                    ss = fmaf(x, x, ss);
+                }
+            }
+            // the reduction synchronises the CTA before scal2 is read
+            const float sig = block_sum(ss, red);
+            const float dn = scal2[0], alpha = scal2[1];
+            Reflector Rn{dn, alpha, 0.0f};
+            float scl = 0.0f;
+            if (sig > 0.0f) {
+                Rn.beta = -copysignf(sqrtf(fmaf(alpha, alpha, sig)), alpha);
+                Rn.tau = (Rn.beta - alpha) / Rn.beta;
+                scl = 1.0f / (alpha - Rn.beta);
+            }
+            for (int j = k + 3 + threadIdx.x; j < N; j += kSytrdThreads) vn[j] *= scl;
+            if (threadIdx.x == 0) vn[k + 2] = 1.0f;
+            __syncthreads();
+            R = Rn;
+        } else if (r == 0 && threadIdx.x == 0) {  // k = N - 3: rows N - 2 and N - 1 get column k's update
+            const float* rowl = Wb + static_cast<int64_t>(N - 1) * N;
+            const float vl = vc[N - 1], wl = wc[N - 1];
+            db[N - 2] = __ldcg(rown + N - 2) - (__fmul_rn(vk1, wc[N - 2]) + __fmul_rn(wk1, vc[N - 2]));
+            eb[N - 2] = __ldcg(rown + N - 1) - (__fmul_rn(vk1, wc[N - 1]) + __fmul_rn(wk1, vc[N - 1]));
+            db[N - 1] = __ldcg(rowl + N - 1) - (__fmul_rn(vl, wc[N - 1]) + __fmul_rn(wl, vc[N - 1]));
         }
     }
-    cluster_barrier();
     if (r == 0 && threadIdx.x == 0) {
-        float* d = d_out + static_cast<int64_t>(b) * N;
-        float* e = e_out + static_cast<int64_t>(b) * N;
-        float* t = tau_out + static_cast<int64_t>(b) * N;
-        if (N >= 2) {
-            d[N - 2] = __ldcg(Wb + static_cast<int64_t>(N - 2) * N + (N - 2));
-            e[N - 2] = __ldcg(Wb + static_cast<int64_t>(N - 2) * N + (N - 1));
-            t[N - 2] = 0.0f;
+        if (N == 2) {
+            db[0] = Wb[0];
+            eb[0] = Wb[1];
+            db[1] = Wb[N + 1];
+        } else if (N == 1) {
+            db[0] = Wb[0];
         }
-        d[N - 1] = __ldcg(Wb + static_cast<int64_t>(N - 1) * N + (N - 1));
-        e[N - 1] = 0.0f;
-        t[N - 1] = 0.0f;
+        eb[N - 1] = 0.0f;
+        tb[N - 1] = 0.0f;
+        if (N >= 2) tb[N - 2] = 0.0f;
     }
     cluster_barrier();  // no CTA leaves while another may still read its shared memory
 }
@@ -295,8 +384,13 @@ __device__ __forceinline__ double start_value(int i, int j) {
 }
 
 // grid (ceil(N / 128), batch), one thread per eigenvalue index j.  Scratch S (batch, 3, N, N) FP64: S[0] the
-// reciprocal LDL^T pivots 1 / D, S[1] the multipliers L, S[2] the iterate x, element i of thread j at [i * N + j] (coalesced over a
-// warp's consecutive j).  Z (batch, N, N) FP32: eigenvector j of T in column j.
+// reciprocal LDL^T pivots 1 / D, S[1] the multipliers L, S[2] the iterate x, element i of thread j at [i * N + j]
+// (coalesced over a warp's consecutive j).  Z (batch, N, N) FP32: eigenvector j of T in column j.
+//
+// Each pass over a vector is a recurrence (one FP64 FMA per element on the previous element's result), so the loads
+// it needs are issued kInvitBlock elements ahead into registers: the recurrence then waits only on FMA latency, not
+// on a memory round trip per element.  The iterate is normalised lazily: the next solve scales it on the fly.
+// Members of a cluster of close eigenvalues get slightly separated shifts (their cluster is orthonormalised after).
 __global__ void __launch_bounds__(128)
 k_tridiag_invit(const float* __restrict__ d_all, const float* __restrict__ e_all, const float* __restrict__ evals,
                 const float* __restrict__ tnorm_all, int N, double* __restrict__ S, float* __restrict__ Z) {
@@ -308,68 +402,126 @@ k_tridiag_invit(const float* __restrict__ d_all, const float* __restrict__ e_all
     const float* lam = evals + static_cast<int64_t>(b) * N;
     const double tnorm = static_cast<double>(tnorm_all[b]);
     const double tol = kClusterTol * tnorm;
-    // j runs the cluster that starts at j; a thread whose eigenvalue continues a cluster has nothing to do
+    int j0 = j;  // first index of j's cluster
+    while (j0 > 0 && static_cast<double>(lam[j0]) - static_cast<double>(lam[j0 - 1]) < tol) --j0;
+    const double lm = static_cast<double>(lam[j]) + (j - j0) * 1e-3 * tol;
+    const int64_t NN = static_cast<int64_t>(N) * N;
+    double* __restrict__ D = S + (static_cast<int64_t>(b) * 3 + 0) * NN + j;
+    double* __restrict__ L = S + (static_cast<int64_t>(b) * 3 + 1) * NN + j;
+    double* __restrict__ X = S + (static_cast<int64_t>(b) * 3 + 2) * NN + j;
+    float* Zb = Z + static_cast<int64_t>(b) * NN;
+    const double pivmin = 1e-14 * tnorm + 1e-300;
+    constexpr int B = kInvitBlock;
+    // LDL^T of T - lm I as the multipliers L and the reciprocal pivots 1 / D, with the first solve's forward pass
+    // z_i = x_i - L_{i-1} z_{i-1} on the pseudo-random start x
+    double dcur = static_cast<double>(db[0]) - lm;
+    if (fabs(dcur) < pivmin) dcur = -pivmin;
+    double inv = 1.0 / dcur;
+    double z = start_value(0, j);
+    D[0] = inv;
+    X[0] = z;
+    for (int i = 1; i < N; ++i) {
+        const double ei = static_cast<double>(eb[i - 1]);
+        const double l = ei * inv;
+        dcur = (static_cast<double>(db[i]) - lm) - l * ei;
+        if (fabs(dcur) < pivmin) dcur = -pivmin;
+        inv = 1.0 / dcur;
+        z = fma(-l, z, start_value(i, j));
+        L[static_cast<int64_t>(i - 1) * N] = l;
+        D[static_cast<int64_t>(i) * N] = inv;
+        X[static_cast<int64_t>(i) * N] = z;
+    }
+    double sc = 1.0;  // pending scale of X
+    for (int it = 0; it < kInvitSolves; ++it) {
+        if (it > 0) {  // forward: z_i = sc x_i - L_{i-1} z_{i-1}
+            z = sc * X[0];
+            X[0] = z;
+            for (int i0 = 1; i0 < N; i0 += B) {
+                double xb[B], lb[B];
+#pragma unroll
+                for (int u = 0; u < B; ++u) {
+                    const int i = i0 + u;
+                    xb[u] = i < N ? X[static_cast<int64_t>(i) * N] : 0.0;
+                    lb[u] = i < N ? L[static_cast<int64_t>(i - 1) * N] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < B; ++u) {
+                    const int i = i0 + u;
+                    if (i < N) {
+                        z = fma(-lb[u], z, sc * xb[u]);
+                        X[static_cast<int64_t>(i) * N] = z;
+                    }
+                }
+            }
+        }
+        // backward: y_i = z_i / D_i - L_i y_{i+1}
+        double y = X[static_cast<int64_t>(N - 1) * N] * D[static_cast<int64_t>(N - 1) * N];
+        X[static_cast<int64_t>(N - 1) * N] = y;
+        double nrm = y * y;
+        for (int i0 = N - 2; i0 >= 0; i0 -= B) {
+            double xb[B], db2[B], lb[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                const int i = i0 - u;
+                xb[u] = i >= 0 ? X[static_cast<int64_t>(i) * N] : 0.0;
+                db2[u] = i >= 0 ? D[static_cast<int64_t>(i) * N] : 0.0;
+                lb[u] = i >= 0 ? L[static_cast<int64_t>(i) * N] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                const int i = i0 - u;
+                if (i >= 0) {
+                    y = fma(xb[u], db2[u], -lb[u] * y);
+                    X[static_cast<int64_t>(i) * N] = y;
+                    nrm = fma(y, y, nrm);
+                }
+            }
+        }
+        sc = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+    }
+    for (int i = 0; i < N; ++i) Zb[static_cast<int64_t>(i) * N + j] = static_cast<float>(sc * X[static_cast<int64_t>(i) * N]);
+}
+
+// grid (ceil(N / 4), batch), 128 threads: a warp per eigenvalue index j; the warp of each cluster's first eigenvalue
+// orthonormalises the cluster's columns of Z (modified Gram-Schmidt, lanes over the rows, FP64 sums)
+__global__ void __launch_bounds__(128)
+k_cluster_orth(const float* __restrict__ evals, const float* __restrict__ tnorm_all, int N, float* __restrict__ Z) {
+    const int b = blockIdx.y;
+    const int j = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (j >= N) return;
+    const float* lam = evals + static_cast<int64_t>(b) * N;
+    const double tol = kClusterTol * static_cast<double>(tnorm_all[b]);
     if (j > 0 && static_cast<double>(lam[j]) - static_cast<double>(lam[j - 1]) < tol) return;
     int jend = j + 1;
     while (jend < N && static_cast<double>(lam[jend]) - static_cast<double>(lam[jend - 1]) < tol) ++jend;
-    const int64_t NN = static_cast<int64_t>(N) * N;
-    double* D = S + (static_cast<int64_t>(b) * 3 + 0) * NN;
-    double* L = S + (static_cast<int64_t>(b) * 3 + 1) * NN;
-    double* X = S + (static_cast<int64_t>(b) * 3 + 2) * NN;
-    float* Zb = Z + static_cast<int64_t>(b) * NN;
-    const double pivmin = 1e-14 * tnorm + 1e-300;
+    if (jend - j < 2) return;
+    float* Zb = Z + static_cast<int64_t>(b) * N * N;
     for (int m = j; m < jend; ++m) {
-        // members of a cluster get slightly separated shifts so that their LDL^T factors differ
-        const double lm = static_cast<double>(lam[m]) + (m - j) * 1e-3 * tol;
-        // LDL^T of T - lm I, kept as the multipliers L and the reciprocal pivots 1 / D (in the column of thread j,
-        // reused by the cluster's members in turn): one FP64 division per row, none in the solves
-        double dcur = static_cast<double>(db[0]) - lm;
-        if (fabs(dcur) < pivmin) dcur = -pivmin;
-        double inv = 1.0 / dcur;
-        D[j] = inv;
-        for (int i = 1; i < N; ++i) {
-            const double ei = static_cast<double>(eb[i - 1]);
-            const double l = ei * inv;
-            dcur = (static_cast<double>(db[i]) - lm) - l * ei;
-            if (fabs(dcur) < pivmin) dcur = -pivmin;
-            inv = 1.0 / dcur;
-            L[static_cast<int64_t>(i - 1) * N + j] = l;
-            D[static_cast<int64_t>(i) * N + j] = inv;
+        for (int q = j; q < m; ++q) {
+            double pr = 0.0;
+            for (int i = lane; i < N; i += 32)
+                pr = fma(static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]),
+                         static_cast<double>(Zb[static_cast<int64_t>(i) * N + m]), pr);
+            pr = warp_sum(pr);
+            for (int i = lane; i < N; i += 32) {
+                float* zm = Zb + static_cast<int64_t>(i) * N + m;
+                *zm = static_cast<float>(static_cast<double>(*zm) - pr * static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]));
+            }
+            __syncwarp();
         }
-        for (int i = 0; i < N; ++i) X[static_cast<int64_t>(i) * N + j] = start_value(i, m);
-        for (int it = 0; it < kInvitSolves; ++it) {
-            // forward: z_i = x_i - L_{i-1} z_{i-1}; backward: y_i = z_i / D_i - L_i y_{i+1}
-            double z = X[j];
-            for (int i = 1; i < N; ++i) {
-                z = X[static_cast<int64_t>(i) * N + j] - L[static_cast<int64_t>(i - 1) * N + j] * z;
-                X[static_cast<int64_t>(i) * N + j] = z;
-            }
-            double y = X[static_cast<int64_t>(N - 1) * N + j] * D[static_cast<int64_t>(N - 1) * N + j];
-            X[static_cast<int64_t>(N - 1) * N + j] = y;
-            double nrm = y * y;
-            for (int i = N - 2; i >= 0; --i) {
-                y = X[static_cast<int64_t>(i) * N + j] * D[static_cast<int64_t>(i) * N + j] -
-                    L[static_cast<int64_t>(i) * N + j] * y;
-                X[static_cast<int64_t>(i) * N + j] = y;
-                nrm = fma(y, y, nrm);
-            }
-            // orthogonalise against the cluster's earlier vectors (already written to Z), then normalise
-            for (int q = j; q < m; ++q) {
-                double pr = 0.0;
-                for (int i = 0; i < N; ++i)
-                    pr = fma(static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]), X[static_cast<int64_t>(i) * N + j], pr);
-                nrm = 0.0;
-                for (int i = 0; i < N; ++i) {
-                    const double v = X[static_cast<int64_t>(i) * N + j] - pr * static_cast<double>(Zb[static_cast<int64_t>(i) * N + q]);
-                    X[static_cast<int64_t>(i) * N + j] = v;
-                    nrm = fma(v, v, nrm);
-                }
-            }
-            const double sc = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
-            for (int i = 0; i < N; ++i) X[static_cast<int64_t>(i) * N + j] *= sc;
+        double nrm = 0.0;
+        for (int i = lane; i < N; i += 32) {
+            const double v = static_cast<double>(Zb[static_cast<int64_t>(i) * N + m]);
+            nrm = fma(v, v, nrm);
         }
-        for (int i = 0; i < N; ++i)
-            Zb[static_cast<int64_t>(i) * N + m] = static_cast<float>(X[static_cast<int64_t>(i) * N + j]);
+        nrm = warp_sum(nrm);
+        const double sc = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+        for (int i = lane; i < N; i += 32) {
+            float* zm = Zb + static_cast<int64_t>(i) * N + m;
+            *zm = static_cast<float>(sc * static_cast<double>(*zm));
+        }
+        __syncwarp();
     }
 }
 
@@ -420,7 +572,7 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
                 int n_refl, int nblocks, float* __restrict__ U) {
     extern __shared__ float sm[];
     float* Zt = sm;                          // N x kTile
-    float* Vc = Zt + N * kTile;              // kChunk x kWy
+    float* Vc = Zt + N * kTile;              // kWy x kChunk: Vc[a * kChunk + ii] = v_{k0+a}[i0 + ii]
     __shared__ float Sm[kWy][kTile + 1];
     __shared__ float Sp[kWy][kTile + 1];
     __shared__ float Tm[kWy][kWy + 1];
@@ -444,15 +596,15 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
         // S = V^T Z over the block's rows, V staged kChunk rows at a time (V[i][a] = v_{k0+a}[i])
         for (int i0 = r0; i0 < N; i0 += kChunk) {
             __syncthreads();
-            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {
-                const int ii = t / kWy, aa = t % kWy, i = i0 + ii, k = k0 + aa;
+            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {  // consecutive threads: one row of W
+                const int aa = t / kChunk, ii = t % kChunk, i = i0 + ii, k = k0 + aa;
                 float v = 0.0f;
                 if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
                 Vc[t] = v;
             }
             __syncthreads();
             const int iend = min(kChunk, N - i0);
-            for (int ii = 0; ii < iend; ++ii) s = fmaf(Vc[ii * kWy + a], Zt[(i0 + ii) * kTile + cc], s);
+            for (int ii = 0; ii < iend; ++ii) s = fmaf(Vc[a * kChunk + ii], Zt[(i0 + ii) * kTile + cc], s);
         }
         Sm[a][cc] = s;
         __syncthreads();
@@ -464,8 +616,8 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
         // Z -= V S'
         for (int i0 = r0; i0 < N; i0 += kChunk) {
             __syncthreads();
-            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {
-                const int ii = t / kWy, aa = t % kWy, i = i0 + ii, k = k0 + aa;
+            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {  // consecutive threads: one row of W
+                const int aa = t / kChunk, ii = t % kChunk, i = i0 + ii, k = k0 + aa;
                 float v = 0.0f;
                 if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
                 Vc[t] = v;
@@ -476,7 +628,7 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
                 const int ii = t / kTile, c = t % kTile;
                 float acc = Zt[(i0 + ii) * kTile + c];
 #pragma unroll
-                for (int m = 0; m < kWy; ++m) acc = fmaf(-Vc[ii * kWy + m], Sp[m][c], acc);
+                for (int m = 0; m < kWy; ++m) acc = fmaf(-Vc[m * kChunk + ii], Sp[m][c], acc);
                 Zt[(i0 + ii) * kTile + c] = acc;
             }
         }
@@ -536,17 +688,22 @@ int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStrea
     FLMM_CUDA(cudaMemcpyAsync(W, A, 4 * NN * batch, cudaMemcpyDeviceToDevice, st));
     // 1. tridiagonalisation, one cluster per matrix
     const int Np = (N + 3) & ~3;
-    const size_t smem1 = sizeof(float) * (6 * static_cast<size_t>(Np) + 34);
+    const size_t smem1 = sizeof(float) * (6 * static_cast<size_t>(Np) + 32 + 2 * kMaxClusterCtas + 2);
+    // cluster size: as many CTAs per matrix as fill the SMs once (one CTA per SM), 2 to 8
+    int dev = 0, sms = 0;
+    FLMM_CUDA(cudaGetDevice(&dev));
+    FLMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int C = std::max(2, std::min(kMaxClusterCtas, sms / std::max(batch, 1)));
     // (per device, so set on every call; the call is cheap)
     FLMM_CUDA(cudaFuncSetAttribute(k_sytrd_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     FLMM_CUDA(cudaFuncSetAttribute(k_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(C);
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(static_cast<unsigned>(kClusterCtas * batch), 1, 1);
+    cfg.gridDim = dim3(static_cast<unsigned>(C * batch), 1, 1);
     cfg.blockDim = dim3(kSytrdThreads, 1, 1);
     cfg.dynamicSmemBytes = smem1;
     cfg.stream = st;
@@ -562,6 +719,8 @@ int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStrea
     // 3. eigenvectors of T
     k_tridiag_invit<<<dim3(ceil_div(N, 128), batch), 128, 0, st>>>(d, e, evals, tn, N, S, Z);
     if ((rc = check_launch("k_tridiag_invit"))) return rc;
+    k_cluster_orth<<<dim3(ceil_div(N, 4), batch), 128, 0, st>>>(evals, tn, N, Z);
+    if ((rc = check_launch("k_cluster_orth"))) return rc;
     // 4. back-transformation into A
     const int n_refl = N > 2 ? N - 2 : 0;
     if (L.nblocks > 0) {
