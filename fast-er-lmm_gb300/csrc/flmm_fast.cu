@@ -33,6 +33,7 @@
 #include <mutex>
 
 #include "flmm_common.cuh"
+#include "flmm_split.cuh"
 #include "flmm_tc.cuh"
 
 using namespace flmm;
@@ -719,25 +720,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
 
 // ---- operand preparation ---------------------------------------------------------------------------------------
 
-__device__ __forceinline__ float row_scale_exp(float amax, int* e_out) {
-    // exponent e with amax * 2^e in [2^14, 2^15); rows of zeros keep e = 0
-    int e = 0;
-    if (amax > 0.0f && isfinite(amax)) {
-        int ex;
-        frexpf(amax, &ex);  // amax = m 2^ex, m in [0.5, 1)
-        e = 15 - ex;
-    }
-    *e_out = e;
-    return ldexpf(1.0f, e);
-}
-
-__device__ __forceinline__ void split_store(float x, float mul, __half* hi, __half* lo, int64_t o) {
-    const float xs = x * mul;  // exact: power-of-two scale
-    const __half h = __float2half_rn(xs);
-    hi[o] = h;
-    lo[o] = __float2half_rn(xs - __half2float(h));
-}
-
 template <typename T>
 __global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __restrict__ hi,
                              __half* __restrict__ lo, int64_t ldo, float* __restrict__ scale) {
@@ -1322,6 +1304,20 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
                                    int R, const int64_t* rows, double* f, double* beta, double* se, double* sfve,
                                    int64_t ldo, double* max_F, float f_refine, int32_t* flag_count,
                                    int32_t* flags, int flag_cap, void* stream) {
+    return flmm_wald_split_f16_df(ctx, A1h, A1l, lda, sa1, Lh, Ll, ldl, sl, rWr, rWr0, P, n_real, B1h, B1l, ldb, sb1,
+                                  Fh, Fl, ldf, sf, Mc, Neff, R, rows, f, beta, se, sfve, ldo, max_F, f_refine,
+                                  flag_count, flags, flag_cap, Neff - 1, stream);
+}
+
+extern "C" int flmm_wald_split_f16_df(flmm_context* ctx, const void* A1h, const void* A1l, int64_t lda,
+                                      const float* sa1, const void* Lh, const void* Ll, int64_t ldl, const float* sl,
+                                      const float* rWr, const float* rWr0, int P, int n_real, const void* B1h,
+                                      const void* B1l, int64_t ldb, const float* sb1, const void* Fh, const void* Fl,
+                                      int64_t ldf, const float* sf, int Mc, int Neff, int R, const int64_t* rows,
+                                      double* f, double* beta, double* se, double* sfve, int64_t ldo, double* max_F,
+                                      float f_refine, int32_t* flag_count, int32_t* flags, int flag_cap, int var_df,
+                                      void* stream) {
+    FLMM_REQUIRE(var_df > 0, "flmm_wald_split_f16_df: var_df must be positive");
     FLMM_REQUIRE(ctx && A1h && A1l && sa1 && Lh && Ll && sl && rWr && rWr0 && B1h && B1l && sb1 && Fh && Fl && sf && max_F &&
                      Neff > 1 && R > 0 && P >= 0 && Mc >= 0 && n_real >= 0 && n_real <= P && lda >= Neff &&
                      ldb >= Neff && ldl >= R && ldf >= R,
@@ -1358,7 +1354,7 @@ extern "C" int flmm_wald_split_f16(flmm_context* ctx, const void* A1h, const voi
     a.rWr = rWr;
     a.rWr0 = rWr0;
     a.n_real = n_real;
-    a.var_df = static_cast<float>(Neff - 1);
+    a.var_df = static_cast<float>(var_df);
     a.rows = rows;
     a.f = f;
     a.beta = beta;
