@@ -13,7 +13,7 @@ device; ``e2e`` times the same call with host (pinned) inputs and host outputs, 
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast|plain] [--impl ours|reference]
                   [--delta grid|learned] [--no-pipeline] [--B B] [--M M] [--no-e2e] [--no-cpu-baseline]
-                  [--no-plain] [--plain-chroms C] [--workload headline|c3]
+                  [--no-plain] [--plain-chroms C] [--workload headline|c3|c5]
 
 Besides ``value`` and ``e2e`` the line carries the metric's own ratio (``chosen_vs_plain``: the plain FP64 form and
 the chosen form timed on the same bounded subset of the workload, its first C chromosomes), the real-only rate,
@@ -26,6 +26,10 @@ runs each chromosome's delta fit on the main stream instead of one chromosome ah
 ``--workload c3`` runs the uneven-batching shape instead: 5,000 samples x 500,000 variants over 22 chromosomes of
 human proportions, 2,000 phenotypes in 12 missingness patterns (groups of 3,000-5,000 samples), 1,000 permutations
 for 50 phenotypes and 10 for the rest, every group on its own strain subset (fasterlmm_gb300.groups).
+
+``--workload c5`` runs the low-rank large-cohort shape (fasterlmm_gb300.lowrank_fast): 50,000 samples, a 2,000-marker
+kinship factor, 100 phenotypes x (1 + 10 permutations), int8 genotypes streamed from pinned host memory in 8,192-
+variant blocks (200,000 tested variants by default, --M up to 1,000,000).
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm (oracle/flmm_oracle.py) on the host's
 cores on a bounded sample of the same workload (one chromosome x one 256-phenotype batch per step).
@@ -140,7 +144,7 @@ def measured_peaks() -> dict:
 # --workload: the headline shape, or the uneven-batching shape (5,000 samples x 500,000 variants over 22
 # human-sized chromosomes, 2,000 phenotypes in 12 missingness patterns, 1,000 permutations for 50 of them and 10
 # for the rest)
-WORKLOADS = {"headline": WORKLOAD, "c3": "n5000_m500k_b2000_na12"}
+WORKLOADS = {"headline": WORKLOAD, "c3": "n5000_m500k_b2000_na12", "c5": "n50000_k2000_m1m_b100_perm10"}
 
 
 def make_inputs(B: int | None, M: int | None, name: str = WORKLOAD):
@@ -469,6 +473,104 @@ def run_grouped(args):
         dist.destroy_process_group()
 
 
+def run_lowrank(args):
+    """
+    The low-rank large-cohort shape through fasterlmm_gb300.lowrank_fast: 50,000 samples, a 2,000-marker kinship
+    factor, tested variants (int8 dosages in pinned host memory) streamed to the device in 8,192-variant blocks
+    while the previous block is scanned, 100 phenotypes x (1 + 10 permutations).  One step = the whole LOCO scan:
+    22 per-chromosome bases (FP64 k x k eigendecompositions), phenotype rotations and FP64 delta fits, and every
+    block's split-FP16 products and fused Wald.  The tested-variant count defaults to 200,000 (10 GB of dosages on
+    the host; --M sets it, up to the spec's 1,000,000).
+    """
+    import torch
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from fasterlmm_gb300 import _lib, build, lowrank_fast, perms
+    from fasterlmm_gb300.core import _ptr, transpose
+    from fasterlmm_gb300.synth import make_lowrank_workload
+    build()
+    name = WORKLOADS[args.workload]
+    t_gen = time.perf_counter()
+    d, w = make_lowrank_workload(name, M=args.M or 200_000, B=args.B)
+    t_gen = time.perf_counter() - t_gen
+    N, k, M, B, n_perm, D = w["N"], w["k_kin"], w["M"], w["B"], w["n_perm"], w["D"]
+    P = B * (1 + n_perm)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    Gkt = t(d.Gk.T)                                                   # (k, N) int8, marker-major
+    Zkt = torch.empty((k, N), dtype=torch.float64, device=dev)
+    _lib.call("flmm_standardise_dosage", _ptr(Gkt), N, N, k, _ptr(Zkt), N, None)
+    Gk_std = transpose(Zkt)                                           # (N, k) standardised factor
+    orders = torch.from_numpy(perms.perm_orders(N, range(B), n_perm)).to(dev)
+    Yt_all = perms.pack_perm_columns(transpose(t(d.Y)), orders)
+    Y_all = transpose(Yt_all)                                         # (N, P): reals, then permutations
+    X = t(d.X)
+    Gt_host = torch.from_numpy(d.Gt).pin_memory()
+    del d.Gt
+    rows_of = {int(c): np.flatnonzero(d.chrom == c) for c in np.unique(d.chrom)}
+    chroms = sorted(rows_of)
+    grid_kw = dict(n_grid=w["n_grid"], log_delta_min=w["log_delta_min"], log_delta_max=w["log_delta_max"])
+
+    def step(tm=None):
+        src = lowrank_fast.dosage_blocks(Gt_host, rows_of, dev)
+        return lowrank_fast.loco_scan_blocks_fast(Gk_std, d.chrom_kin, src, M, chroms, X, Y_all, n_real=B, timers=tm,
+                                                  **grid_kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    launches0 = _lib.kernel_launches()
+    timers: dict = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = step(timers)
+        del out
+    ev1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    launches = _lib.kernel_launches() - launches0
+    clk = clocks.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    value = M * P * args.steps / elapsed
+    stages = {kk: round(sum(a.elapsed_time(b) for a, b in v if b is not None) / args.steps, 3)
+              for kk, v in timers.items()}
+    peaks = measured_peaks()
+    # the fused Wald launches of a step: 4 (k_c + N) flop per test (the on-rank and off-rank dot products)
+    wald_s = stages.get("wald", 0.0) / 1e3
+    wald_flop = 4.0 * (k + N) * P * M
+    roof = None
+    if wald_s > 0:
+        ach = wald_flop / wald_s / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peaks["tensor_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["tensor_tflops"], "traffic": None,
+                "kernel": "k_pair<2> over K = k + N (fused split-FP16 low-rank Wald) with its block's operand prep",
+                "wald_ms_per_step": 1e3 * wald_s, "algorithmic_flop_per_step": wald_flop,
+                "peak_source": peaks["source"] + " bf16 dense (FP16 rate is the same)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp16x2-split tensor (FP32 acc) + f64",
+            "data": "synthetic (seeded: Binomial(2, MAF~U[0.05,0.5]) int8 genotypes, RINT phenotypes, "
+                    "h2~U[0.1,0.7], 10 causal)",
+            "config": {"workload": name, "N": N, "k_kin": k, "M": M, "B": B, "n_perm": n_perm, "P": P,
+                       "chromosomes": w["n_chrom"], "covariates": D, "grid": w["n_grid"], "block": lowrank_fast.BLOCK,
+                       "h2d_bytes_per_step": int(M) * N,
+                       "stream": "int8 dosages in pinned host memory, copied per block on a side stream beside the "
+                                 "previous block's scan, standardised on the device",
+                       "l2": "inputs larger than L2 (each block's split operands 1.7 GB)",
+                       "parallelism": f"{world} replica(s), no cross-GPU exchange"},
+            "wall_s_timed": wall, "gpu_launches": launches, "roofline": roof, "stage_ms_per_step": stages,
+            "generate_s": round(t_gen, 1), "e2e": None, "cpu_baseline": None,
+            "notes": "genotypes cross from host memory inside every step; outputs stay on the device; no CPU sample "
+                     "for this shape (one LOCO basis at N = 50,000 is ~4e11 flop on the host)",
+            "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def fp32_peak_tflops() -> float:
     import torch
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
@@ -585,10 +687,13 @@ def main():
     ap.add_argument("--plain-chroms", type=int, default=2,
                     help="chromosomes of the workload that the plain-form comparison scans (default 2 of 20)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="headline",
-                    help="headline: 1,000 x 100,000 x 6,484 phenotypes; c3: the uneven-batching shape")
+                    help="headline: 1,000 x 100,000 x 6,484 phenotypes; c3: the uneven-batching shape; c5: the "
+                         "low-rank large cohort (50,000 samples, streamed genotypes)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c5":
+        run_lowrank(args)
     elif args.workload != "headline":
         run_grouped(args)
     else:

@@ -108,7 +108,11 @@ SIGNATURES: dict[str, list] = {
                                _i64, _p, _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, C.c_float, _p, _p, _i, _i, _p],
     "flmm_lr_prep_columns": [_p, _i, _p, _i64, _p, _i64, _i, _p, _p, _i, _p, C.c_double, C.c_double, _i, _p, _p,
                              _i64, _p, _p, _i64, _p, _p, _p, _p, _p],
-    "flmm_lr_prep_variants": [_p, _i64, _p, _i64, _i, _i, _i, _p, _i64, _i, _p, _p, _i64, _p, _p, _p, _i64, _p, _p],
+    "flmm_lr_prep_variants": [_p, _i64, _p, _i64, _p, _i64, _i, _i, _i, _p, _i64, _i, _p, _p, _i64, _p, _p, _p, _i64,
+                              _p, _p],
+    "flmm_lr_residual": [_p, _i64, _p, _i64, _i, _i, _p, _i64, _p, _p],
+    "flmm_lr_wald_refine": [_p, _p, _i, C.c_float, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p, _i, _i,
+                            _i, _i, _i, _p, _p, _p, _p, _p, _i64, _p, _p],
     "flmm_lr_interp_nodes": [_p, _i, _p, C.c_double, C.c_double, _i, _p, _i64, _p],
     "flmm_wald_refine_f32": [_p, _p, _p, _i, C.c_float, _p, _i64, _p, _i64, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p,
                              _i64, _p, _p],

@@ -135,12 +135,16 @@ def standardise_columns_t(Z, dev: torch.device | None = None) -> Tensor:
 
 
 def standardise_columns(arr):
-    """Drop-in for io.standardise_columns (fasterlmm/io.py:223-254): same shape and type back."""
+    """Drop-in for io.standardise_columns (fasterlmm/io.py:223-254): same shape and type back.  Computed in FP64; a
+    floating-point tensor comes back in its own dtype, as the reference's torch branch returns it (io.py:235-246),
+    and an array as FP64, as its numpy branch does."""
     src_dev = arr.device if isinstance(arr, Tensor) else None
     Zt = standardise_columns_t(arr)
     out = Zt.T
     if isinstance(arr, np.ndarray):
         return out.cpu().numpy()
+    if arr.is_floating_point() and arr.dtype != F64:
+        out = out.to(arr.dtype)
     return out if src_dev is None or src_dev.type == "cuda" else out.to(src_dev)
 
 

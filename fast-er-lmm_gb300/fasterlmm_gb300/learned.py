@@ -264,16 +264,142 @@ def train(out: Path, *, n_sets: int = 48, steps: int = 4000, seed: int = 2024060
     return info
 
 
+# ---- the learned-proposal configuration: training and held-out evaluation at one cohort shape -------------------
+
+def _simulate(Zt: Tensor, B: int, seed: int) -> Tensor:
+    """B phenotypes (B, N) on the device from standardised genotypes Zt (M, N) by the method's simulator recipe
+    (fasterlmm/sim.py:21-28) with per-phenotype h2 ~ U[0, 0.95], 1-500 causal variants and effects N(0, h2 / k)."""
+    M, N = Zt.shape
+    rng = np.random.default_rng([seed, 4, 1])
+    Yt = torch.empty((B, N), dtype=F64, device=Zt.device)
+    for b in range(B):
+        h2 = rng.uniform(0.0, 0.95)
+        k = int(rng.integers(1, 501))
+        idx = torch.from_numpy(rng.choice(M, size=k, replace=False)).to(Zt.device)
+        beta = torch.from_numpy(rng.standard_normal(k) * np.sqrt(h2 / k)).to(Zt.device)
+        noise = torch.from_numpy(rng.standard_normal(N) * np.sqrt(1.0 - h2)).to(Zt.device)
+        Yt[b] = beta @ Zt.index_select(0, idx) + noise
+    return Yt
+
+
+def config4(out_weights: Path, *, N: int = 2000, M: int = 50_000, n_train: int = 20_000, n_eval: int = 10_000,
+            n_perm: int = 100, steps: int = 4000, n_grid: int = 200, seed: int = 20250404, wald_variants: int = 2000,
+            timers: bool = True) -> dict:
+    """
+    Train the proposal on n_train phenotypes of one simulated cohort (N x M, single kinship of all variants; labels
+    from the exact fit on an n_grid-point grid) with the library's training kernels, then evaluate it on n_eval
+    held-out phenotypes x (1 + n_perm) columns against the full grid: grid evaluations saved, fallback rate, lost
+    audits, |d log delta|, and |d(-log10 p)| of a fused Wald scan of `wald_variants` variants under either fit.
+    """
+    from .core import ScanResult
+    from .fast import SplitRows, WaldOperands, _eigh_batched_f32_refined, _spectrum, fit_delta_fast, gemm_split, \
+        wald_fast
+    from .perms import pack_perm_columns, perm_orders_device
+    from .post import neg_log10_pvalue
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ctx = _lib.context(dev.index)
+    from .synth import make_dataset
+    t0 = time.time()
+    d = make_dataset(N, M, 22, 1, 1, seed=seed, config_id=4, maf_lo=0.05, k_lo=1, k_hi=1)
+    Zt = standardise_columns_t(torch.from_numpy(d.Z_float()).to(dev), dev)
+    del d
+    Yt = _simulate(Zt, n_train + n_eval, seed)
+    t_sim = time.time() - t0
+    X = torch.ones((N, 1), dtype=F64, device=dev)
+    basis = CovariateBasis(X)
+    Kp = torch.empty((1, N, N), dtype=F64, device=dev)
+    project_kinship(kinship_from_gram(gram_t(Zt), None, M), basis, Kp[0])
+    U, ev = _eigh_batched_f32_refined(ctx, Kp)
+    D = 1
+    s = _spectrum(ev[0], D)
+    Us = SplitRows.of(U[0, D:])
+
+    def rotate(Yt):
+        Yr = basis.regress_out(Yt)
+        out = torch.empty((Yr.shape[0], N - D), dtype=F32, device=dev)
+        gemm_split(ctx, SplitRows.of(Yr).view(), Us.view(), out)
+        return out
+
+    # training: features and exact-fit labels of the training phenotypes
+    UY_tr = rotate(Yt[:n_train])
+    lab, _ = fit_delta_fast(s, UY_tr, n_grid=n_grid)
+    X_tr = features_t(s, UY_tr).cpu().numpy()
+    y_tr = lab.cpu().numpy()
+    mu, sd = X_tr.mean(axis=0), X_tr.std(axis=0) + 1e-6
+    Xt = torch.from_numpy(((X_tr - mu) / sd).astype(np.float32)).to(dev)
+    yt = torch.from_numpy(y_tr.astype(np.float32)).to(dev)
+    t1 = time.time()
+    params, losses = fit_mlp(Xt, yt, np.arange(n_train), steps=steps, seed=seed)
+    torch.cuda.synchronize()
+    t_fit = time.time() - t1
+    arrays = export_weights(params, mu, sd)
+    model = DeltaMLP(arrays, dev)
+    # held-out evaluation: each phenotype with n_perm shuffles (numpy's PCG64 orders, as the scan draws them)
+    cols = list(range(n_train, n_train + n_eval))
+    orders = perm_orders_device(N, cols, n_perm, 19930909, dev)
+    Yt_all = pack_perm_columns(Yt[n_train:].contiguous(), orders)
+    UY = rotate(Yt_all)
+    del Yt_all
+    P = UY.shape[0]
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    fit_delta_fast(s, UY[:1024], n_grid=n_grid)  # warm both paths
+    fit_delta_learned(s, UY[:1024], n_grid=n_grid, model=model)
+    e0.record()
+    ld_full, _ = fit_delta_fast(s, UY, n_grid=n_grid)
+    e1.record()
+    stats: dict = {}
+    ld_l, _ = fit_delta_learned(s, UY, n_grid=n_grid, model=model, stats=stats)
+    e2.record()
+    torch.cuda.synchronize()
+    g = grid_evaluations(stats)
+    dld = (ld_l - ld_full).abs().cpu().numpy()
+    # Wald scan of a block of variants under either fit: -log10 p of the real columns and the permutation maxima
+    rows = torch.arange(wald_variants, dtype=torch.int64, device=dev)
+    USt = torch.empty((wald_variants, N - D), dtype=F32, device=dev)
+    gemm_split(ctx, SplitRows.of(Zt[:wald_variants]).view(), Us.view(), USt)
+    ops = WaldOperands(dev)
+    res = {}
+    for tag, ld in (("full", ld_full), ("learned", ld_l)):
+        out = {k: torch.zeros((wald_variants, n_eval), dtype=F64, device=dev) for k in ("f", "beta", "se", "sfve")}
+        max_F = torch.full((P,), float("-inf"), dtype=F64, device=dev)
+        wald_fast(ctx, ops, s, UY, ld, USt, n_eval, rows, out, max_F)
+        res[tag] = (neg_log10_pvalue(out["f"], N - D - 1), neg_log10_pvalue(max_F, N - D - 1))
+    dp = (res["learned"][0] - res["full"][0]).abs().max().item()
+    dq = (res["learned"][1] - res["full"][1]).abs().max().item()
+    rec = {"cohort": {"N": N, "M": M, "chromosomes": 22, "kinship": "single, all variants", "covariates": "intercept"},
+           "training": {"phenotypes": n_train, "labels": f"exact fit from the {n_grid}-point grid argmin",
+                        "steps": steps, "trainer": "flmm_mlp_grad + flmm_mlp_adamw (BF16 operands, FP32 master)",
+                        "fit_s": round(t_fit, 2), "loss_first": float(losses[:50].mean()),
+                        "loss_last": float(losses[-50:].mean())},
+           "evaluation": {"phenotypes": n_eval, "permutations": n_perm, "columns": P, **g,
+                          "abs_d_log_delta_median": float(np.median(dld)),
+                          "abs_d_log_delta_p99": float(np.quantile(dld, 0.99)),
+                          "abs_d_log_delta_max": float(dld.max()),
+                          "wald_variants": wald_variants, "max_abs_d_neglog10p_real": dp,
+                          "max_abs_d_neglog10p_perm_max": dq,
+                          "fit_ms_full_grid": e0.elapsed_time(e1), "fit_ms_learned": e1.elapsed_time(e2)},
+           "simulate_s": round(t_sim, 1)}
+    np.savez(out_weights, **arrays, info=json.dumps(rec))
+    return rec
+
+
 def main(argv=None) -> None:
-    ap = argparse.ArgumentParser(description="train the learned delta proposal")
-    ap.add_argument("cmd", choices=["train"])
+    ap = argparse.ArgumentParser(description="train (and evaluate) the learned delta proposal")
+    ap.add_argument("cmd", choices=["train", "config4"])
     ap.add_argument("--out", default=str(WEIGHTS))
     ap.add_argument("--sets", type=int, default=48)
     ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--n-train", type=int, default=20_000)
+    ap.add_argument("--n-eval", type=int, default=10_000)
+    ap.add_argument("--n-perm", type=int, default=100)
     args = ap.parse_args(argv)
     from . import build
     build()
-    print(json.dumps(train(Path(args.out), n_sets=args.sets, steps=args.steps)), flush=True)
+    if args.cmd == "train":
+        print(json.dumps(train(Path(args.out), n_sets=args.sets, steps=args.steps)), flush=True)
+    else:
+        print(json.dumps(config4(Path(args.out), n_train=args.n_train, n_eval=args.n_eval, n_perm=args.n_perm,
+                                 steps=args.steps)), flush=True)
 
 
 if __name__ == "__main__":

@@ -206,3 +206,67 @@ def make_workload(name: str, *, seed: int = 19930909, B: int | None = None, M: i
         gen["chrom_sizes"] = chrom_sizes_human(w["M"], w["n_chrom"])
     data = make_dataset(w["N"], w["M"], w["n_chrom"], w["D"], w["B"], seed=seed, **gen)
     return data, w
+
+
+# The low-rank large-cohort shape: a kinship factor of k markers and M tested variants over 22 human-sized
+# chromosomes, N samples, B phenotypes (h2 ~ U[0.1, 0.7], 10 causal tested variants each); the permutation columns
+# are drawn by the scan's driver.
+LOWRANK_WORKLOADS = {
+    "n50000_k2000_m1m_b100_perm10": dict(N=50_000, k_kin=2_000, M=1_000_000, n_chrom=22, D=5, B=100, n_perm=10,
+                                         n_grid=64, log_delta_min=-10.0, log_delta_max=10.0, config_id=5),
+}
+
+
+@dataclass
+class LowRankData:
+    Gt: np.ndarray         # (M, N) int8 tested dosages, variant-major (a block of variants is contiguous)
+    chrom: np.ndarray      # (M,) chromosome of each tested variant, contiguous blocks 1..n_chrom
+    Gk: np.ndarray         # (N, k) int8 kinship-factor dosages
+    chrom_kin: np.ndarray  # (k,) chromosome of each kinship marker
+    X: np.ndarray          # (N, D)
+    Y: np.ndarray          # (N, B) after RINT
+
+
+def _variant_major_blocks(M: int, N: int, maf: np.ndarray, key: tuple, threads: int, step: int = 2048) -> np.ndarray:
+    """(M, N) int8 Binomial(2, maf_m) dosages as two Bernoulli draws per call, each block of `step` variants from
+    its own PCG64 stream (SeedSequence [*key, block]); independent of the thread count."""
+    Gt = np.empty((M, N), dtype=np.int8)
+
+    def draw(m0):
+        m1 = min(M, m0 + step)
+        r = np.random.Generator(np.random.PCG64(np.random.SeedSequence([*key, m0 // step])))
+        p = maf[m0:m1, None]
+        blk = (r.random((m1 - m0, N)) < p).astype(np.int8)
+        blk += (r.random((m1 - m0, N)) < p).astype(np.int8)
+        Gt[m0:m1] = blk
+
+    _for_blocks(draw, range(0, M, step), threads)
+    return Gt
+
+
+def make_lowrank_workload(name: str, *, seed: int = 19930909, M: int | None = None, B: int | None = None,
+                          threads: int = 16) -> tuple[LowRankData, dict]:
+    w = dict(LOWRANK_WORKLOADS[name])
+    if M is not None:
+        w["M"] = M
+    if B is not None:
+        w["B"] = B
+    N, k, Mv, nc, D, Bn = w["N"], w["k_kin"], w["M"], w["n_chrom"], w["D"], w["B"]
+    rng = np.random.default_rng([seed, w["config_id"]])
+    sizes, sizes_k = chrom_sizes_human(Mv, nc), chrom_sizes_human(k, nc)
+    chrom = np.repeat(np.arange(1, nc + 1), sizes)
+    chrom_kin = np.repeat(np.arange(1, nc + 1), sizes_k)
+    maf = rng.uniform(0.05, 0.5, size=Mv)
+    maf_k = rng.uniform(0.05, 0.5, size=k)
+    Gt = _variant_major_blocks(Mv, N, maf, (seed, w["config_id"], 1), threads)
+    Gk = np.ascontiguousarray(_variant_major_blocks(k, N, maf_k, (seed, w["config_id"], 2), threads).T)
+    X = np.concatenate([np.ones((N, 1)), rng.standard_normal((N, D - 1))], axis=1)
+    Y = np.empty((N, Bn))
+    h2 = rng.uniform(0.1, 0.7, size=Bn)
+    for b in range(Bn):
+        idx = rng.choice(Mv, size=10, replace=False)
+        Zc = Gt[idx].astype(np.float64)
+        Zc = (Zc - Zc.mean(axis=1, keepdims=True)) / np.clip(Zc.std(axis=1, keepdims=True), 1e-12, None)
+        g = Zc.T @ rng.standard_normal(10)
+        Y[:, b] = g / g.std() * np.sqrt(h2[b]) + rng.standard_normal(N) * np.sqrt(1.0 - h2[b])
+    return LowRankData(Gt=Gt, chrom=chrom, Gk=Gk, chrom_kin=chrom_kin, X=X, Y=rint_columns(Y)), w

@@ -290,28 +290,39 @@ int flmm_wald_split_f16_df(flmm_context* ctx, const void* A1h, const void* A1l, 
 
 /* ---- split-precision low-rank Wald (fasterlmm/lowrank.py:239-316) ----------------------------------------------
  *
- * With w~_i = (shat + delta) / (s_i + delta), c = (shat + delta) / delta (shat = mean s), the low-rank sWy is one
- * product over K = k + N of the column row [(w~ - c) o UY | c Y_r] and the variant row [US | S] (the off-rank part
- * S_r^T Y_r - US^T UY, with S_r^T Y_r = S^T Y_r as Y_r is orthogonal to the covariates), and sWs is the interpolated
- * product of [US^2 | ||S_r||^2] with node weights [w~(x_r) - c(x_r) | c(x_r)]; flmm_wald_split_f16_df then runs the
- * fused scan with K = k + N and var_df = N - D - 1.
+ * With w~_i = (shat + delta) / (s_i + delta), c = (shat + delta) / delta (shat = mean s) and the off-rank residuals
+ * UUY = Y_r - U_eff UY, UUS = S_r - U_eff US (lowrank.py:110, 289), the low-rank sWy is one product over K = k + N of
+ * the column row [w~ o UY | c UUY] and the variant row [US | UUS], and sWs the interpolated product of
+ * [US^2 | ||UUS||^2] with node weights [w~(x_r) | c(x_r)]; flmm_wald_split_f16_df then runs the fused scan with
+ * K = k + N and var_df = N - D - 1.
  *
- * flmm_lr_prep_columns: UYt (P, ldu) FP32 on-rank rotations, Yrt (P, ldy) FP64 covariate-regressed columns,
- * yy_off (P,) FP64 = ||Y_r||^2 - ||UY||^2, s32 (k,) FP32, shat (device scalar, flmm_mean_f32 of s), column log deltas
- * -> A1 (P, lda >= k + N) split, the Lagrange weights L (P, ldl) split, rWr = sum w~ UY^2 + c yy_off, rWr0 = rWr /
- * (shat + delta).  flmm_lr_prep_variants: USt (Mc, ldus) FP32 on-rank rotations of standardised variants Zt (Mc, ldz)
- * FP64, orthonormal covariate basis rows Qt (D, ldq), D <= 16 -> B1 = [US | S] (Mc, ldb >= k + N) and B2 = [US^2 |
- * ||S_r||^2] (Mc, ldb2 >= k + 1), each split with its row scales.  flmm_lr_interp_nodes: node weights W (R, ldw >=
- * k + 1) FP64 at x_r = x0 + r h. */
-int flmm_lr_prep_columns(const float* s32, int k, const float* UYt, int64_t ldu, const double* Yrt, int64_t ldy, int N,
-                         const double* yy_off, const double* log_delta, int P, const float* shat, double x0, double h,
-                         int R, void* A1h, void* A1l, int64_t lda, void* Lh, void* Ll, int64_t ldl, float* sa1,
-                         float* sl, float* rWr, float* rWr0, void* stream);
-int flmm_lr_prep_variants(const float* USt, int64_t ldus, const double* Zt, int64_t ldz, int Mc, int k, int N,
-                          const double* Qt, int64_t ldq, int D, void* B1h, void* B1l, int64_t ldb, float* sb1,
-                          void* B2h, void* B2l, int64_t ldb2, float* sb2, void* stream);
+ * flmm_lr_residual: R = Y - C (rows, N) FP64 from Y FP64 and a product C FP32, and the row sums of squares ss.
+ * flmm_lr_prep_columns: UYt (P, ldu) FP32 on-rank rotations, UUYt (P, ldy) FP64 off-rank residuals, yy_off (P,) FP64
+ * = ||UUY||^2, s32 (k,) FP32, shat (device scalar, flmm_mean_f32 of s), column log deltas -> A1 (P, lda >= k + N)
+ * split, the Lagrange weights L (P, ldl) split, rWr = sum w~ UY^2 + c yy_off, rWr0 = rWr / (shat + delta).
+ * flmm_lr_prep_variants: USt (Mc, ldus) FP32 on-rank rotations of the standardised variants Zt (Mc, ldz) FP64, Ct =
+ * U_eff US (Mc, ldc) FP32, orthonormal covariate basis rows Qt (D, ldq), D <= 16 -> UUS = Zt - Qt^T Qt Zt - Ct formed
+ * in FP32, B1 = [US | UUS] (Mc, ldb >= k + N) and B2 = [US^2 | ||UUS||^2] (Mc, ldb2 >= k + 1), each split with its row
+ * scales.  flmm_lr_interp_nodes: node weights W (R, ldw >= k + 1) FP64 at x_r = x0 + r h. */
+int flmm_lr_residual(const double* Y, int64_t ldy, const float* C, int64_t ldc, int rows, int N, double* R,
+                     int64_t ldr, double* ss, void* stream);
+int flmm_lr_prep_columns(const float* s32, int k, const float* UYt, int64_t ldu, const double* UUYt, int64_t ldy,
+                         int N, const double* yy_off, const double* log_delta, int P, const float* shat, double x0,
+                         double h, int R, void* A1h, void* A1l, int64_t lda, void* Lh, void* Ll, int64_t ldl,
+                         float* sa1, float* sl, float* rWr, float* rWr0, void* stream);
+int flmm_lr_prep_variants(const float* USt, int64_t ldus, const double* Zt, int64_t ldz, const float* Ct, int64_t ldc,
+                          int Mc, int k, int N, const double* Qt, int64_t ldq, int D, void* B1h, void* B1l,
+                          int64_t ldb, float* sb1, void* B2h, void* B2l, int64_t ldb2, float* sb2, void* stream);
 int flmm_lr_interp_nodes(const double* s, int k, const float* shat, double x0, double h, int R, double* W, int64_t ldw,
                          void* stream);
+/* The strong real tests listed by flmm_wald_split_f16_df for a low-rank block (as flmm_wald_refine_f32 for the full
+ * rank): each recomputed over the on-rank part (USt, UYt, s32) and the off-rank residuals (UUS = Sr - Ct, UUYt) with
+ * no cancelling subtraction, on var_df degrees of freedom; outputs overwritten in place, max_F raised. */
+int flmm_lr_wald_refine(const int32_t* flags, const int32_t* flag_count, int flag_cap, float f_refine, const float* USt,
+                        int64_t ldus, const float* UYt, int64_t lduy, const double* Sr, int64_t ldz, const float* Ct,
+                        int64_t ldc, const double* UUYt, int64_t lduu, const float* s32, const double* log_delta,
+                        int k, int N, int Mc, int n_real, int var_df, const int64_t* rows, double* f, double* beta,
+                        double* se, double* sfve, int64_t ldo, double* max_F, void* stream);
 
 /* Re-evaluation of the strong real tests listed by flmm_wald_split_f16 (the reference's Wald formulas,
  * fasterlmm/core.py:649-667, without the cancelling subtraction rss = rWr - sWy^2 / sWs): from the FP32 rotated

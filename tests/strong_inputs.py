@@ -109,3 +109,20 @@ def na_dataset(c: dict = NA1600):
     Y = Y.copy()
     Y[miss.T] = np.nan
     return G, X, Y, chrom
+
+
+# The low-rank case of the golden fixture lowrank_n2000: 2,000 samples, a kinship factor of 400 markers on four
+# chromosomes (each LOCO factor has rank ~300 < N, the reference's k < N branch), 3,000 tested variants on the same
+# chromosomes, 3 covariates, 6 phenotypes kept in detail and 18 further columns that only feed max_F.
+LR2000 = dict(N=2000, sizes=[900, 800, 700, 600], sizes_kin=[120, 110, 90, 80], D=3,
+              specs=[(0.9, 1, 1), (0.6, 5, 2), (0.4, 20, 3), (0.8, 2, 4), (0.2, 10, 1), (0.0, 0, 2)],
+              n_extra=18, seed=20002000, seed_kin=4004, seed_extra=606)
+
+
+def lowrank_dataset(c: dict = LR2000):
+    """(G test (N, M) int8, X, Y_all (N, B + n_extra), chrom, G_kin (N, k) int8, chrom_kin)."""
+    G, X, Y, chrom = strong_dataset(c["N"], c["sizes"], c["D"], c["specs"], seed=c["seed"])
+    Gk, _, _, chrom_kin = strong_dataset(c["N"], c["sizes_kin"], c["D"], [], seed=c["seed_kin"])
+    rng = np.random.Generator(np.random.PCG64(c["seed_extra"]))
+    extra = np.stack([_rint(_normals(rng, c["N"])) for _ in range(c["n_extra"])], axis=1)
+    return G, X, np.concatenate([Y, extra], axis=1), chrom, Gk, chrom_kin

@@ -52,8 +52,12 @@ def test_standardise_and_grm_match_oracle(golden):
     np.testing.assert_allclose(Zs, orc.standardise_columns(Z), rtol=1e-12, atol=1e-12)
     K = core.grm(torch.from_numpy(Zs).to(DEV)).cpu().numpy()
     np.testing.assert_allclose(K, orc.grm(Zs), rtol=1e-11, atol=1e-12)
-    # the numpy path returns numpy
+    # the numpy path returns numpy; a float32 tensor comes back float32, as the reference's torch branch returns it
     assert isinstance(core.standardise_columns(Z), np.ndarray)
+    Z32 = core.standardise_columns(torch.from_numpy(Z).float().to(DEV))
+    assert Z32.dtype == torch.float32 and Z32.shape == Z.shape
+    np.testing.assert_allclose(Z32.cpu().numpy(), orc.standardise_columns(Z.astype(np.float32).astype(np.float64)),
+                               rtol=1e-6, atol=1e-6)
 
 
 def test_components_match_golden(golden):
