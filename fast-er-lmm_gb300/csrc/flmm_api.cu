@@ -10,6 +10,8 @@
 #include <cstring>
 #include <new>
 
+#include <mutex>
+
 #include "flmm_common.cuh"
 
 constexpr int kEighWorkers = 8;
@@ -123,14 +125,32 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
 int flmm_ctx_sm_count(flmm_context* ctx) { return ctx->sm_count; }
 int* flmm_ctx_err_flag(flmm_context* ctx) { return ctx->err_flag; }
 
+int* flmm::device_err_flag(int device) {
+    static std::mutex mu;
+    static int* flags[64] = {};
+    if (device < 0 || device >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!flags[device]) {
+        int prev = 0;
+        if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) return nullptr;
+        int* f = nullptr;
+        if (cudaMalloc(&f, sizeof(int)) == cudaSuccess && cudaMemset(f, 0, sizeof(int)) == cudaSuccess) flags[device] = f;
+        cudaSetDevice(prev);
+    }
+    return flags[device];
+}
+
 extern "C" int flmm_context_check(flmm_context* ctx, void* stream) {
     FLMM_REQUIRE(ctx, "flmm_context_check: NULL context");
-    int h = 0;
-    FLMM_CUDA(cudaMemcpyAsync(&h, ctx->err_flag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
+    int h[2] = {0, 0};
+    int* dflag = device_err_flag(ctx->device);
+    FLMM_CUDA(cudaMemcpyAsync(&h[0], ctx->err_flag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
+    if (dflag) FLMM_CUDA(cudaMemcpyAsync(&h[1], dflag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
     FLMM_CUDA(cudaStreamSynchronize(as_stream(stream)));
-    if (h != 0) {
+    if (h[0] != 0 || h[1] != 0) {
         FLMM_CUDA(cudaMemsetAsync(ctx->err_flag, 0, sizeof(int), as_stream(stream)));
-        return fail(FLMM_ERR_TIMEOUT, "a tensor-core kernel gave up a bounded wait (code %d)", h);
+        if (dflag) FLMM_CUDA(cudaMemsetAsync(dflag, 0, sizeof(int), as_stream(stream)));
+        return fail(FLMM_ERR_TIMEOUT, "a tensor-core kernel gave up a bounded wait (code %d)", h[0] ? h[0] : h[1]);
     }
     return FLMM_OK;
 }

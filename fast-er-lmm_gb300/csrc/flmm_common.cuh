@@ -19,12 +19,23 @@ int check_launch(const char* what);
 // Same error conversion without counting a launch (after library calls such as cuSOLVER).
 int check_cuda(const char* what);
 
+// Device int raised by kernels without a context (e.g. the refinement's tensor-core product) when a bounded wait
+// gives up; one per device, allocated on first use, reported and cleared by flmm_context_check.  nullptr if the
+// allocation failed.
+int* device_err_flag(int device);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // The library's own batched FP32 eigensolver (csrc/flmm_eigh_own.cu): A (batch, N, N) symmetric in, one eigenvector
 // per row out, evals (batch, N) ascending; work of eigh_own_workspace_bytes(N, batch) bytes.
 size_t eigh_own_workspace_bytes(int N, int batch);
 int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStream_t st);
+
+// The refinement's FP64-accurate product on the tensor cores (csrc/flmm_ozaki.cu): W (batch, N, N) = U~ A^T, U~ the
+// digit-plane rounding of U (written to Ut); work of refine_product_tc_bytes(N, batch) bytes.
+size_t refine_product_tc_bytes(int N, int batch);
+int refine_product_tc(const float* U, const double* A, int N, int batch, float* Ut, double* W, void* work,
+                      cudaStream_t st);
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 

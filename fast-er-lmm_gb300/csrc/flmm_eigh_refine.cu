@@ -8,10 +8,15 @@
 //     lambda_j = u_j^T A u_j / u_j^T u_j,     r_j = A u_j - lambda_j u_j,
 //     E_ij = u_i^T r_j / (lambda_j - lambda_i)  (i != j),   E_jj = (1 - u_j^T u_j) / 2,
 // the update is u'_j = u_j + sum_i E_ij u_i.  Only A u_j needs high precision: r_j is ~1e-7 of A u_j and must keep
-// ~4 digits, so W = U A is formed in double-FP32 arithmetic (hi / lo pairs, exact products by FMA, TwoSum
-// accumulation, ~2^-44 relative) on the FP32 pipe; u_i^T r_j and the update are small corrections and run in FP32.
+// ~4 digits, so W = U A is formed FP64-accurately -- by default on the FP16 tensor cores from exact digit planes
+// (flmm_ozaki.cu; the step then works on the planes' rounding U~ of U, ~2^-46 relative), else in double-FP32
+// arithmetic on the FP32 pipe (hi / lo pairs, exact products by FMA, TwoSum accumulation, ~2^-44 relative);
+// u_i^T r_j and the update are small corrections and run in FP32.
 // Pairs closer than tau = 1e-6 max|lambda| are left unrotated (their mixing does not change the likelihood).
 #include <math.h>
+
+#include <cstdlib>
+#include <cstring>
 
 #include "flmm_common.cuh"
 
@@ -210,7 +215,8 @@ __global__ void k_refine_coeffs(const float* __restrict__ M, const double* __res
 }
 
 struct RefineWs {
-    float *Ah, *Al, *R, *Mt, *T;
+    void* prod;  // the product's workspace: digit planes (tensor-core form) or the FP32 split of A (double-FP32 form)
+    float *Ah, *Al, *Ut, *R, *Mt, *T;
     double *W, *nrm;
     size_t bytes;
 };
@@ -222,18 +228,46 @@ RefineWs carve(void* base, int N, int batch) {
     size_t off = 0;
     auto take = [&](size_t nbytes) {
         const uintptr_t p = b + off;
-        off += (nbytes + 255) / 256 * 256;
+        off += (nbytes + 1023) / 1024 * 1024;
         return p;
     };
-    w.Ah = reinterpret_cast<float*>(take(sizeof(float) * nn));
-    w.Al = reinterpret_cast<float*>(take(sizeof(float) * nn));
+    const size_t split_bytes = 2 * ((sizeof(float) * nn + 1023) / 1024 * 1024);
+    const size_t tc_bytes = refine_product_tc_bytes(N, batch);
+    const uintptr_t prod = take(tc_bytes > split_bytes ? tc_bytes : split_bytes);
+    w.prod = reinterpret_cast<void*>(prod);
+    w.Ah = reinterpret_cast<float*>(prod);
+    w.Al = reinterpret_cast<float*>(prod + split_bytes / 2);
+    w.Ut = reinterpret_cast<float*>(take(sizeof(float) * nn));
     w.W = reinterpret_cast<double*>(take(sizeof(double) * nn));
     w.R = reinterpret_cast<float*>(take(sizeof(float) * nn));
     w.Mt = reinterpret_cast<float*>(take(sizeof(float) * nn));
     w.nrm = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(N) * batch));
-    w.T = w.Ah;  // the split of A is dead once W is formed
+    w.T = reinterpret_cast<float*>(prod);  // the product's workspace is dead once W is formed
     w.bytes = off;
     return w;
+}
+
+// The product's form: tensor cores (digit planes, flmm_ozaki.cu) unless FLMM_REFINE_PRODUCT=df32 selects the
+// double-FP32 kernel on the FP32 pipe (kept for cross-checks; both agree to ~2^-44 relative).
+int default_form() {
+    static int form = [] {
+        const char* e = std::getenv("FLMM_REFINE_PRODUCT");
+        return (e && std::strcmp(e, "df32") == 0) ? 1 : 0;
+    }();
+    return form;
+}
+
+// W = U~ A^T in the given form; U~ (the vectors the product is exact for) goes to Ut.
+int product(const double* A, const float* U, int N, int batch, int form, const RefineWs& ws, cudaStream_t st) {
+    const int64_t total = static_cast<int64_t>(N) * N * batch;
+    if (form == 0) return refine_product_tc(U, A, N, batch, ws.Ut, ws.W, ws.prod, st);
+    FLMM_CUDA(cudaMemcpyAsync(ws.Ut, U, sizeof(float) * total, cudaMemcpyDeviceToDevice, st));
+    k_split_pairs<<<ceil_div(total, 256), 256, 0, st>>>(A, total, ws.Ah, ws.Al);
+    int rc = check_launch("k_split_pairs");
+    if (rc) return rc;
+    const dim3 g64(ceil_div(N, DB), ceil_div(N, DB), batch);
+    k_df32_gemm_nt<<<g64, DT, 0, st>>>(U, ws.Ah, ws.Al, N, ws.W);
+    return check_launch("k_df32_gemm_nt");
 }
 
 }  // namespace
@@ -241,6 +275,28 @@ RefineWs carve(void* base, int N, int batch) {
 extern "C" int flmm_eigh_refine_workspace_bytes(int N, int batch, size_t* bytes) {
     FLMM_REQUIRE(bytes && N > 0 && batch > 0, "flmm_eigh_refine_workspace_bytes: bad arguments");
     *bytes = carve(nullptr, N, batch).bytes;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_refine_product_workspace_bytes(int N, int batch, size_t* bytes) {
+    FLMM_REQUIRE(bytes && N > 0 && batch > 0, "flmm_refine_product_workspace_bytes: bad arguments");
+    *bytes = carve(nullptr, N, batch).bytes;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_refine_product(const float* U, const double* A, int N, int batch, int form, float* Ut, double* W,
+                                   void* work, size_t work_bytes, void* stream) {
+    FLMM_REQUIRE(U && A && Ut && W && work && N > 0 && batch > 0 && batch <= 65535 && (form == 0 || form == 1),
+                 "flmm_refine_product: bad arguments");
+    RefineWs ws = carve(work, N, batch);
+    if (work_bytes < ws.bytes)
+        return fail(FLMM_ERR_WORKSPACE, "flmm_refine_product: need %zu bytes, got %zu", ws.bytes, work_bytes);
+    cudaStream_t st = as_stream(stream);
+    const int rc = product(A, U, N, batch, form, ws, st);
+    if (rc) return rc;
+    const int64_t total = static_cast<int64_t>(N) * N * batch;
+    FLMM_CUDA(cudaMemcpyAsync(Ut, ws.Ut, sizeof(float) * total, cudaMemcpyDeviceToDevice, st));
+    FLMM_CUDA(cudaMemcpyAsync(W, ws.W, sizeof(double) * total, cudaMemcpyDeviceToDevice, st));
     return FLMM_OK;
 }
 
@@ -252,23 +308,21 @@ extern "C" int flmm_eigh_refine_f32(const double* A, float* U, float* U_out, dou
     if (work_bytes < ws.bytes)
         return fail(FLMM_ERR_WORKSPACE, "flmm_eigh_refine_f32: need %zu bytes, got %zu", ws.bytes, work_bytes);
     cudaStream_t st = as_stream(stream);
-    const int64_t total = static_cast<int64_t>(N) * N * batch;
-    k_split_pairs<<<ceil_div(total, 256), 256, 0, st>>>(A, total, ws.Ah, ws.Al);
-    int rc = check_launch("k_split_pairs");
+    // W = U~ A^T; from here on the step works on U~ (ws.Ut), the vectors the product is exact for
+    int rc = product(A, U, N, batch, default_form(), ws, st);
     if (rc) return rc;
+    const float* Uc = ws.Ut;
     const dim3 g64(ceil_div(N, DB), ceil_div(N, DB), batch);
-    k_df32_gemm_nt<<<g64, DT, 0, st>>>(U, ws.Ah, ws.Al, N, ws.W);
-    if ((rc = check_launch("k_df32_gemm_nt"))) return rc;
     const int64_t rows = static_cast<int64_t>(N) * batch;
-    k_rq_residual<<<ceil_div(rows * 32, 256), 256, 0, st>>>(ws.W, U, N, static_cast<int>(rows), evals, ws.nrm, ws.R);
+    k_rq_residual<<<ceil_div(rows * 32, 256), 256, 0, st>>>(ws.W, Uc, N, static_cast<int>(rows), evals, ws.nrm, ws.R);
     if ((rc = check_launch("k_rq_residual"))) return rc;
     // M[i, j] = u_i . r_j
-    k_f32_gemm<true, false><<<g64, FT, 0, st>>>(U, ws.R, nullptr, N, ws.Mt);
+    k_f32_gemm<true, false><<<g64, FT, 0, st>>>(Uc, ws.R, nullptr, N, ws.Mt);
     if ((rc = check_launch("k_f32_gemm<nt>"))) return rc;
     const dim3 gc(ceil_div(static_cast<int64_t>(N) * N, 256), batch);
     k_refine_coeffs<<<gc, 256, 0, st>>>(ws.Mt, evals, ws.nrm, N, ws.T);
     if ((rc = check_launch("k_refine_coeffs"))) return rc;
     // U' = U + T U
-    k_f32_gemm<false, true><<<g64, FT, 0, st>>>(ws.T, U, U, N, U_out);
+    k_f32_gemm<false, true><<<g64, FT, 0, st>>>(ws.T, Uc, Uc, N, U_out);
     return check_launch("k_f32_gemm<nn>");
 }

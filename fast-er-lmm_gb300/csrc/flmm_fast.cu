@@ -1192,6 +1192,11 @@ int launch_product(const TcMaps& maps_tc, const TcMaps& maps_pair, const TcArgs&
 
 }  // namespace
 
+// FP16 operand maps for the other tcgen05 kernels of the library (flmm_ozaki.cu).
+int flmm::tc::make_map_f16(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK, int box_rows) {
+    return make_map(map, base, rows, K, ld, BK, box_rows);
+}
+
 extern "C" int flmm_tc_config(int mode, int pair, int group) {
     FLMM_REQUIRE(mode >= 0 && mode <= 2 && (mode != 2 || group >= 1),
                  "flmm_tc_config: mode 0 (default), 1 (autotune) or 2 (forced pair / group >= 1)");

@@ -297,6 +297,10 @@ __device__ __forceinline__ void mma_commit_pair(uint64_t* bar, uint16_t cta_mask
         : "memory");
 }
 
+// FP16 matrix (rows, K) with row pitch ld elements (a multiple of 8, base 16-byte aligned) -> tiled TMA map with box
+// {BK, box_rows}, BK 32 (64-byte swizzle) or 64 (128-byte swizzle); rows and columns outside the matrix read as zero.
+int make_map_f16(CUtensorMap* map, const void* base, int rows, int K, int64_t ld, int BK, int box_rows);
+
 // Bounded wait that ignores the kernel's error flag: used at teardown to drain TMA copies still in flight.
 __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
     const long long t0 = clock64();

@@ -43,6 +43,8 @@ SIGNATURES: dict[str, list] = {
     "flmm_eigh_batched_f32": [_p, _p, _i, _i, _p, _p, _sz, _p],
     "flmm_eigh_refine_workspace_bytes": [_i, _i, _psz],
     "flmm_eigh_refine_f32": [_p, _p, _p, _p, _i, _i, _p, _sz, _p],
+    "flmm_refine_product_workspace_bytes": [_i, _i, _psz],
+    "flmm_refine_product": [_p, _p, _i, _i, _i, _p, _p, _p, _sz, _p],
     "flmm_compat_spectrum": [_p, _i, _i, _p, _p],
     "flmm_compat_spectrum_f32": [_p, _i, _i, _p, _p],
     "flmm_regress_out": [_p, _i64, _i, _i, _p, _i, _p, _p, _i64, _p],

@@ -120,11 +120,20 @@ int flmm_eigh_batched_f32(flmm_context* ctx, float* A, int N, int batch, float* 
 
 /* One Ogita-Aishima refinement step for the FP32 decomposition of FP64 symmetric A (batch, N, N): U (batch, N, N)
  * FP32 eigenvector rows in, U_out refined rows out (U_out != U), evals (batch, N) FP64 Rayleigh quotients out.  A U
- * is formed in double-FP32 arithmetic; the corrections in FP32.  No counterpart in the reference (its eigh is
- * FP64, fasterlmm/core.py:54-77); it brings the FP32 eigenbasis to the accuracy the fast form's delta fit needs. */
+ * is formed FP64-accurately (flmm_refine_product, tensor-core form unless FLMM_REFINE_PRODUCT=df32 is set in the
+ * environment); the corrections in FP32.  No counterpart in the reference (its eigh is FP64,
+ * fasterlmm/core.py:54-77); it brings the FP32 eigenbasis to the accuracy the fast form's delta fit needs. */
 int flmm_eigh_refine_workspace_bytes(int N, int batch, size_t* bytes);
 int flmm_eigh_refine_f32(const double* A, float* U, float* U_out, double* evals, int N, int batch, void* work,
                          size_t work_bytes, void* stream);
+
+/* The refinement's product W (batch, N, N) FP64 = U~ A^T for FP32 U and FP64 symmetric A (batch, N, N).  form 0:
+ * FP16 tensor cores on exact digit planes (Ozaki splitting; U~ is U rounded to 28 bits below each row's largest
+ * element, A to 48 bits; ~2^-46 relative); form 1: double-FP32 arithmetic on the FP32 pipe (U~ = U; ~2^-44).  U~
+ * is written to Ut.  Workspace from flmm_refine_product_workspace_bytes. */
+int flmm_refine_product_workspace_bytes(int N, int batch, size_t* bytes);
+int flmm_refine_product(const float* U, const double* A, int N, int batch, int form, float* Ut, double* W, void* work,
+                        size_t work_bytes, void* stream);
 
 /* Kept spectrum: s (Neff,) = max(evals[D + i] - 1, 0) (fasterlmm/core.py:514); the _f32 form reads FP32 evals. */
 int flmm_compat_spectrum(const double* evals, int N, int D, double* s, void* stream);
