@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
                 drain64(tl0 + static_cast<uint32_t>(slot * kBN), acc0);
                 fence_before_sync();
                 __syncwarp();
-                if (lane == 0) mbar_arrive_cluster(slot_empty0 + static_cast<uint32_t>(slot * 8));
+                if (lane == 0) mbar_arrive_cluster_relaxed(slot_empty0 + static_cast<uint32_t>(slot * 8));
                 if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
             }
             if (!ok) break;
@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
                           tb * kBN, sc1, sc2, rws);
                 fence_before_sync();
                 __syncwarp();
-                if (lane == 0) mbar_arrive_cluster(slot_empty0 + static_cast<uint32_t>(slot * 8));
+                if (lane == 0) mbar_arrive_cluster_relaxed(slot_empty0 + static_cast<uint32_t>(slot * 8));
                 if (++slot == kSlots) { slot = 0; sphase ^= 1u; }
             }
         }

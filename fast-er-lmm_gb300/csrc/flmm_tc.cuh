@@ -223,6 +223,14 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
 }
 
+// The same arrive without release semantics: for handing a drained tensor-memory slot back to the MMA issuer, where
+// the only accesses to order are the caller's tcgen05.ld of the slot, which tcgen05.wait::ld has completed and
+// tcgen05.fence::before_thread_sync orders before the arrive; the release would also wait for the thread's global
+// stores to become visible at cluster scope.
+__device__ __forceinline__ void mbar_arrive_cluster_relaxed(uint32_t bar_cluster) {
+    asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+
 __device__ __forceinline__ uint32_t mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
