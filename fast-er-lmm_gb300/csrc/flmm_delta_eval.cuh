@@ -17,7 +17,39 @@ struct NewtonEval {
     float loss;   // Neff log S1 + sum log (s + delta), up to constants
 };
 
-// One evaluation by a warp at x = log delta (x is warp-uniform), all in FP32.
+// Sums over the aligned group of W lanes (W = 16 or 32) holding this thread; every lane of the group gets the sum.
+// Groups of 16 let one warp work on two columns, which then share the per-evaluation scalar work (reductions,
+// divisions, the Newton and bracketing logic) that dominates a column's instruction count.
+template <int W>
+__device__ __forceinline__ unsigned group_mask() {
+    return W == 32 ? 0xffffffffu : (((1u << W) - 1u) << (threadIdx.x & 31u & ~static_cast<unsigned>(W - 1)));
+}
+
+template <int W>
+__device__ __forceinline__ float group_sum(float v) {
+    const unsigned m = group_mask<W>();
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o);
+    return v;
+}
+
+// group sum of a compensated pair (hi + lo), TwoSum at every level of the butterfly
+template <int W>
+__device__ __forceinline__ float group_sum_pair(float hi, float lo) {
+    const unsigned m = group_mask<W>();
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(m, hi, o);
+        const float ol = __shfl_xor_sync(m, lo, o);
+        float sum, err;
+        two_sum(hi, oh, sum, err);
+        hi = sum;
+        lo = lo + ol + err;
+    }
+    return hi + lo;
+}
+
+// One evaluation by a group of W lanes at x = log delta (x is uniform over the group), all in FP32.
 //
 // g is formed around the centre c = 1 / (sbar + delta), sbar the mean eigenvalue: with d_n = r_n - c =
 // (sbar - s_n) r_n c,
@@ -64,12 +96,13 @@ struct EvalSums {
     }
 };
 
+template <int W>
 __device__ inline NewtonEval finish_eval(const EvalSums& t, float U, int Neff, const EvalPoint& pt, bool want_loss) {
-    const float D1 = warp_sum_pair(t.d1, t.cd1);
-    const float E1 = warp_sum_pair(t.e1, t.ce1);
-    const float E2 = warp_sum(t.e2);
-    const float E3 = warp_sum(t.e3);
-    const float F2 = warp_sum(t.f2);
+    const float D1 = group_sum_pair<W>(t.d1, t.cd1);
+    const float E1 = group_sum_pair<W>(t.e1, t.ce1);
+    const float E2 = group_sum<W>(t.e2);
+    const float E3 = group_sum<W>(t.e3);
+    const float F2 = group_sum<W>(t.f2);
     const float c = pt.c;
     NewtonEval e;
     const float neff = static_cast<float>(Neff);
@@ -87,29 +120,32 @@ __device__ inline NewtonEval finish_eval(const EvalSums& t, float U, int Neff, c
         e.gp = 1.0f;
     }
     e.loss = 0.0f;
-    if (want_loss) e.loss = neff * logf(fmaxf(c * U + E1, 1e-30f)) + warp_sum(t.sl);
+    if (want_loss) e.loss = neff * logf(fmaxf(c * U + E1, 1e-30f)) + group_sum<W>(t.sl);
     return e;
 }
 
-// One evaluation over a column read from global (L1 / L2) memory; dsb[n] = sbar - s[n] and the column's sum of
-// squares U are precomputed.  Not inlined: the refinement calls the evaluator from a dozen places, and one shared
-// copy of the loop keeps the instruction cache warm (inlined copies made instruction fetch the main stall).
+// One evaluation by a group of W lanes over a column read from global (L1 / L2) memory; dsb[n] = sbar - s[n] and the
+// column's sum of squares U are precomputed.  Not inlined: the refinement calls the evaluator from a dozen places,
+// and one shared copy of the loop keeps the instruction cache warm (inlined copies made instruction fetch the main
+// stall).
+template <int W>
 static __device__ __noinline__ NewtonEval eval_global_column(const float* __restrict__ s32,
                                                              const float* __restrict__ dsb,
                                                              const float* __restrict__ u, int Neff, float sbar,
                                                              float U, double x, bool want_loss) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (W - 1);
     const EvalPoint pt = eval_point(x, sbar);
     EvalSums t;
     // four iterations per trip: their loads issue together instead of each waiting out its own L1 / L2 latency
     // (each lane still adds its terms in the same order, so the sums are unchanged)
 #pragma unroll 4
-    for (int n = lane; n < Neff; n += 32) t.add(s32[n], dsb[n], u[n] * u[n], pt, want_loss);
-    return finish_eval(t, U, Neff, pt, want_loss);
+    for (int n = lane; n < Neff; n += W) t.add(s32[n], dsb[n], u[n] * u[n], pt, want_loss);
+    return finish_eval<W>(t, U, Neff, pt, want_loss);
 }
 
-// Evaluator over a column in global memory.  (Keeping the squares in registers instead cost occupancy and ran
-// slower.)
+// Evaluator over a column in global memory, W lanes per column.  (Keeping the squares in registers instead cost
+// occupancy and ran slower.)
+template <int W>
 struct GlobalColumn {
     const float* s32;
     const float* dsb;
@@ -118,7 +154,7 @@ struct GlobalColumn {
     float sbar, U;
 
     __device__ NewtonEval operator()(double x, bool want_loss) const {
-        return eval_global_column(s32, dsb, u, Neff, sbar, U, x, want_loss);
+        return eval_global_column<W>(s32, dsb, u, Neff, sbar, U, x, want_loss);
     }
 };
 
@@ -179,8 +215,8 @@ struct FirstEvals {
     bool have_at = false, have_nb = false;
 };
 
-// log delta of one column from its grid argmin i (warp-uniform result).  `first`, if given, holds evaluations
-// already done.
+// log delta of one column from its grid argmin i (uniform over the column's lanes).  `first`, if given, holds
+// evaluations already done.
 template <class Ev>
 __device__ double refine_column(const Ev& ev, const double* __restrict__ grid, int G, int i, int refine,
                                 const FirstEvals* first = nullptr) {

@@ -45,97 +45,128 @@ __global__ void k_grid_weights_f32(const double* __restrict__ s, int Neff, const
     }
 }
 
-constexpr int TG = 64, TP = 64, TK = 32, NT = 256;
+// Tiles of the grid product: 64 grid nodes x 128 columns per block, 32-deep k steps, 128 threads of 8 x 8
+// accumulators (nodes 8 ty .. +7 against columns 4 tx .. +3 and 64 + 4 tx .. +3, so the quarter-warps' 128-bit shared
+// loads fall in distinct banks).  Shared rows are padded by 4 floats for the same reason on the transposing stores.
+constexpr int TG = 64, TP = 128, TK = 32, NT = 128;
+constexpr int WS_LD = TG + 4, US_LD = TP + 4;
 
-// loss[g, p] = Neff log(yWy) + sum_log[g] (+ constants that do not move the argmin), first argmin over g
-// kList: the CTA's 64 columns are entries [64 b, 64 b + 64) of the column list cols[0 .. *count) instead of columns
-// [64 b, 64 b + 64); CTAs past the list's end return at once (the grid is sized for the longest list, P).
+// loss[g, p] = Neff log(yWy) + sum_log[g] (+ constants that do not move the argmin), first argmin over g.  Every
+// accumulator adds its k terms in order with one FMA each, as a plain loop over n would.
+// kList: the CTA's columns are entries [128 b, 128 b + 128) of the column list cols[0 .. *count) instead of columns
+// [128 b, 128 b + 128); CTAs past the list's end return at once (the grid is sized for the longest list, P).
 template <bool kList>
 __global__ void __launch_bounds__(NT)
 k_grid_argmin_f32(const float* __restrict__ Wg, const float* __restrict__ sum_log, const float* __restrict__ UYt,
                   int64_t ldu, int Neff, int P, int G, int32_t* __restrict__ idx_out, const int32_t* __restrict__ cols,
                   const int32_t* __restrict__ count) {
-    __shared__ float Ws[TK][TG + 1];
-    __shared__ float Us[TK][TP + 1];
-    __shared__ float red_v[16][TP];
-    __shared__ int red_i[16][TP];
+    __shared__ __align__(16) float Ws[TK * WS_LD];
+    __shared__ __align__(16) float Us[TK * US_LD];
+    __shared__ float red_v[8][TP];
+    __shared__ int red_i[8][TP];
     __shared__ int col_s[TP];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int lane = tid & 31, warp = tid >> 5;
     const int p0 = blockIdx.x * TP;
     if (kList) {
         const int n = min(*count, P);
         if (p0 >= n) return;
-        if (tid < TP) col_s[tid] = (p0 + tid < n) ? cols[p0 + tid] : -1;
-        __syncthreads();
     }
-    // column of tile slot q (-1: none)
-    auto column = [&](int q) -> int {
-        if (kList) return col_s[q];
-        return (p0 + q < P) ? p0 + q : -1;
-    };
+    for (int q = tid; q < TP; q += NT) {
+        if (kList) {
+            const int n = min(*count, P);
+            col_s[q] = (p0 + q < n) ? cols[p0 + q] : -1;
+        } else {
+            col_s[q] = (p0 + q < P) ? p0 + q : -1;
+        }
+    }
+    __syncthreads();
     const float neff = static_cast<float>(Neff);
     float best = INFINITY;
     int best_g = 0;
     for (int g0 = 0; g0 < G; g0 += TG) {
-        float acc[4][4] = {};
+        float acc[8][8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[r][c] = 0.0f;
+        // register prefetch: the next k tile's entries are loaded while the current one is multiplied
+        float wv[16], uv[32];
+        auto load_tile = [&](int k0) {
+            const int gk = k0 + lane;
+            const bool kok = gk < Neff;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int gg = g0 + 16 * warp + i;
+                wv[i] = (gg < G && kok) ? Wg[static_cast<int64_t>(gg) * Neff + gk] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const int col = col_s[32 * warp + i];
+                const float u = (col >= 0 && kok) ? UYt[static_cast<int64_t>(col) * ldu + gk] : 0.0f;
+                uv[i] = u * u;
+            }
+        };
+        load_tile(0);
         for (int k0 = 0; k0 < Neff; k0 += TK) {
+            // weights: warp w stores nodes 16 w .. +15 of k = lane, squared column entries columns 32 w .. +31, four
+            // per 128-bit store
 #pragma unroll
-            for (int l = 0; l < (TG * TK) / NT; ++l) {
-                int t = tid + l * NT, g = t / TK, k = t % TK;
-                int gg = g0 + g, gk = k0 + k;
-                Ws[k][g] = (gg < G && gk < Neff) ? Wg[static_cast<int64_t>(gg) * Neff + gk] : 0.0f;
-            }
+            for (int i = 0; i < 16; i += 4)
+                *reinterpret_cast<float4*>(&Ws[lane * WS_LD + 16 * warp + i]) =
+                    make_float4(wv[i], wv[i + 1], wv[i + 2], wv[i + 3]);
 #pragma unroll
-            for (int l = 0; l < (TP * TK) / NT; ++l) {
-                int t = tid + l * NT, p = t / TK, k = t % TK;
-                int gp = column(p), gk = k0 + k;
-                float u = (gp >= 0 && gk < Neff) ? UYt[static_cast<int64_t>(gp) * ldu + gk] : 0.0f;
-                Us[k][p] = u * u;
-            }
+            for (int i = 0; i < 32; i += 4)
+                *reinterpret_cast<float4*>(&Us[lane * US_LD + 32 * warp + i]) =
+                    make_float4(uv[i], uv[i + 1], uv[i + 2], uv[i + 3]);
             __syncthreads();
-#pragma unroll
+            if (k0 + TK < Neff) load_tile(k0 + TK);
+#pragma unroll 4
             for (int k = 0; k < TK; ++k) {
-                float a[4], b[4];
+                const float4 a0 = *reinterpret_cast<const float4*>(&Ws[k * WS_LD + 8 * ty]);
+                const float4 a1 = *reinterpret_cast<const float4*>(&Ws[k * WS_LD + 8 * ty + 4]);
+                const float4 b0 = *reinterpret_cast<const float4*>(&Us[k * US_LD + 4 * tx]);
+                const float4 b1 = *reinterpret_cast<const float4*>(&Us[k * US_LD + 64 + 4 * tx]);
+                const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-                for (int r = 0; r < 4; ++r) a[r] = Ws[k][ty + 16 * r];
+                for (int r = 0; r < 8; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) b[c] = Us[k][tx + 16 * c];
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+                    for (int c = 0; c < 8; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
             }
             __syncthreads();
         }
+        // per column: the first minimum over this thread's 8 nodes, then over the 8 threads of the column
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < 8; ++c) {
+            const int q = (c < 4) ? 4 * tx + c : 64 + 4 * tx + (c - 4);
             float bv = INFINITY;
             int bi = G;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                int g = g0 + ty + 16 * r;
+            for (int r = 0; r < 8; ++r) {
+                const int g = g0 + 8 * ty + r;
                 if (g < G) {
-                    float v = neff * logf(fmaxf(acc[r][c], 1e-30f)) + sum_log[g];
+                    const float v = neff * logf(fmaxf(acc[r][c], 1e-30f)) + sum_log[g];
                     if (v < bv) { bv = v; bi = g; }
                 }
             }
-            red_v[ty][tx + 16 * c] = bv;
-            red_i[ty][tx + 16 * c] = bi;
+            red_v[ty][q] = bv;
+            red_i[ty][q] = bi;
         }
         __syncthreads();
-        if (tid < TP) {
-            for (int r = 0; r < 16; ++r) {
-                float v = red_v[r][tid];
-                int gi = red_i[r][tid];
+        for (int q = tid; q < TP; q += NT) {
+            // one thread per column (NT == TP)
+            for (int r = 0; r < 8; ++r) {
+                const float v = red_v[r][q];
+                const int gi = red_i[r][q];
                 if (v < best || (v == best && gi < best_g)) { best = v; best_g = gi; }
             }
         }
         __syncthreads();
     }
-    if (tid < TP) {
-        const int col = column(tid);
-        if (col >= 0) idx_out[col] = best_g;
-    }
+    static_assert(NT == TP, "one thread per column in the final reduction");
+    const int col = col_s[tid];
+    if (col >= 0) idx_out[col] = best_g;
 }
 
 // The spectrum as the evaluations read it, once per fit: s32 = fl32(s), dsb = sbar - s32, sbar = mean(s).
@@ -162,13 +193,18 @@ __global__ void k_spectrum_prep(const double* __restrict__ s, int Neff, float* _
     if (threadIdx.x == 0) *sbar_out = sbar;
 }
 
-// One warp per column; the spectrum arrays are shared by every warp of the grid through L1 / L2.
+// Lanes per column of the refinement: two columns per warp (see group_sum).
+constexpr int kNewtonLanes = 16;
+
+// One group of kNewtonLanes lanes per column; the spectrum arrays are shared by every group of the grid through
+// L1 / L2.
 __global__ void k_newton_refine(const float* __restrict__ s32, const float* __restrict__ dsb,
                                 const float* __restrict__ sbar_p, int Neff, const float* __restrict__ UYt, int64_t ldu,
                                 int P, const double* __restrict__ grid, int G, const int32_t* __restrict__ idx,
                                 int refine, double* __restrict__ log_delta) {
-    const int lane = threadIdx.x & 31;
-    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    constexpr int W = kNewtonLanes;
+    const int lane = threadIdx.x & (W - 1);
+    const int64_t p = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / W;
     if (p >= P) return;
     const float* u = UYt + p * ldu;
     const float sbar = *sbar_p;
@@ -182,7 +218,7 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
     EvalSums t, ta, tb;
     float uh = 0.f, uc = 0.f;
 #pragma unroll 4
-    for (int n = lane; n < Neff; n += 32) {
+    for (int n = lane; n < Neff; n += W) {
         const float un = u[n];
         const float uu = un * un;
         const float sn = s32[n], dn = dsb[n];
@@ -193,16 +229,16 @@ __global__ void k_newton_refine(const float* __restrict__ s32, const float* __re
             tb.add(sn, dn, uu, pb, false);
         }
     }
-    const float U = warp_sum_pair(uh, uc);
+    const float U = group_sum_pair<W>(uh, uc);
     FirstEvals first;
-    first.at = finish_eval(t, U, Neff, pt, false);
+    first.at = finish_eval<W>(t, U, Neff, pt, false);
     first.have_at = true;
     if (inner) {
-        first.lo = finish_eval(ta, U, Neff, pa, false);
-        first.hi = finish_eval(tb, U, Neff, pb, false);
+        first.lo = finish_eval<W>(ta, U, Neff, pa, false);
+        first.hi = finish_eval<W>(tb, U, Neff, pb, false);
         first.have_nb = true;
     }
-    const GlobalColumn ev{s32, dsb, u, Neff, sbar, U};
+    const GlobalColumn<W> ev{s32, dsb, u, Neff, sbar, U};
     const double out = refine_column(ev, grid, G, i, refine, &first);
     if (lane == 0) log_delta[p] = out;
 }
@@ -219,7 +255,7 @@ int launch_fast_fit(const double* s, int Neff, const float* UYt, int64_t ldu, in
     if ((rc = check_launch("k_grid_argmin_f32"))) return rc;
     k_spectrum_prep<<<1, 256, 0, st>>>(s, Neff, w.s32, w.dsb, w.sbar);
     if ((rc = check_launch("k_spectrum_prep"))) return rc;
-    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * kNewtonLanes, 256), 256, 0, st>>>(
         w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, n_grid, grid_idx, refine, log_delta);
     return check_launch("k_newton_refine");
 }
@@ -264,7 +300,7 @@ int launch_refine(const double* s, int Neff, const float* UYt, int64_t ldu, int 
     k_spectrum_prep<<<1, 256, 0, st>>>(s, Neff, w.s32, w.dsb, w.sbar);
     int rc = check_launch("k_spectrum_prep");
     if (rc) return rc;
-    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * 32, 256), 256, 0, st>>>(
+    k_newton_refine<<<ceil_div(static_cast<int64_t>(P) * kNewtonLanes, 256), 256, 0, st>>>(
         w.s32, w.dsb, w.sbar, Neff, UYt, ldu, P, w.grid, G, idx, refine, log_delta);
     return check_launch("k_newton_refine");
 }

@@ -722,35 +722,53 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
 
 // ---- operand preparation ---------------------------------------------------------------------------------------
 
+// One warp per row, eight rows per 256-thread block: the row's largest |x|, then the split.  FP64 inputs are rounded
+// to FP32 first (2^-24 relative, below the split's 2^-22), which keeps the per-element work off the FP64 pipe (a
+// small fraction of the FP32 rate on this GPU).
 template <typename T>
-__global__ void k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __restrict__ hi,
-                             __half* __restrict__ lo, int64_t ldo, float* __restrict__ scale) {
-    __shared__ float red[32];
-    const int64_t r = blockIdx.x;
+__global__ void __launch_bounds__(256)
+k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __restrict__ hi,
+             __half* __restrict__ lo, int64_t ldo, float* __restrict__ scale) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (r >= rows) return;
     const T* x = X + r * ldx;
     float amax = 0.0f;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
+#pragma unroll 4
+    for (int k = lane; k < K; k += 32) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = amax;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (threadIdx.x == 0) red[0] = v;
-    }
-    __syncthreads();
     int e;
-    const float mul = row_scale_exp(red[0], &e);
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        // FP64 inputs are rounded to FP32 before the split only after scaling, so the split keeps 22 bits
-        const double xd = static_cast<double>(x[k]) * static_cast<double>(mul);
-        const __half h = __double2half(xd);
-        hi[r * ldo + k] = h;
-        lo[r * ldo + k] = __double2half(xd - static_cast<double>(__half2float(h)));
-    }
+    const float mul = row_scale_exp(amax, &e);
+#pragma unroll 4
+    for (int k = lane; k < K; k += 32) split_store(static_cast<float>(x[k]), mul, hi, lo, r * ldo + k);
+    if (lane == 0) scale[r] = ldexpf(1.0f, -e);
+}
+
+// The same split with one 256-thread block per row, for long rows (the kinship markers' rows span every marker).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_split_long_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __restrict__ hi,
+                  __half* __restrict__ lo, int64_t ldo, float* __restrict__ scale) {
+    __shared__ float red[8];
+    const int64_t r = blockIdx.x;
+    if (r >= rows) return;
+    const T* x = X + r * ldx;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float amax = 0.0f;
+#pragma unroll 4
+    for (int k = threadIdx.x; k < K; k += 256) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if (lane == 0) red[wid] = amax;
+    __syncthreads();
+    amax = red[0];
+#pragma unroll
+    for (int w = 1; w < 8; ++w) amax = fmaxf(amax, red[w]);
+    int e;
+    const float mul = row_scale_exp(amax, &e);
+#pragma unroll 4
+    for (int k = threadIdx.x; k < K; k += 256) split_store(static_cast<float>(x[k]), mul, hi, lo, r * ldo + k);
     if (threadIdx.x == 0) scale[r] = ldexpf(1.0f, -e);
 }
 
@@ -768,7 +786,9 @@ constexpr int kPrepCache = 32;  // per-lane register cache of k_wald_prep_column
 // rWr = sum w~ UY^2, and the column's Lagrange weights L (R entries, 10 non-zero) split.  A block of kPrepCols warps
 // handles kPrepCols columns.  GB300's FP64 rate is ~1/60 of its FP32 rate, so FP64 is kept off the per-element
 // path: the Lagrange weights (FP64 products, one division each) are formed by ten threads per column before the
-// warps start, delta = exp(x) comes from a hi / lo split of x in FP32, and rWr is a compensated FP32 sum.
+// warps start, delta = exp(x) comes from a hi / lo split of x in FP32, and rWr is a compensated FP32 sum.  The
+// weights use the hardware reciprocal (within 1 ulp, below the split's 2^-22; tests strong enough for rWr's
+// rounding to matter are re-evaluated in FP64).
 constexpr int kPrepCols = 8;
 
 __global__ void __launch_bounds__(32 * kPrepCols)
@@ -830,7 +850,7 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
             av[i] = 0.0f;
             if (n < Neff) {
                 const float un = uv[i];
-                const float a = (num / (sv[i] + delta)) * un;
+                const float a = (num * rcp_approx(sv[i] + delta)) * un;
                 av[i] = a;
                 m1 = fmaxf(m1, fabsf(a));
                 neumaier(acc, comp, a * un);
@@ -839,7 +859,7 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
     } else {
         for (int n = lane; n < Neff; n += 32) {
             const float un = u[n];
-            const float a = (num / (s32[n] + delta)) * un;
+            const float a = (num * rcp_approx(s32[n] + delta)) * un;
             m1 = fmaxf(m1, fabsf(a));
             neumaier(acc, comp, a * un);
         }
@@ -856,7 +876,8 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
             if (n < Neff) split_store(av[i], mul1, A1h, A1l, p * lda + n);
         }
     } else {
-        for (int n = lane; n < Neff; n += 32) split_store((num / (s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
+        for (int n = lane; n < Neff; n += 32)
+            split_store((num * rcp_approx(s32[n] + delta)) * u[n], mul1, A1h, A1l, p * lda + n);
     }
     const int base = lbase[j];
     float lm = 0.0f;
@@ -1233,12 +1254,20 @@ extern "C" int flmm_split_rows_f16(const void* X, int x_is_f64, int64_t ldx, int
                  "flmm_split_rows_f16: bad arguments");
     if (rows == 0) return FLMM_OK;
     cudaStream_t st = as_stream(stream);
+    __half* h = static_cast<__half*>(hi);
+    __half* l = static_cast<__half*>(lo);
+    if (K > 4096) {  // long rows: a block per row
+        if (x_is_f64)
+            k_split_long_rows<double><<<rows, 256, 0, st>>>(static_cast<const double*>(X), ldx, rows, K, h, l, ldo, scale);
+        else
+            k_split_long_rows<float><<<rows, 256, 0, st>>>(static_cast<const float*>(X), ldx, rows, K, h, l, ldo, scale);
+        return check_launch("k_split_long_rows");
+    }
+    const unsigned grid = ceil_div(static_cast<int64_t>(rows) * 32, 256);  // one warp per row
     if (x_is_f64)
-        k_split_rows<double><<<rows, 256, 0, st>>>(static_cast<const double*>(X), ldx, rows, K,
-                                                    static_cast<__half*>(hi), static_cast<__half*>(lo), ldo, scale);
+        k_split_rows<double><<<grid, 256, 0, st>>>(static_cast<const double*>(X), ldx, rows, K, h, l, ldo, scale);
     else
-        k_split_rows<float><<<rows, 256, 0, st>>>(static_cast<const float*>(X), ldx, rows, K,
-                                                   static_cast<__half*>(hi), static_cast<__half*>(lo), ldo, scale);
+        k_split_rows<float><<<grid, 256, 0, st>>>(static_cast<const float*>(X), ldx, rows, K, h, l, ldo, scale);
     return check_launch("k_split_rows");
 }
 
