@@ -36,6 +36,11 @@ int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStrea
 size_t refine_product_tc_bytes(int N, int batch);
 int refine_product_tc(const float* U, const double* A, int N, int batch, float* Ut, double* W, void* work,
                       cudaStream_t st);
+// The step's corrections on the same workspace, after refine_product_tc: M = U~ R^T, then U_out = U~ + T U~ with T
+// (batch, N, N) FP32 stored at the start of the workspace and scratch an (batch, N, N) FP32 buffer.
+int refine_m_tc(const float* R, int N, int batch, float* M, void* work, cudaStream_t st);
+int refine_update_tc(const float* T, const float* Ut, float* scratch, int N, int batch, float* U_out, void* work,
+                     cudaStream_t st);
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 

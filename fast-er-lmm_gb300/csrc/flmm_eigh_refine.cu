@@ -312,17 +312,23 @@ extern "C" int flmm_eigh_refine_f32(const double* A, float* U, float* U_out, dou
     int rc = product(A, U, N, batch, default_form(), ws, st);
     if (rc) return rc;
     const float* Uc = ws.Ut;
+    const bool tc = default_form() == 0;
     const dim3 g64(ceil_div(N, DB), ceil_div(N, DB), batch);
     const int64_t rows = static_cast<int64_t>(N) * batch;
     k_rq_residual<<<ceil_div(rows * 32, 256), 256, 0, st>>>(ws.W, Uc, N, static_cast<int>(rows), evals, ws.nrm, ws.R);
     if ((rc = check_launch("k_rq_residual"))) return rc;
     // M[i, j] = u_i . r_j
-    k_f32_gemm<true, false><<<g64, FT, 0, st>>>(Uc, ws.R, nullptr, N, ws.Mt);
-    if ((rc = check_launch("k_f32_gemm<nt>"))) return rc;
+    if (tc) {
+        if ((rc = refine_m_tc(ws.R, N, batch, ws.Mt, ws.prod, st))) return rc;
+    } else {
+        k_f32_gemm<true, false><<<g64, FT, 0, st>>>(Uc, ws.R, nullptr, N, ws.Mt);
+        if ((rc = check_launch("k_f32_gemm<nt>"))) return rc;
+    }
     const dim3 gc(ceil_div(static_cast<int64_t>(N) * N, 256), batch);
     k_refine_coeffs<<<gc, 256, 0, st>>>(ws.Mt, evals, ws.nrm, N, ws.T);
     if ((rc = check_launch("k_refine_coeffs"))) return rc;
     // U' = U + T U
+    if (tc) return refine_update_tc(ws.T, Uc, ws.Mt, N, batch, U_out, ws.prod, st);
     k_f32_gemm<false, true><<<g64, FT, 0, st>>>(ws.T, Uc, Uc, N, U_out);
     return check_launch("k_f32_gemm<nn>");
 }

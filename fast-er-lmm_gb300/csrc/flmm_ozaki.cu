@@ -45,26 +45,36 @@ using namespace flmm::tc;
 
 namespace {
 
-constexpr int kUPlanes = 4;
-constexpr int kAPlanes = 7;
-constexpr int kLevels = 8;        // levels 0..7
 constexpr int kDigitShift = 7;    // bits per digit below the first
 constexpr int kMaxChunk = 1024;   // reduction of one launch (exact accumulation bound)
-constexpr int kBM = 128;          // U rows per tile (TMEM lanes)
-constexpr int kBN = 64;           // A rows per tile (columns of one level accumulator)
+constexpr int kBM = 128;          // A-side rows per tile (TMEM lanes)
+constexpr int kBN = 64;           // B-side rows per tile (columns of one level accumulator)
 constexpr int kBK = 32;           // reduction depth of one stage (64-byte rows, 64-byte swizzle)
-constexpr int kStages = 3;
-constexpr int kUTile = kBM * kBK * 2;                                   // 8 KB
-constexpr int kATile = kBN * kBK * 2;                                   // 4 KB
-constexpr int kStageBytes = kUPlanes * kUTile + kAPlanes * kATile;     // 60 KB
+constexpr int kATile = kBM * kBK * 2;                                   // 8 KB: one A-side plane
+constexpr int kBTile = kBN * kBK * 2;                                   // 4 KB: one B-side plane
 constexpr uint32_t kSBO = 8u * kBK * 2u;                                // bytes between 8-row groups
 constexpr uint32_t kSwizzle64 = 4u;
 constexpr int kThreads = 320;
 constexpr int kEpilogueThreads = 256;
-constexpr int kTmemCols = 512;                                          // 8 levels x 64 columns
-constexpr int kSmemBytes = kStages * kStageBytes + 256 + 1024;
-static_assert(kLevels * kBN <= kTmemCols, "tensor memory budget");
-static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
+
+// One configuration of the digit-plane product: PA planes on the A side (128 rows per tile), PB on the B side (64),
+// levels 0 .. LV - 1 kept, FP64 output (the refinement's A U) or FP32 output (its corrections).
+template <int PA, int PB, int LV, bool F64>
+struct OzCfg {
+    static constexpr int kStageBytes = PA * kATile + PB * kBTile;
+    static constexpr int kStages = (192 * 1024) / kStageBytes < 4 ? (192 * 1024) / kStageBytes : 4;
+    static constexpr int kTmemCols = LV * kBN <= 256 ? 256 : 512;
+    static constexpr int kSmemBytes = kStages * kStageBytes + 256 + 1024;
+    static_assert(LV * kBN <= kTmemCols && kTmemCols <= 512, "tensor memory budget");
+    static_assert(kStages >= 2, "pipeline depth");
+    static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
+};
+// Configurations used: the refinement's A U as <4, 7, 8, FP64> (U~ in 4 planes, A in 7, levels 0..7, 25 pairs); the
+// corrections u_i . r_j as <4, 4, 3, FP32> (6 pairs: the coefficients E_ij are themselves corrections and need ~1e-3
+// relative accuracy) and T U~ as <4, 4, 5, FP32> (13 pairs: FP32 accuracy against the row's largest rotation, which
+// reaches 0.25 for nearly degenerate pairs).
+constexpr int kUPlanes = 4;
+constexpr int kAPlanes = 7;
 static_assert(kMaxChunk % kBK == 0, "chunks must start on a k-block");
 
 struct OzMaps {
@@ -74,10 +84,12 @@ struct OzMaps {
 struct OzArgs {
     int N, batch;
     int k0, klen;        // reduction range of this launch
-    const int* eU;       // (batch N) row exponents of U
-    const int* eA;       // (batch N) row exponents of A
-    double* W;           // (batch, N, N)
-    int accumulate;      // add into W (launches after the first)
+    const int* eU;       // (batch N) row exponents of the A side
+    const int* eA;       // (batch N) row exponents of the B side
+    double* W;           // (batch, N, N), FP64 output
+    float* C;            // (batch, N, N), FP32 output
+    const float* D;      // (batch, N, N) added to the FP32 output, or null
+    int accumulate;      // add into the output (launches after the first)
     int* err;
 };
 
@@ -115,7 +127,7 @@ __global__ void k_digits_u(const float* __restrict__ U, int64_t rows, int N, __h
         float r = d[kUPlanes - 1];
 #pragma unroll
         for (int t = kUPlanes - 2; t >= 0; --t) r = d[t] + r * (1.0f / 128.0f);
-        Ut[j * N + n] = ldexpf(r, e - 6);
+        if (Ut) Ut[j * N + n] = ldexpf(r, e - 6);
     }
     if (lane == 0) expo[j] = e;
 }
@@ -153,7 +165,12 @@ __global__ void k_digits_a(const double* __restrict__ A, int64_t rows, int N, __
 
 // ---- the tensor-core product ----------------------------------------------------------------------------------
 
+template <int PA, int PB, int LV, bool F64>
 __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ OzMaps maps, const OzArgs args) {
+    using Cfg = OzCfg<PA, PB, LV, F64>;
+    constexpr int kStages = Cfg::kStages;
+    constexpr int kStageBytes = Cfg::kStageBytes;
+    constexpr int kTmemCols = Cfg::kTmemCols;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
@@ -214,11 +231,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
                     uint8_t* base = smem + stage * kStageBytes;
                     const int x = args.k0 + kb * kBK;
 #pragma unroll
-                    for (int p = 0; p < kUPlanes; ++p)
-                        tma_load_2d(base + p * kUTile, &maps.u, x, (p * args.batch + b) * N + ti * kBM, &full[stage]);
+                    for (int p = 0; p < PA; ++p)
+                        tma_load_2d(base + p * kATile, &maps.u, x, (p * args.batch + b) * N + ti * kBM, &full[stage]);
 #pragma unroll
-                    for (int p = 0; p < kAPlanes; ++p)
-                        tma_load_2d(base + kUPlanes * kUTile + p * kATile, &maps.a, x,
+                    for (int p = 0; p < PB; ++p)
+                        tma_load_2d(base + PA * kATile + p * kBTile, &maps.a, x,
                                     (p * args.batch + b) * N + tm * kBN, &full[stage]);
                     if (++stage == kStages) { stage = 0; phase ^= 1u; }
                 }
@@ -227,7 +244,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
                 if (armed[s]) mbar_drain(&full[s], armed_phase[s]);
         }
     } else if (warp == 1) {
-        // ---- MMA issuer: the 25 plane pairs of every 16-deep step, each into its level's accumulator ----
+        // ---- MMA issuer: the plane pairs (i, j) with i + j < LV of every 16-deep step, each into its level's
+        // accumulator ----
         if (lane == 0) {
             int stage = 0;
             uint32_t phase = 0;
@@ -243,15 +261,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
 #pragma unroll
                     for (int kk = 0; kk < kBK / 16; ++kk) {
 #pragma unroll
-                        for (int l = 0; l < kLevels; ++l) {
-                            const int i_lo = l - (kAPlanes - 1) > 0 ? l - (kAPlanes - 1) : 0;
-                            const int i_hi = l < kUPlanes - 1 ? l : kUPlanes - 1;
+                        for (int l = 0; l < LV; ++l) {
+                            const int i_lo = l - (PB - 1) > 0 ? l - (PB - 1) : 0;
+                            const int i_hi = l < PA - 1 ? l : PA - 1;
 #pragma unroll
                             for (int i = i_lo; i <= i_hi; ++i) {
                                 const int j = l - i;
-                                const uint64_t ad = smem_desc(sbase + i * kUTile, kSBO, kSwizzle64) + 2u * kk;
+                                const uint64_t ad = smem_desc(sbase + i * kATile, kSBO, kSwizzle64) + 2u * kk;
                                 const uint64_t bd =
-                                    smem_desc(sbase + kUPlanes * kUTile + j * kATile, kSBO, kSwizzle64) + 2u * kk;
+                                    smem_desc(sbase + PA * kATile + j * kBTile, kSBO, kSwizzle64) + 2u * kk;
                                 const uint32_t acc = (kb > 0 || kk > 0 || i > i_lo) ? 1u : 0u;
                                 mma_f16(tmem_base + static_cast<uint32_t>(l * kBN), ad, bd, idesc, acc);
                             }
@@ -284,25 +302,41 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
             const int i = ti * kBM + r;
             const bool row_ok = i < N;
             const int eu = row_ok ? args.eU[static_cast<int64_t>(b) * N + i] : 0;
-            double* wrow = args.W + (static_cast<int64_t>(b) * N + (row_ok ? i : 0)) * N;
+            const int64_t orow = (static_cast<int64_t>(b) * N + (row_ok ? i : 0)) * N;
 #pragma unroll 1
             for (int g = 0; g < 2; ++g) {
                 const int c0 = tm * kBN + half * (kBN / 2) + g * 16;
                 const uint32_t ta = tl0 + static_cast<uint32_t>(g * 16);
                 float hi[16], lo[16], v[16];
-                tmem_ld16_wait(ta, hi);
+                if constexpr (F64) {
+                    // double-FP32 sum of the levels, stored in FP64
+                    tmem_ld16_wait(ta, hi);
 #pragma unroll
-                for (int c = 0; c < 16; ++c) lo[c] = 0.0f;
+                    for (int c = 0; c < 16; ++c) lo[c] = 0.0f;
 #pragma unroll
-                for (int l = 1; l < kLevels; ++l) {
-                    tmem_ld16_wait(ta + static_cast<uint32_t>(l * kBN), v);
-                    const float w = ldexpf(1.0f, -kDigitShift * l);
+                    for (int l = 1; l < LV; ++l) {
+                        tmem_ld16_wait(ta + static_cast<uint32_t>(l * kBN), v);
+                        const float w = ldexpf(1.0f, -kDigitShift * l);
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        float s, err;
-                        two_sum(hi[c], v[c] * w, s, err);
-                        hi[c] = s;
-                        lo[c] += err;
+                        for (int c = 0; c < 16; ++c) {
+                            float s, err;
+                            two_sum(hi[c], v[c] * w, s, err);
+                            hi[c] = s;
+                            lo[c] += err;
+                        }
+                    }
+                } else {
+                    // FP32 sum of the levels, smallest first
+                    tmem_ld16_wait(ta + static_cast<uint32_t>((LV - 1) * kBN), hi);
+                    const float wl = ldexpf(1.0f, -kDigitShift * (LV - 1));
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) hi[c] *= wl;
+#pragma unroll
+                    for (int l = LV - 2; l >= 0; --l) {
+                        tmem_ld16_wait(ta + static_cast<uint32_t>(l * kBN), v);
+                        const float w = ldexpf(1.0f, -kDigitShift * l);
+#pragma unroll
+                        for (int c = 0; c < 16; ++c) hi[c] = fmaf(v[c], w, hi[c]);
                     }
                 }
                 if (row_ok) {
@@ -311,8 +345,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
                         const int m = c0 + c;
                         if (m < N) {
                             const int ex = eu + args.eA[static_cast<int64_t>(b) * N + m] - 12;
-                            const double x = ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]), ex);
-                            wrow[m] = args.accumulate ? wrow[m] + x : x;
+                            if constexpr (F64) {
+                                const double x = ldexp(static_cast<double>(hi[c]) + static_cast<double>(lo[c]), ex);
+                                args.W[orow + m] = args.accumulate ? args.W[orow + m] + x : x;
+                            } else {
+                                float x = ldexpf(hi[c], ex);
+                                if (args.accumulate) x += args.C[orow + m];
+                                else if (args.D) x += args.D[orow + m];
+                                args.C[orow + m] = x;
+                            }
                         }
                     }
                 }
@@ -331,10 +372,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki(const __grid_constant__ O
     }
 }
 
+// Workspace: 11 digit planes in one block (the product's 4 + 7; the corrections reuse them: T over planes 0-1,
+// its digits on planes 2-5, the digits of U~^T on planes 6-9, the residuals' digits on planes 4-7) and the row
+// exponents of both sides.
 struct OzWs {
+    __half* planes;
     __half *up, *ap;
     int *eu, *ea;
-    int64_t ldp;
+    int64_t ldp, plane;  // elements per plane: rows x ldp
     size_t bytes;
 };
 
@@ -342,14 +387,16 @@ OzWs carve_oz(void* base, int N, int batch) {
     OzWs w{};
     w.ldp = (static_cast<int64_t>(N) + 7) / 8 * 8;
     const size_t rows = static_cast<size_t>(N) * batch;
+    w.plane = static_cast<int64_t>(rows) * w.ldp;
     size_t off = 0;
     auto take = [&](size_t nbytes) {
         void* p = base ? static_cast<char*>(base) + off : nullptr;
         off += (nbytes + 1023) / 1024 * 1024;
         return p;
     };
-    w.up = static_cast<__half*>(take(sizeof(__half) * kUPlanes * rows * w.ldp));
-    w.ap = static_cast<__half*>(take(sizeof(__half) * kAPlanes * rows * w.ldp));
+    w.planes = static_cast<__half*>(take(sizeof(__half) * (kUPlanes + kAPlanes) * rows * w.ldp));
+    w.up = w.planes;
+    w.ap = w.planes ? w.planes + kUPlanes * w.plane : nullptr;
     w.eu = static_cast<int*>(take(sizeof(int) * rows));
     w.ea = static_cast<int*>(take(sizeof(int) * rows));
     w.bytes = off;
@@ -363,34 +410,34 @@ int sm_count_current() {
     return sm;
 }
 
-}  // namespace
+// FP32 rows (rows, pitch N) -> 4 digit planes at `planes` (plane stride w.plane) and row exponents; Ut (optional) the
+// rounding the planes represent.
+int digits_f32(const float* X, int64_t rows, int N, __half* planes, const OzWs& w, int* expo, float* Ut,
+               cudaStream_t st) {
+    k_digits_u<<<ceil_div(rows * 32, 256), 256, 0, st>>>(X, rows, N, planes, w.ldp, rows, expo, Ut);
+    return check_launch("k_digits_u");
+}
 
-namespace flmm {
-
-size_t refine_product_tc_bytes(int N, int batch) { return carve_oz(nullptr, N, batch).bytes; }
-
-// W (batch, N, N) FP64 = U~ A^T with U~ (written to Ut) the digit-plane rounding of U; work of
-// refine_product_tc_bytes(N, batch) bytes (1,024-byte aligned).
-int refine_product_tc(const float* U, const double* A, int N, int batch, float* Ut, double* W, void* work,
-                      cudaStream_t st) {
-    const OzWs w = carve_oz(work, N, batch);
+// The digit-plane product of configuration <PA, PB, LV, F64>: out[b][i][m] = sum over pairs of A-side planes (rows i)
+// and B-side planes (rows m), scaled by the row exponents; FP64 into W or FP32 into C (+ D).  Reductions longer than
+// kMaxChunk run as several launches that add into the output.
+template <int PA, int PB, int LV, bool F64>
+int launch_oz(const __half* aplanes, const int* ea_side, const __half* bplanes, const int* eb_side, int N, int batch,
+              const OzWs& w, double* W, float* C, const float* D, cudaStream_t st) {
+    using Cfg = OzCfg<PA, PB, LV, F64>;
     const int64_t rows = static_cast<int64_t>(N) * batch;
-    const int64_t plane_rows = rows;
-    if (rows * kAPlanes > 0x7fffffffLL) return fail(FLMM_ERR_ARG, "refine product: too many rows for a TMA map");
-    k_digits_u<<<ceil_div(rows * 32, 256), 256, 0, st>>>(U, rows, N, w.up, w.ldp, plane_rows, w.eu, Ut);
-    int rc = check_launch("k_digits_u");
-    if (rc) return rc;
-    k_digits_a<<<ceil_div(rows * 32, 256), 256, 0, st>>>(A, rows, N, w.ap, w.ldp, plane_rows, w.ea);
-    if ((rc = check_launch("k_digits_a"))) return rc;
-
+    if (rows * PB > 0x7fffffffLL || rows * PA > 0x7fffffffLL)
+        return fail(FLMM_ERR_ARG, "refine product: too many rows for a TMA map");
     OzMaps maps;
     std::memset(&maps, 0, sizeof(maps));
-    if ((rc = tc::make_map_f16(&maps.u, w.up, static_cast<int>(kUPlanes * rows), N, w.ldp, kBK, kBM))) return rc;
-    if ((rc = tc::make_map_f16(&maps.a, w.ap, static_cast<int>(kAPlanes * rows), N, w.ldp, kBK, kBN))) return rc;
+    int rc;
+    if ((rc = tc::make_map_f16(&maps.u, aplanes, static_cast<int>(PA * rows), N, w.ldp, kBK, kBM))) return rc;
+    if ((rc = tc::make_map_f16(&maps.a, bplanes, static_cast<int>(PB * rows), N, w.ldp, kBK, kBN))) return rc;
     static std::once_flag attr_once;
     static cudaError_t attr_rc = cudaSuccess;
     std::call_once(attr_once, [] {
-        attr_rc = cudaFuncSetAttribute(k_ozaki, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+        attr_rc = cudaFuncSetAttribute(k_ozaki<PA, PB, LV, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       Cfg::kSmemBytes);
     });
     if (attr_rc != cudaSuccess) return fail(FLMM_ERR_CUDA, "k_ozaki: %s", cudaGetErrorString(attr_rc));
     int dev = 0;
@@ -407,15 +454,85 @@ int refine_product_tc(const float* U, const double* A, int N, int batch, float* 
         a.batch = batch;
         a.k0 = k0;
         a.klen = N - k0 < kMaxChunk ? N - k0 : kMaxChunk;
-        a.eU = w.eu;
-        a.eA = w.ea;
+        a.eU = ea_side;
+        a.eA = eb_side;
         a.W = W;
+        a.C = C;
+        a.D = D;
         a.accumulate = k0 > 0;
         a.err = err;
-        k_ozaki<<<grid, kThreads, kSmemBytes, st>>>(maps, a);
+        k_ozaki<PA, PB, LV, F64><<<grid, kThreads, Cfg::kSmemBytes, st>>>(maps, a);
         if ((rc = check_launch("k_ozaki"))) return rc;
     }
     return FLMM_OK;
+}
+
+// batched (N, N) FP32 transpose, 32 x 32 tiles through shared memory
+__global__ void k_transpose_f32(const float* __restrict__ X, int N, float* __restrict__ Y) {
+    __shared__ float t[32][33];
+    const int64_t nn = static_cast<int64_t>(N) * N;
+    const float* x = X + blockIdx.z * nn;
+    float* y = Y + blockIdx.z * nn;
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int i = by + r, j = bx + threadIdx.x;
+        t[r][threadIdx.x] = (i < N && j < N) ? x[static_cast<int64_t>(i) * N + j] : 0.0f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int i = bx + r, j = by + threadIdx.x;
+        if (i < N && j < N) y[static_cast<int64_t>(i) * N + j] = t[threadIdx.x][r];
+    }
+}
+
+}  // namespace
+
+namespace flmm {
+
+size_t refine_product_tc_bytes(int N, int batch) { return carve_oz(nullptr, N, batch).bytes; }
+
+// W (batch, N, N) FP64 = U~ A^T with U~ (written to Ut) the digit-plane rounding of U; work of
+// refine_product_tc_bytes(N, batch) bytes (1,024-byte aligned).  The digit planes of U~ stay in the workspace for
+// refine_m_tc.
+int refine_product_tc(const float* U, const double* A, int N, int batch, float* Ut, double* W, void* work,
+                      cudaStream_t st) {
+    const OzWs w = carve_oz(work, N, batch);
+    const int64_t rows = static_cast<int64_t>(N) * batch;
+    int rc = digits_f32(U, rows, N, w.up, w, w.eu, Ut, st);
+    if (rc) return rc;
+    k_digits_a<<<ceil_div(rows * 32, 256), 256, 0, st>>>(A, rows, N, w.ap, w.ldp, rows, w.ea);
+    if ((rc = check_launch("k_digits_a"))) return rc;
+    return launch_oz<4, 7, 8, true>(w.up, w.eu, w.ap, w.ea, N, batch, w, W, nullptr, nullptr, st);
+}
+
+// M[b][i][j] = u~_i . r_j (FP32) from the digit planes of U~ that refine_product_tc left in `work` and the residual
+// rows R (batch N, N) FP32.
+int refine_m_tc(const float* R, int N, int batch, float* M, void* work, cudaStream_t st) {
+    const OzWs w = carve_oz(work, N, batch);
+    const int64_t rows = static_cast<int64_t>(N) * batch;
+    __half* rp = w.planes + 4 * w.plane;
+    int rc = digits_f32(R, rows, N, rp, w, w.ea, nullptr, st);
+    if (rc) return rc;
+    return launch_oz<4, 4, 3, false>(w.up, w.eu, rp, w.ea, N, batch, w, nullptr, M, nullptr, st);
+}
+
+// U_out = U~ + T U~ (FP32), T (batch, N, N) FP32 at the start of `work` (over planes 0-1), scratch an (batch, N, N)
+// FP32 buffer for U~^T.
+int refine_update_tc(const float* T, const float* Ut, float* scratch, int N, int batch, float* U_out, void* work,
+                     cudaStream_t st) {
+    const OzWs w = carve_oz(work, N, batch);
+    const int64_t rows = static_cast<int64_t>(N) * batch;
+    if (reinterpret_cast<const char*>(T) + sizeof(float) * rows * N > reinterpret_cast<const char*>(w.planes + 2 * w.plane))
+        return fail(FLMM_ERR_ARG, "refine update: T overlaps its digit planes");
+    const dim3 tg(ceil_div(N, 32), ceil_div(N, 32), batch);
+    k_transpose_f32<<<tg, dim3(32, 8), 0, st>>>(Ut, N, scratch);
+    int rc = check_launch("k_transpose_f32");
+    if (rc) return rc;
+    __half* tp = w.planes + 2 * w.plane;
+    __half* up = w.planes + 6 * w.plane;
+    if ((rc = digits_f32(T, rows, N, tp, w, w.eu, nullptr, st))) return rc;
+    if ((rc = digits_f32(scratch, rows, N, up, w, w.ea, nullptr, st))) return rc;
+    return launch_oz<4, 4, 5, false>(tp, w.eu, up, w.ea, N, batch, w, nullptr, U_out, Ut, st);
 }
 
 }  // namespace flmm
