@@ -469,6 +469,10 @@ class _RowSink:
     def __init__(self, out: dict, host_out: dict, dev: torch.device, host_nullh2: bool = False):
         self.out, self.host, self.dev = out, host_out, dev
         self.stream = torch.cuda.Stream(device=dev)
+        # the (n_real,) nullh2 vectors cross on their own stream, so a chromosome's host-side row fill starts when
+        # its fit is done instead of behind the earlier chromosomes' result copies (the link is the step's bottleneck
+        # once results flow, and the fills would otherwise finish after the last copy)
+        self.vec_stream = torch.cuda.Stream(device=dev)
         self.pending = []  # row ranges not copied early
         self.host_nullh2 = host_nullh2
         self.fills = []
@@ -493,11 +497,11 @@ class _RowSink:
         vh = torch.empty(vec.shape, dtype=vec.dtype, pin_memory=True)
         ev = torch.cuda.Event()
         ev.record(torch.cuda.current_stream(self.dev))
-        self.stream.wait_event(ev)
+        self.vec_stream.wait_event(ev)
         done = torch.cuda.Event()
-        with torch.cuda.stream(self.stream):
+        with torch.cuda.stream(self.vec_stream):
             vh.copy_(vec, non_blocking=True)
-            done.record(self.stream)
+            done.record(self.vec_stream)
         dst = self.host["nullh2"]
         ld = dst.stride(0)
 
@@ -534,6 +538,7 @@ class _RowSink:
             self.host["max_F"].copy_(max_F, non_blocking=True)
         main.synchronize()
         self.stream.synchronize()
+        self.vec_stream.synchronize()
         for f, _, _ in self.fills:
             f.result()
         if self.pool is not None:
