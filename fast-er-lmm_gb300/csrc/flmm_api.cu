@@ -15,12 +15,19 @@
 #include "flmm_common.cuh"
 
 constexpr int kEighWorkers = 8;
+constexpr int kFlagSlots = 64;
 
 struct flmm_context {
     int device = 0;
     int sm_count = 0;
     cusolverDnHandle_t solver = nullptr;
     int* err_flag = nullptr;  // device int raised by kernels whose bounded waits time out
+    // mapped host copies of the flags for flmm_context_check (kFlagSlots pairs, one per concurrent call): a kernel
+    // writes them over the host link, so reading them never queues on the copy engines behind a scan's streamed
+    // result copies
+    int* flags_host = nullptr;
+    int* flags_dev = nullptr;
+    std::atomic<unsigned> flag_slot{0};
     // worker streams / handles for running independent eigendecompositions side by side
     cudaStream_t workers[kEighWorkers] = {};
     cusolverDnHandle_t wsolver[kEighWorkers] = {};
@@ -106,6 +113,11 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
         delete ctx;
         return fail(FLMM_ERR_CUDA, "flmm_context_create: cannot allocate the device error flag");
     }
+    if (cudaHostAlloc(&ctx->flags_host, 2 * kFlagSlots * sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&ctx->flags_dev, ctx->flags_host, 0) != cudaSuccess) {
+        flmm_context_destroy(ctx);
+        return fail(FLMM_ERR_CUDA, "flmm_context_create: cannot allocate the mapped flag buffer");
+    }
     bool ok = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) == cudaSuccess &&
               cusolverDnCreateParams(&ctx->params) == CUSOLVER_STATUS_SUCCESS;
     for (int w = 0; ok && w < kEighWorkers; ++w) {
@@ -140,13 +152,26 @@ int* flmm::device_err_flag(int device) {
     return flags[device];
 }
 
+// both error flags into the context's mapped host buffer
+__global__ void k_read_flags(const int* __restrict__ ctx_flag, const int* __restrict__ dev_flag, int* out) {
+    if (threadIdx.x == 0) {
+        out[0] = *reinterpret_cast<const volatile int*>(ctx_flag);
+        out[1] = dev_flag ? *reinterpret_cast<const volatile int*>(dev_flag) : 0;
+    }
+}
+
 extern "C" int flmm_context_check(flmm_context* ctx, void* stream) {
     FLMM_REQUIRE(ctx, "flmm_context_check: NULL context");
-    int h[2] = {0, 0};
     int* dflag = device_err_flag(ctx->device);
-    FLMM_CUDA(cudaMemcpyAsync(&h[0], ctx->err_flag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
-    if (dflag) FLMM_CUDA(cudaMemcpyAsync(&h[1], dflag, sizeof(int), cudaMemcpyDeviceToHost, as_stream(stream)));
+    const unsigned slot = ctx->flag_slot.fetch_add(1u) % kFlagSlots;
+    volatile int* hf = ctx->flags_host + 2 * slot;
+    hf[0] = 0;
+    hf[1] = 0;
+    k_read_flags<<<1, 32, 0, as_stream(stream)>>>(ctx->err_flag, dflag, ctx->flags_dev + 2 * slot);
+    int rc = check_launch("k_read_flags");
+    if (rc) return rc;
     FLMM_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    const int h[2] = {hf[0], hf[1]};
     if (h[0] != 0 || h[1] != 0) {
         FLMM_CUDA(cudaMemsetAsync(ctx->err_flag, 0, sizeof(int), as_stream(stream)));
         if (dflag) FLMM_CUDA(cudaMemsetAsync(dflag, 0, sizeof(int), as_stream(stream)));
@@ -159,6 +184,7 @@ extern "C" int flmm_context_destroy(flmm_context* ctx) {
     if (!ctx) return FLMM_OK;
     if (ctx->solver) cusolverDnDestroy(ctx->solver);
     if (ctx->err_flag) cudaFree(ctx->err_flag);
+    if (ctx->flags_host) cudaFreeHost(ctx->flags_host);
     for (int w = 0; w < kEighWorkers; ++w) {
         if (ctx->wsolver[w]) cusolverDnDestroy(ctx->wsolver[w]);
         if (ctx->workers[w]) cudaStreamDestroy(ctx->workers[w]);

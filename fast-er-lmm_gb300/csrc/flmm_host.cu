@@ -33,3 +33,25 @@ extern "C" int flmm_fill_rows_host_f64(double* dst, int64_t ld, int64_t rows, co
     for (auto& th : pool) th.join();
     return FLMM_OK;
 }
+
+extern "C" int flmm_host_alloc_mapped(size_t bytes, void** host_ptr, void** dev_ptr) {
+    FLMM_REQUIRE(host_ptr && dev_ptr && bytes > 0, "flmm_host_alloc_mapped: bad arguments");
+    *host_ptr = nullptr;
+    *dev_ptr = nullptr;
+    void* h = nullptr;
+    FLMM_CUDA(cudaHostAlloc(&h, bytes, cudaHostAllocMapped));
+    void* d = nullptr;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess || d == nullptr) {
+        cudaFreeHost(h);
+        return flmm::fail(FLMM_ERR_CUDA, "flmm_host_alloc_mapped: no device mapping (%s)", cudaGetErrorString(e));
+    }
+    *host_ptr = h;
+    *dev_ptr = d;
+    return FLMM_OK;
+}
+
+extern "C" int flmm_host_free_mapped(void* host_ptr) {
+    if (host_ptr) FLMM_CUDA(cudaFreeHost(host_ptr));
+    return FLMM_OK;
+}

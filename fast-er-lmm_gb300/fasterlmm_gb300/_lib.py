@@ -91,6 +91,8 @@ SIGNATURES: dict[str, list] = {
     "flmm_write_gwas_tsv": [_s, _i64, _p, _p, _p, _p, _p, _d, _p, _p, _p, _p, _p, _i64, _p, _i64, _s, _i64],
     "flmm_write_column_tsv": [_s, _s, _p, _i64],
     "flmm_fill_rows_host_f64": [_p, _i64, _i64, _p, _i64, _i],
+    "flmm_host_alloc_mapped": [_sz, C.POINTER(_p), C.POINTER(_p)],
+    "flmm_host_free_mapped": [_p],
     "flmm_context_check": [_p, _p],
     "flmm_split_rows_f16": [_p, _i, _i64, _i, _i, _p, _p, _i64, _p, _p],
     "flmm_gemm_split_f16": [_p, _p, _p, _p, _i64, _i, _p, _p, _p, _i64, _i, _i, _p, _i64, _i, _p],

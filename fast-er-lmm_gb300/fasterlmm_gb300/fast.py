@@ -16,6 +16,8 @@ with each chromosome's columns starting on a 64-column boundary, so the Gram of 
 
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import torch
 from torch import Tensor
@@ -402,9 +404,9 @@ def scan_t(Zt: Tensor, X: Tensor, Yt: Tensor, chrom: np.ndarray, *, n_real: int,
         if sink is not None:
             sink.push(order, a, n)
             if host_nullh2 and n:
-                vec = torch.empty(n_real, dtype=F64, device=dev)
-                _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(nullh2_row), 1, _ptr(vec), n_real, st)
-                sink.push_nullh2(vec, order, a, n)
+                vh, vd = sink.mapped_vec(n_real)
+                _lib.call("flmm_fill_nullh2", _ptr(ld), n_real, _ptr(nullh2_row), 1, vd, n_real, st)
+                sink.push_nullh2(vh, n_real, order, a, n)
         if on_chrom is not None:
             on_chrom(k_idx + 1, len(units))
     _lib.call("flmm_context_check", ctx, st)
@@ -451,6 +453,10 @@ def _spectrum(evals: Tensor, D: int) -> Tensor:
     return s
 
 
+# mapped host buffers for the streamed nullh2 vectors, by size, kept for the process (host_alloc is slow)
+_MAPPED_FREE: dict = {}
+
+
 class _RowSink:
     """
     Copies finished result rows into caller tensors on a side stream.  A chromosome whose rows are contiguous in
@@ -464,22 +470,26 @@ class _RowSink:
     """
 
     KEYS = ("f", "beta", "se", "sfve", "nullh2")
-    FILL_THREADS = 8
+    # Row fills and result copies both write host memory.  Per step of the 1,000 x 100,000 x 71,324 scan (e2e, median
+    # of 4): fills deferred until the copies drained 197 ms, fills beside the copies on 2 x 8 threads 227 ms (the
+    # copies slowed from 5.4 to ~8 ms per chromosome), on one worker of 2 threads 173 ms (the copies keep most of
+    # the bandwidth and the fills finish with them).
+    FILL_THREADS = 2
+    FILL_WORKERS = 1
 
     def __init__(self, out: dict, host_out: dict, dev: torch.device, host_nullh2: bool = False):
         self.out, self.host, self.dev = out, host_out, dev
         self.stream = torch.cuda.Stream(device=dev)
-        # the (n_real,) nullh2 vectors cross on their own stream, so a chromosome's host-side row fill starts when
-        # its fit is done instead of behind the earlier chromosomes' result copies (the link is the step's bottleneck
-        # once results flow, and the fills would otherwise finish after the last copy)
-        self.vec_stream = torch.cuda.Stream(device=dev)
+        # mapped host buffers of the (n_real,) nullh2 vectors, written by the kernel that forms them: a copy would
+        # queue on the copy engine behind the earlier chromosomes' result copies
+        self.mapped = []
         self.pending = []  # row ranges not copied early
         self.host_nullh2 = host_nullh2
         self.fills = []
         self.pool = None
         if host_nullh2:
             from concurrent.futures import ThreadPoolExecutor
-            self.pool = ThreadPoolExecutor(max_workers=2)
+            self.pool = ThreadPoolExecutor(max_workers=self.FILL_WORKERS)
 
     @staticmethod
     def host_fill_possible(host_out: dict | None, order, blocks) -> bool:
@@ -489,29 +499,36 @@ class _RowSink:
         return order is None or all(np.array_equal(order[a:a + n], np.arange(order[a], order[a] + n))
                                     for _, a, n in blocks if n)
 
-    def push_nullh2(self, vec: Tensor, order, a: int, n: int) -> None:
-        """Copy one chromosome's nullh2 vector (n_real,) to the host and fill its n rows there."""
+    def mapped_vec(self, n_real: int) -> tuple[int, int]:
+        """A mapped host buffer of n_real doubles: (host address, device address)."""
+        nbytes = 8 * max(n_real, 1)
+        free = _MAPPED_FREE.setdefault(nbytes, [])
+        if free:
+            hp, dp = free.pop()
+        else:
+            h, d = C.c_void_p(), C.c_void_p()
+            _lib.call("flmm_host_alloc_mapped", nbytes, C.byref(h), C.byref(d))
+            hp, dp = h.value, d.value
+        self.mapped.append((nbytes, hp, dp))
+        return hp, dp
+
+    def push_nullh2(self, vec_host: int, n_real: int, order, a: int, n: int) -> None:
+        """Fill one chromosome's n rows of the host nullh2 table from its vector, which the kernel just queued on the
+        current stream writes into the mapped buffer at vec_host."""
         if n == 0:
             return
         r0 = a if order is None else int(order[a])
-        vh = torch.empty(vec.shape, dtype=vec.dtype, pin_memory=True)
-        ev = torch.cuda.Event()
-        ev.record(torch.cuda.current_stream(self.dev))
-        self.vec_stream.wait_event(ev)
         done = torch.cuda.Event()
-        with torch.cuda.stream(self.vec_stream):
-            vh.copy_(vec, non_blocking=True)
-            done.record(self.vec_stream)
+        done.record(torch.cuda.current_stream(self.dev))
         dst = self.host["nullh2"]
         ld = dst.stride(0)
 
         def fill():
             done.synchronize()
-            _lib.call("flmm_fill_rows_host_f64", dst.data_ptr() + 8 * r0 * ld, ld, n, vh.data_ptr(), vh.numel(),
+            _lib.call("flmm_fill_rows_host_f64", dst.data_ptr() + 8 * r0 * ld, ld, n, vec_host, n_real,
                       self.FILL_THREADS)
 
-        # vec and vh stay referenced until finish(): the side stream may copy vec after this call returns
-        self.fills.append((self.pool.submit(fill), vh, vec))
+        self.fills.append((self.pool.submit(fill), None, None))
 
     def push(self, order, a: int, n: int) -> None:
         if n == 0:
@@ -538,11 +555,13 @@ class _RowSink:
             self.host["max_F"].copy_(max_F, non_blocking=True)
         main.synchronize()
         self.stream.synchronize()
-        self.vec_stream.synchronize()
         for f, _, _ in self.fills:
             f.result()
         if self.pool is not None:
             self.pool.shutdown(wait=True)
+        for nbytes, hp, dp in self.mapped:
+            _MAPPED_FREE.setdefault(nbytes, []).append((hp, dp))
+        self.mapped = []
         pick = lambda k, t: self.host[k] if k in self.host else t
         res = {k: pick(k, v) for k, v in self.out.items()}
         if self.host_nullh2:

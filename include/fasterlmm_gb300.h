@@ -564,6 +564,13 @@ int flmm_write_column_tsv(const char* path, const char* header, const double* v,
  * device.  No counterpart in the reference, which keeps its results on one device. */
 int flmm_fill_rows_host_f64(double* dst, int64_t ld, int64_t rows, const double* vec, int64_t n, int threads);
 
+/* Page-locked host memory mapped into the device's address space (cudaHostAllocMapped): *host_ptr for the host,
+ * *dev_ptr for kernels, which then write it over the host link without the copy engines (whose queue the scan's
+ * result copies occupy).  The streamed result path has each chromosome's nullh2 vector written there.  Free with
+ * flmm_host_free_mapped. */
+int flmm_host_alloc_mapped(size_t bytes, void** host_ptr, void** dev_ptr);
+int flmm_host_free_mapped(void* host_ptr);
+
 #ifdef __cplusplus
 }
 #endif
