@@ -11,9 +11,10 @@
 //           and the per-chromosome Gram (fasterlmm/io.py:264);
 //   NG = 2: the Wald scan (fasterlmm/core.py:649-667): sWy = (w o UY) US^T and sWs = w (US o US)^T accumulated
 //           side by side, with beta, var_beta, F, SE, SFVE and the per-column genome max computed in the epilogue.
-// Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, warps 2-9 run the epilogue
-// (warp w reads TMEM lanes 32 (w % 4) .. +31, half of the tile's columns).  Shared memory holds 192 KB of operand
-// stages.
+// Warp roles: warp 0 issues TMA loads, warp 1 owns tensor memory and issues the MMAs, the rest run the epilogue
+// (warp w reads TMEM lanes 32 (w % 4) .. +31): warps 2-9 with half of the tile's columns each in the single-CTA
+// kernel, warps 2-17 with a quarter each in the pair kernel (four epilogue warps per scheduler, 96 registers a
+// thread).  Shared memory holds 192 KB of operand stages.
 //
 // Accumulation in K chunks: the tensor core's FP32 accumulation does not round to nearest -- every MMA step loses
 // about an ulp of the accumulator's magnitude towards zero, so a product over K accumulated in one place carries a
@@ -45,6 +46,10 @@ constexpr int kBM = 128;  // A rows per tile (TMEM lanes)
 constexpr int kBN = 128;  // B rows per tile (accumulator columns)
 constexpr int kThreads = 320;        // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kEpilogueThreads = 256;
+// the pair kernel: warp 0 TMA, warp 1 MMA, warps 2-17 epilogue (four per TMEM lane quarter, 32 columns each)
+constexpr int kPairEpiWarps = 16;
+constexpr int kPairThreads = 64 + 32 * kPairEpiWarps;
+constexpr int kPairCols = kBN / (kPairEpiWarps / 4);  // accumulator columns per epilogue thread
 constexpr int kBK = 64;  // reduction depth of one pipeline stage: 64 gives 3 stages of 64 KB, 32 gives 6 of 32 KB
 constexpr int kSlots = 4;  // tensor-memory chunk accumulators of kBN columns (all 512 columns)
 // k-blocks of 64 per chunk accumulator (TcArgs::chunk_kb; FLMM_CHUNK_KB / FLMM_WALD_CHUNK_KB override): 2 for the
@@ -138,9 +143,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // Wald statistics of one epilogue thread: accumulator row p (a column of the phenotype table) against tile columns
 // [cbeg, cbeg + 64) (variants): the sums of product 0 in y[] (drained from its chunk accumulators), product 1 read
 // from its TMEM slot at tl_s (this thread's lane, column cbeg), the warp's staged scales sc1 / sc2 and output rows.
-__device__ __forceinline__ void wald_rows(const TcArgs& args, const float (&y)[64], uint32_t tl_s, int p,
+template <int NC>
+__device__ __forceinline__ void wald_rows(const TcArgs& args, const float (&y)[NC], uint32_t tl_s, int p,
                                           bool real_tile, int nvalid, int cbeg, int mbase, const float* sc1,
                                           const float* sc2, const int64_t* rws) {
+    static_assert(NC == 32 || NC == 64, "columns per epilogue thread");
     // Wald statistics (fasterlmm/core.py:651-667) in FP32 on the unscaled sums, rearranged so that each test needs
     // two reciprocals: with q = sWy^2 / sWs and rss = rWr - q,
     //     F = beta^2 / var_beta = q df / rss,  beta = sWy / sWs,  var_beta = rss / (df sWs).
@@ -155,12 +162,16 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, const float (&y)[6
     // one 16-column quarter per iteration; the loop is kept rolled (the statistics' code is long) and the quarter's
     // sums are picked from the register array by selects
 #pragma unroll 1
-    for (int qd = 0; qd < 4; ++qd) {
+    for (int qd = 0; qd < NC / 16; ++qd) {
         const int c0 = cbeg + 16 * qd;
         float vy[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            vy[j] = qd == 0 ? y[j] : (qd == 1 ? y[16 + j] : (qd == 2 ? y[32 + j] : y[48 + j]));
+        for (int j = 0; j < 16; ++j) {
+            if constexpr (NC == 64)
+                vy[j] = qd == 0 ? y[j] : (qd == 1 ? y[16 + j] : (qd == 2 ? y[32 + j] : y[48 + j]));
+            else
+                vy[j] = qd == 0 ? y[j] : y[16 + j];
+        }
         float vs[16];
         tmem_ld16_wait(tl_s + static_cast<uint32_t>(16 * qd), vs);
         if (!row_ok) continue;
@@ -224,14 +235,15 @@ __device__ __forceinline__ void wald_rows(const TcArgs& args, const float (&y)[6
 
 // C = sa sb^T (acc) for one epilogue thread: accumulator row i against tile columns [cbeg, cbeg + 64) starting at
 // column col0 of C, with the drained sums v[], staged column scales sc1.
-__device__ __forceinline__ void gemm_rows(const TcArgs& args, const float (&v)[64], int i, int col0, int nvalid,
+template <int NC>
+__device__ __forceinline__ void gemm_rows(const TcArgs& args, const float (&v)[NC], int i, int col0, int nvalid,
                                           int cbeg, const float* sc1) {
     const bool row_ok = i < args.Mr;
     if (!row_ok) return;
     const float sa = args.sa[i];
     float* crow = args.C + static_cast<int64_t>(i) * args.ldc + col0;
 #pragma unroll
-    for (int qd = 0; qd < 4; ++qd) {
+    for (int qd = 0; qd < NC / 16; ++qd) {
         const int c0 = cbeg + 16 * qd;
         const float* sc = sc1 + 16 * qd;
         const float* vv = v + 16 * qd;
@@ -289,6 +301,17 @@ __device__ __forceinline__ void drain64(uint32_t tl, float (&acc)[64]) {
         : "memory");
 #pragma unroll
     for (int j = 0; j < 64; ++j) acc[j] += __uint_as_float(v[j]);
+}
+
+// The same for 32 columns: two loads in flight, one wait.
+__device__ __forceinline__ void drain32(uint32_t tl, float (&acc)[32]) {
+    float a[16], b[16];
+    tmem_ld16x2(tl, tl + 16u, a, b);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        acc[j] += a[j];
+        acc[16 + j] += b[j];
+    }
 }
 
 template <int NG, int BK>
@@ -504,8 +527,8 @@ struct PairCfg {
     static constexpr uint32_t kSBO = 1024u;    // bytes between 8-row groups
     static constexpr int kTmemCols = kSlots * kBN;  // the ring of chunk accumulators
     static constexpr int kBarBytes = 256;
-    static constexpr int kEpiWarpBytes = 64 * 4 * 2 + 64 * 8;
-    static constexpr int kEpiBytes = 8 * kEpiWarpBytes;
+    static constexpr int kEpiWarpBytes = kPairCols * 4 * 2 + kPairCols * 8;
+    static constexpr int kEpiBytes = kPairEpiWarps * kEpiWarpBytes;
     static constexpr int kSmemBytes = kStages * kStageBytes + kBarBytes + kEpiBytes + 1024;
     static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
 };
@@ -514,7 +537,7 @@ constexpr int kPairRows = 256;  // A rows per pair tile
 
 
 template <int NG>
-__global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ TcMaps maps, const TcArgs args) {
+__global__ void __launch_bounds__(kPairThreads, 1) k_pair(const __grid_constant__ TcMaps maps, const TcArgs args) {
     using C = PairCfg<NG>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -545,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
         }
         for (int b = 0; b < kSlots; ++b) {
             mbar_init(&slot_full[b], 1);
-            mbar_init(&slot_empty[b], 2 * (kEpilogueThreads / 32));
+            mbar_init(&slot_empty[b], 2 * kPairEpiWarps);
         }
         mbar_init(final_bar, 1);
         fence_barrier_init();
@@ -648,13 +671,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
             mbar_drain(final_bar, 0);
         }
     } else {
-        // ---- epilogue (both CTAs): as in k_tc, rows of this CTA's half of the pair tile ----
+        // ---- epilogue (both CTAs): warps 2..17, warp w reads TMEM lanes 32 (w % 4) .. +31 (thread = one accumulator
+        // row of this CTA's half of the pair tile) and quarter (w - 2) / 4 of the tile's columns: four warps per lane
+        // quarter, so that each scheduler has four epilogue warps to hide the epilogue's latencies with ----
         const int q = warp & 3;
-        const int cbeg = ((warp - 2) >> 2) * (kBN / 2);
+        const int cbeg = ((warp - 2) >> 2) * kPairCols;
         const int r = q * 32 + lane;
         float* sc1 = reinterpret_cast<float*>(epi_smem + (warp - 2) * C::kEpiWarpBytes);
-        float* sc2 = sc1 + 64;
-        int64_t* rws = reinterpret_cast<int64_t*>(sc2 + 64);
+        float* sc2 = sc1 + kPairCols;
+        int64_t* rws = reinterpret_cast<int64_t*>(sc2 + kPairCols);
         const uint32_t slot_empty0 = map_to_rank(smem_u32(slot_empty), 0);
         const uint32_t tl0 = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(cbeg);
         int slot = 0;
@@ -667,7 +692,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
             const int row0 = ta * kPairRows + static_cast<int>(rank) * 128;
             const bool real_tile = NG == 2 && row0 < args.n_real;  // uniform over the CTA
             __syncwarp();
-            for (int k = lane; k < kBN / 2; k += 32) {
+            for (int k = lane; k < kPairCols; k += 32) {
                 const int c = cbeg + k;
                 const int m = tb * kBN + c;
                 const bool okc = c < nvalid;
@@ -678,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
                 }
             }
             __syncwarp();
-            float acc0[64];
+            float acc0[kPairCols];
 #pragma unroll
             for (int j = 0; j < 64; ++j) acc0[j] = 0.0f;
             // product 0: drain every chunk into acc0 and hand its slot back
@@ -687,7 +712,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pair(const __grid_constant__ Tc
                 const bool got = mbar_wait(&slot_full[slot], sphase, args.err, 4);
                 if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
                 fence_after_sync();
-                drain64(tl0 + static_cast<uint32_t>(slot * kBN), acc0);
+                drain32(tl0 + static_cast<uint32_t>(slot * kBN), acc0);
                 fence_before_sync();
                 __syncwarp();
                 if (lane == 0) mbar_arrive_cluster_relaxed(slot_empty0 + static_cast<uint32_t>(slot * 8));
@@ -1017,7 +1042,7 @@ int pair_clusters(int device) {
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.gridDim = dim3(static_cast<unsigned>(sm & ~1), 1, 1);
-        cfg.blockDim = dim3(kThreads, 1, 1);
+        cfg.blockDim = dim3(kPairThreads, 1, 1);
         cfg.dynamicSmemBytes = PairCfg<NG>::kSmemBytes;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
@@ -1043,7 +1068,7 @@ int launch_pair(const TcMaps& maps, const TcArgs& args, int n_clusters_max, cuda
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(static_cast<unsigned>(2 * n_cl), 1, 1);
-    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.blockDim = dim3(kPairThreads, 1, 1);
     cfg.dynamicSmemBytes = PairCfg<NG>::kSmemBytes;
     cfg.stream = st;
     cfg.attrs = attr;
