@@ -346,23 +346,43 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the driver context each address was looked up in
 
-// Device address of g_fit_scratch on the current device, looked up once per device.  In host code the array's name
-// is only a host-side stand-in, so the address must come from the runtime.  The kept address belongs to the primary
-// context the first call saw: it does not survive cudaDeviceReset (which reloads the module) and is wrong in a
-// non-primary driver context, so the entry point is documented as not usable there.
+// the driver's cuCtxGetCurrent, from the runtime's entry-point table (no link-time dependency on the driver library)
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    return fn;
+}
+
+// Device address of g_fit_scratch in the current context.  In host code the array's name is only a host-side
+// stand-in, so the address comes from the runtime; it is kept per device together with the driver context it was
+// looked up in, and looked up again when the current context differs (after cudaDeviceReset, which reloads the
+// module, or in a non-primary context).  The lookup itself does not allocate once the module is loaded.
 int scratch_address(void** out) {
     int dev = 0;
     FLMM_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(FLMM_ERR_DEVICE, "device index %d out of range", dev);
+    void* ctx = nullptr;
+    if (CtxGetCurrentFn f = ctx_get_current()) {
+        if (f(&ctx) != 0) ctx = nullptr;
+    }
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || ctx == nullptr || ctx != g_scratch_ctx[dev]) {
         void* ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_fit_scratch);
         if (e != cudaSuccess || !ptr)
             return fail(FLMM_ERR_CUDA, "cudaGetSymbolAddress(g_fit_scratch) on device %d: %s", dev,
                         cudaGetErrorString(e));
         g_scratch_addr[dev] = ptr;
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_addr[dev];
     return FLMM_OK;

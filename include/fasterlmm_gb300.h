@@ -247,11 +247,11 @@ int flmm_fit_delta_fast(const double* s, int Neff, const float* UYt, int64_t ldu
  * loop that may not call cudaMalloc (it can synchronise the device).  The scratch is a fixed 4 MiB device array in
  * the library (held by every GPU that loads it until exit).  A call fits when flmm_fit_delta_fast_workspace_bytes
  * (Neff, n_grid) <= 4 MiB, i.e. 4 (n_grid Neff + n_grid + 2 Neff + 4) + 8 n_grid + 512 <= 4,194,304 bytes (n_grid * Neff
- * a little under 1,048,576); larger requests fail with FLMM_ERR_WORKSPACE.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current and keeps it for the process: make that
- * first call before any stream capture, and do not use this entry point after cudaDeviceReset or from a non-primary
- * driver context (the kept address belongs to the primary context the first call saw).  All calls share the array:
- * calls whose kernels overlap on the GPU race and must be serialised by the caller.  Allocates nothing. */
+ * a little under 1,048,576); larger requests fail with FLMM_ERR_WORKSPACE.  The array's device address is looked up
+ * (cudaGetSymbolAddress) on the first call in each driver context and kept with that context, so a call after
+ * cudaDeviceReset or from another context looks it up again: make the first call of a context before any stream
+ * capture.  All calls share the array: calls whose kernels overlap on the GPU race and must be serialised by the
+ * caller.  Allocates nothing. */
 int flmm_fit_delta_fast_noalloc(const double* s, int Neff, const float* UYt, int64_t ldu, int P, int n_grid,
                                 double lo, double hi, int refine, double* log_delta, int32_t* grid_idx, void* stream);
 
