@@ -70,8 +70,8 @@ struct OzCfg {
     static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
 };
 // Configurations used: the refinement's A U as <4, 7, 8, FP64> (U~ in 4 planes, A in 7, levels 0..7, 25 pairs); the
-// corrections u_i . r_j as <4, 4, 3, FP32> (6 pairs: the coefficients E_ij are themselves corrections and need ~1e-3
-// relative accuracy) and T U~ as <4, 4, 5, FP32> (13 pairs: FP32 accuracy against the row's largest rotation, which
+// corrections u_i . r_j as <3, 3, 3, FP32> (6 pairs on planes 0..2 of either side: the coefficients E_ij are
+// themselves corrections and need ~1e-3 relative accuracy) and T U~ as <4, 4, 5, FP32> (13 pairs: FP32 accuracy against the row's largest rotation, which
 // reaches 0.25 for nearly degenerate pairs).
 constexpr int kUPlanes = 4;
 constexpr int kAPlanes = 7;
@@ -513,7 +513,8 @@ int refine_m_tc(const float* R, int N, int batch, float* M, void* work, cudaStre
     __half* rp = w.planes + 4 * w.plane;
     int rc = digits_f32(R, rows, N, rp, w, w.ea, nullptr, st);
     if (rc) return rc;
-    return launch_oz<4, 4, 3, false>(w.up, w.eu, rp, w.ea, N, batch, w, nullptr, M, nullptr, st);
+    // levels 0..2 use planes 0..2 of either side only: the fourth planes are not loaded
+    return launch_oz<3, 3, 3, false>(w.up, w.eu, rp, w.ea, N, batch, w, nullptr, M, nullptr, st);
 }
 
 // U_out = U~ + T U~ (FP32), T (batch, N, N) FP32 at the start of `work` (over planes 0-1), scratch an (batch, N, N)
