@@ -430,7 +430,8 @@ def _eigh_batched_f32(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
 
 
 def _eigh_batched_f32_refined(ctx, Kp: Tensor) -> tuple[Tensor, Tensor]:
-    """FP32 eigendecomposition plus one refinement step: (eigenvector rows FP32, FP64 Rayleigh-quotient evals)."""
+    """FP32 eigendecomposition plus refine_steps(N) refinement steps: (eigenvector rows FP32, ascending FP64 evals,
+    the Rayleigh quotients of the last step's input vectors)."""
     dev = Kp.device
     batch, N, _ = Kp.shape
     U, _ = _eigh_batched_f32(ctx, Kp)

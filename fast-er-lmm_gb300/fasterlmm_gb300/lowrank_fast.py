@@ -60,6 +60,42 @@ class _MarkerPanel:
             padded[offs[c]:offs[c] + n] = self.Grt[a:a + n]
         self.split_T = SplitRows.of(transpose(padded))                            # (N, k_pad) sample-major
         self.N = N
+        self.decomposed = {}  # chromosome -> (ascending evals (k_in,) FP64, eigenvector rows (k_in, k_in))
+
+    def decompose_loco(self, chroms, ctx) -> None:
+        """Eigendecompositions of the LOCO marker Grams of every chromosome in `chroms`, in one batched call of the
+        library's FP32 solver with the refinement steps (FP64-accurate eigenpairs) instead of one FP64 decomposition
+        per chromosome.  The Grams differ in size by the left-out chromosome, so each is padded to the largest with
+        -rho I (rho above every Gram's row sums, so the padding's eigenvalues lie below the Grams' non-negative
+        spectra) and its k_in largest eigenpairs are kept.  Only where the batched solver covers the size (below
+        2,500) and the basis takes the Gram branch (k_in < N)."""
+        todo = [c for c in chroms if c in self.blocks and c not in self.decomposed]
+        sizes = {c: self.k_all - self.blocks[c][1] for c in todo}
+        todo = [c for c in todo if 0 < sizes[c] < self.N]
+        if len(todo) < 2:
+            return
+        k_max = max(sizes.values())
+        if k_max >= 2500:
+            return
+        dev = self.gram.device
+        A = torch.zeros((len(todo), k_max, k_max), dtype=F64, device=dev)
+        rho = 0.0
+        for b, c in enumerate(todo):
+            idx = torch.from_numpy(self.kept(c)).to(dev)
+            Gc = self.gram.index_select(0, idx).index_select(1, idx)
+            A[b, :sizes[c], :sizes[c]] = Gc
+            rho = max(rho, float(Gc.abs().sum(dim=1).max()))
+        rho = 2.0 * rho + 1.0
+        for b, c in enumerate(todo):
+            k_in = sizes[c]
+            if k_in < k_max:
+                d = torch.arange(k_in, k_max, device=dev)
+                A[b, d, d] = -rho
+        U, evals = fast._eigh_batched_f32_refined(ctx, A)
+        for b, c in enumerate(todo):
+            k_in = sizes[c]
+            lo = k_max - k_in  # the padding's eigenpairs come first (ascending order)
+            self.decomposed[c] = (evals[b, lo:].contiguous(), U[b, lo:, :k_in].double().contiguous())
 
     def kept(self, c) -> np.ndarray:
         """Marker positions (in chromosome order) of the kinship without chromosome c (c = None: all)."""
@@ -80,8 +116,11 @@ class _MarkerPanel:
             sel = torch.nonzero(evals.clamp(min=0.0) > (SV_FLOOR * SV_FLOOR) / k_in).flatten()
             Us = U[sel].contiguous()
             return evals[sel].clamp(min=0.0).contiguous(), Us.float(), transpose(Us).float()
-        idx = torch.from_numpy(keep).to(dev)
-        evals, V = _eigh_rows(self.gram.index_select(0, idx).index_select(1, idx).contiguous())
+        if c in self.decomposed:
+            evals, V = self.decomposed.pop(c)
+        else:
+            idx = torch.from_numpy(keep).to(dev)
+            evals, V = _eigh_rows(self.gram.index_select(0, idx).index_select(1, idx).contiguous())
         sv = evals.clamp(min=0.0).sqrt()
         sel = torch.nonzero(sv > SV_FLOOR).flatten()
         sv = sv[sel]
@@ -187,6 +226,8 @@ def loco_scan_blocks_fast(Gk: Tensor, g_chrom: np.ndarray, block_source, M: int,
     Yrt = basis.regress_out(transpose(Yd))                                    # (P, N) FP64
     Yrs = SplitRows.of(Yrt)
     panel = _MarkerPanel(Gk, g_chrom, basis, ctx)
+    if loco:
+        panel.decompose_loco(list(chroms), ctx)
     done(slot)
     out, max_F = _alloc_outputs(M, n_real, P, dev, zero=True)
     ops = WaldOperands(dev)  # the strong-test list
