@@ -587,22 +587,39 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
         Zt[t] = c < ncols ? Zb[static_cast<int64_t>(i) * N + c0 + c] : 0.0f;
     }
     const int a = threadIdx.x / kTile, cc = threadIdx.x % kTile;  // one (reflector, column) pair per thread
+    // V is staged kChunk rows at a time; each thread loads its kPre entries of the next stage into registers while
+    // the current one is used, so the stage's global loads overlap the block's arithmetic instead of preceding it
+    constexpr int kPre = kChunk * kWy / kBtThreads;
+    static_assert(kChunk * kWy % kBtThreads == 0, "stage entries per thread");
+    float pre[kPre];
+    int pk0 = 0;
+    auto load_stage = [&](int i0) {
+#pragma unroll
+        for (int u = 0; u < kPre; ++u) {
+            const int t = threadIdx.x + u * kBtThreads;
+            const int aa = t / kChunk, ii = t % kChunk, i = i0 + ii, k = pk0 + aa;
+            pre[u] = (i < N && k < n_refl && i > k) ? Wb[static_cast<int64_t>(k) * N + i] : 0.0f;
+        }
+    };
+    auto store_stage = [&]() {
+#pragma unroll
+        for (int u = 0; u < kPre; ++u) Vc[threadIdx.x + u * kBtThreads] = pre[u];
+    };
     for (int q = nblocks - 1; q >= 0; --q) {
         const int k0 = q * kWy;
         const int r0 = k0 + 1;  // first row any reflector of the block touches
         if (threadIdx.x < kWy * kWy)
             Tm[threadIdx.x / kWy][threadIdx.x % kWy] = Tq_all[(static_cast<int64_t>(b) * nblocks + q) * kWy * kWy + threadIdx.x];
         float s = 0.0f;
-        // S = V^T Z over the block's rows, V staged kChunk rows at a time (V[i][a] = v_{k0+a}[i])
+        pk0 = k0;
+        // S = V^T Z over the block's rows, V staged kChunk rows at a time (V[i][a] = v_{k0+a}[i]; consecutive
+        // threads read one row of W)
+        load_stage(r0);
         for (int i0 = r0; i0 < N; i0 += kChunk) {
             __syncthreads();
-            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {  // consecutive threads: one row of W
-                const int aa = t / kChunk, ii = t % kChunk, i = i0 + ii, k = k0 + aa;
-                float v = 0.0f;
-                if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
-                Vc[t] = v;
-            }
+            store_stage();
             __syncthreads();
+            if (i0 + kChunk < N) load_stage(i0 + kChunk);
             const int iend = min(kChunk, N - i0);
             for (int ii = 0; ii < iend; ++ii) s = fmaf(Vc[a * kChunk + ii], Zt[(i0 + ii) * kTile + cc], s);
         }
@@ -614,15 +631,12 @@ k_backtransform(const float* __restrict__ W, const float* __restrict__ Tq_all, c
         Sp[a][cc] = sp;
         __syncthreads();
         // Z -= V S'
+        load_stage(r0);
         for (int i0 = r0; i0 < N; i0 += kChunk) {
             __syncthreads();
-            for (int t = threadIdx.x; t < kChunk * kWy; t += kBtThreads) {  // consecutive threads: one row of W
-                const int aa = t / kChunk, ii = t % kChunk, i = i0 + ii, k = k0 + aa;
-                float v = 0.0f;
-                if (i < N && k < n_refl && i > k) v = Wb[static_cast<int64_t>(k) * N + i];
-                Vc[t] = v;
-            }
+            store_stage();
             __syncthreads();
+            if (i0 + kChunk < N) load_stage(i0 + kChunk);
             const int iend = min(kChunk, N - i0);
             for (int t = threadIdx.x; t < iend * kTile; t += kBtThreads) {
                 const int ii = t / kTile, c = t % kTile;
