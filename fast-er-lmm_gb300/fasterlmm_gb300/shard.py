@@ -4,8 +4,12 @@ Phenotype sharding across processes, one GPU each (fasterlmm/cli.py:290-292, 615
 The scan has no exchange step: phenotype columns are independent once a chromosome's spectrum exists, so each rank
 scans a round-robin slice of the phenotypes on its own GPU with no collective on the data path.  Permutations are
 seeded on each phenotype's column in the full table (``seed_idx``), so a sharded run reproduces the unsharded one
-column for column.  ``gather_results`` then collects the shards' results on one rank (a result collection after
-the scan, over any torch.distributed backend: gloo for host tensors, NCCL for device tensors).
+column for column.  Results leave the ranks the way the reference's do (fasterlmm/cli.py:658-686, its shard
+workers write their own phenotypes' files and the parent only merges what is on disk): ``write_shard`` writes a
+rank's phenotypes' output files itself, and ``gather_results_files`` reassembles the tables on one rank through a
+shared directory, so the process group carries only a barrier and the column lists.  ``gather_results`` does the
+same through the process group itself (``gather_object``: every table is pickled through it, which suits small
+runs and tests).
 """
 
 from __future__ import annotations
@@ -74,4 +78,66 @@ def gather_results(mine: list, res: ScanResult, perm_max_F: torch.Tensor, pheno_
     return ScanResult(max_F=max_F, **out), pmf
 
 
-__all__ = ["shard_phenotypes", "display_offset", "perm_threshold_shard", "gather_results"]
+_KEYS = ("f", "beta", "se", "sfve", "nullh2")
+
+
+def gather_results_files(shared_dir, mine: list, res: ScanResult, perm_max_F: torch.Tensor, pheno_idx: list, *,
+                         group=None, dst: int = 0):
+    """
+    ``gather_results`` through the filesystem: every rank writes its shard's tables as .npy files into shared_dir
+    (a directory all ranks see), one barrier, and rank dst reads them memory-mapped into the assembled result.  The
+    process group carries the column lists and the barrier only, never the tables.  Same return values as
+    gather_results; the files are removed once dst has read them.
+    """
+    import numpy as np
+    import torch.distributed as dist
+    from pathlib import Path
+    root = Path(shared_dir)
+    root.mkdir(parents=True, exist_ok=True)
+    rank = dist.get_rank(group)
+    world = dist.get_world_size(group)
+    for k in _KEYS:
+        np.save(root / f"rank{rank}_{k}.npy", getattr(res, k).detach().double().cpu().numpy())
+    np.save(root / f"rank{rank}_perm_max_F.npy", perm_max_F.detach().double().cpu().numpy())
+    cols = [None] * world if rank == dst else None
+    dist.gather_object(list(mine), cols, dst=dst, group=group)  # also orders every rank's files before dst reads
+    if cols is None:
+        dist.barrier(group=group)  # dst is done with the files
+        return None, None
+    pos = {p: i for i, p in enumerate(pheno_idx)}
+    B = len(pheno_idx)
+    first = np.load(root / "rank0_f.npy", mmap_mode="r")
+    M = first.shape[0]
+    out = {k: torch.empty((M, B), dtype=torch.float64) for k in _KEYS}
+    pmf_parts = [np.load(root / f"rank{r}_perm_max_F.npy") for r in range(world)]
+    n_perm = next((pm.shape[1] for pm in pmf_parts if pm.ndim == 2), 0)
+    pmf = torch.empty((B, n_perm), dtype=torch.float64)
+    for r in range(world):
+        if not cols[r]:
+            continue
+        idx = torch.tensor([pos[c] for c in cols[r]], dtype=torch.long)
+        for k in _KEYS:
+            out[k][:, idx] = torch.from_numpy(np.ascontiguousarray(np.load(root / f"rank{r}_{k}.npy", mmap_mode="r")))
+        pmf[idx] = torch.from_numpy(pmf_parts[r]).reshape(len(cols[r]), n_perm)
+    for r in range(world):
+        for k in _KEYS + ("perm_max_F",):
+            (root / f"rank{r}_{k}.npy").unlink(missing_ok=True)
+    dist.barrier(group=group)
+    max_F = torch.empty(B * (1 + n_perm), dtype=torch.float64)
+    max_F[:B] = out["f"].max(dim=0).values if M else torch.full((B,), float("-inf"), dtype=torch.float64)
+    max_F[B:] = pmf.reshape(-1)
+    return ScanResult(max_F=max_F, **out), pmf
+
+
+def write_shard(outdir, mine_names: list, res: ScanResult, perm_max_F: torch.Tensor, df2: int, ctx, p_var, **kw):
+    """
+    This rank's phenotypes' output files (gwas.tsv, perms.tsv, threshold.txt, lambda_gc.txt per phenotype, through
+    output.write_batch) written by the rank itself into outdir, as the reference's shard workers write theirs: the
+    files of all ranks together are the unsharded run's, and no table crosses between processes.
+    """
+    from .output import write_batch
+    write_batch(outdir, list(mine_names), res, perm_max_F, df2, ctx, p_var, **kw)
+
+
+__all__ = ["shard_phenotypes", "display_offset", "perm_threshold_shard", "gather_results", "gather_results_files",
+           "write_shard"]

@@ -82,3 +82,35 @@ def test_write_batch_files(golden, tmp_path):
     assert sorted(r[0] for r in rows) == sorted(names)
     text = write_lambda_table(tmp_path, None, rows, {n: i for i, n in enumerate(names)}).read_text().splitlines()
     assert [t.split("\t")[0] for t in text[1:]] == names
+
+
+def test_sharded_writes_match_the_unsharded_files(golden, tmp_path):
+    """Each rank writing its own round-robin phenotypes' files (shard.write_shard, the reference's shard-worker
+    layout, fasterlmm/cli.py:292) gives the same files, byte for byte, as one unsharded write of the whole batch:
+    a phenotype's files depend on its own columns only."""
+    from fasterlmm_gb300 import shard
+    from fasterlmm_gb300.core import ScanResult
+    from fasterlmm_gb300.output import VariantTable, write_batch
+    g, res, pmf = _scan(golden)
+    M, B = res.f.shape
+    N, D = g["X"].shape
+    df2 = N - D - 1
+    rng = np.random.default_rng(7)
+    ctx = VariantTable.of([f"v{i}" for i in range(M)], g["chrom"].astype(np.float64),
+                          np.arange(M, dtype=np.float64) * 100.0, rng.uniform(0.1, 0.5, M), n_perm=20)
+    p_var = g["Y"].var(axis=0)
+    names = [f"ph{j}" for j in range(B)]
+    whole = tmp_path / "whole"
+    parts = tmp_path / "parts"
+    write_batch(whole, names, res, pmf, df2, ctx, p_var, per_pheno_dirs=True, threads=4)
+    for r in range(2):  # the two ranks of a world of two, one after the other
+        mine = shard.shard_phenotypes(list(range(B)), r, 2)
+        idx = torch.tensor(mine, device=res.f.device)
+        cols = {k: getattr(res, k).index_select(1, idx) for k in ("f", "beta", "se", "sfve", "nullh2")}
+        pmf_r = pmf.index_select(0, idx)
+        res_r = ScanResult(max_F=torch.cat([cols["f"].max(dim=0).values, pmf_r.reshape(-1)]), **cols)
+        shard.write_shard(parts, [names[j] for j in mine], res_r, pmf_r, df2, ctx, p_var[mine], per_pheno_dirs=True,
+                          threads=4)
+    for name in names:
+        for f in ("gwas.tsv", "perms.tsv", "threshold.txt", "lambda_gc.txt"):
+            assert (parts / name / f).read_bytes() == (whole / name / f).read_bytes(), (name, f)
