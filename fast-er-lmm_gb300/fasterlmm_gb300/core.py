@@ -10,7 +10,12 @@ Two numeric forms run the same algorithm:
 
 * ``form="plain"``: FP64 end to end, with the reference's operation order and its 50-step golden-section search.
 * ``form="fast"``: split-precision tensor-core rotation and Wald kernels with FP32 accumulation, an FP32 grid
-  followed by an FP64 Newton refinement of log delta (see fasterlmm_gb300.fast).
+  followed by a safeguarded Newton refinement of log delta whose sums are compensated FP32 (log delta itself is
+  carried in FP64; see fasterlmm_gb300.fast).
+
+Called directly, every driver defaults to ``form="plain"``, the reference's own arithmetic.  The drop-in
+installer (fasterlmm_gb300.shim.install) binds ``form="fast"`` unless told otherwise, since the fast form is
+the one held to the scan's stated tolerances (beta/SE rtol 1e-5, |d(-log10 p)| <= 1e-3) at full speed.
 
 Beyond the reference's keywords, the LOCO / single-K drivers accept the delta-grid options of
 fit_delta_grid_compat (n_grid, log_delta_min, log_delta_max, refine), which the reference's loop leaves at their

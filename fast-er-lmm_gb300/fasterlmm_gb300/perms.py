@@ -70,7 +70,8 @@ def perm_threshold(data, pheno_idx: list[int], *, n_perm: int = 100, seed: int =
     Drop-in for perms.perm_threshold.  ``data`` is the reference's AlignedDataset (or any object with Z, Y, X,
     chrom and optional Z_kin / chrom_kin): raw dosages (N, M) with NaN for missing calls, phenotypes (N, P),
     covariates (N, D).  Returns (ScanResult for the B real columns, perm_max_F (B, n_perm)) on the device of
-    data.Z.  The extra keywords select the delta grid and the numeric form (see fasterlmm_gb300.core); ``out``
+    data.Z.  The extra keywords select the delta grid and the numeric form (see fasterlmm_gb300.core: "plain" is
+    the default here, "fast" the default of the drop-in installer fasterlmm_gb300.shim.install); ``out``
     optionally gives preallocated result tensors (keys f, beta, se, sfve, nullh2 of shape (M, B) and max_F of shape
     (B + B n_perm,), e.g. pinned host memory) that the results are copied into and returned in; ``timers`` is passed
     to the fast engine (CUDA events around its Wald launches).
