@@ -31,8 +31,10 @@ for 50 phenotypes and 10 for the rest, every group on its own strain subset (fas
 kinship factor, 100 phenotypes x (1 + 10 permutations), int8 genotypes streamed from pinned host memory in 8,192-
 variant blocks (200,000 tested variants by default, --M up to 1,000,000).
 
-``--impl reference`` times the CPU restatement of the reference's algorithm (oracle/flmm_oracle.py) on the host's
-cores on a bounded sample of the same workload (one chromosome x one 256-phenotype batch per step).
+``--impl reference`` times the reference's own CPU path on the host's cores on a bounded sample of the same workload
+(one chromosome x one 256-phenotype batch per step): the reference package's functions in FP64 torch where it is
+installed under baseline/_ref, else the CPU restatement of its algorithm (oracle/flmm_oracle.py).  The line's
+``cpu_baseline`` is the same measurement inside the GPU run.
 Under torchrun (N > 1) every rank runs its own replica of the workload (the scan has no cross-GPU exchange) and
 the line reports the total over ranks against the slowest rank's time.
 """
@@ -153,39 +155,121 @@ def make_inputs(B: int | None, M: int | None, name: str = WORKLOAD):
     return d, w
 
 
-# ---- CPU baseline: the oracle on a bounded sample ------------------------------------------------------------------
+# ---- CPU baseline: the reference (or the oracle) on a bounded sample ---------------------------------------------
 
-def cpu_sample_run(d, w, B_sample: int, chrom_id: int = 1) -> tuple[float, int]:
-    """One CLI-sized batch (B_sample phenotypes + their permutations) through one LOCO chromosome, oracle on CPU."""
+REF_DIR = ROOT / "baseline" / "_ref"
+
+
+def _reference_modules():
+    """
+    The reference package itself (pure Python/torch), installed under baseline/_ref by the one offline install
+    ``pip install --no-deps --target baseline/_ref <reference checkout>``; None where it is absent.  Its modules
+    fasterlmm.io and fasterlmm.normalize import pandas at module top although the scan never calls it; where
+    pandas is not installed an empty stand-in module serves the import and is removed again afterwards.
+    """
+    if not (REF_DIR / "fasterlmm" / "core.py").exists():
+        return None
+    stub = None
+    try:
+        import pandas  # noqa: F401
+    except ImportError:
+        import types
+        stub = sys.modules["pandas"] = types.ModuleType("pandas")
+    if str(REF_DIR) not in sys.path:
+        sys.path.insert(0, str(REF_DIR))
+    try:
+        import fasterlmm.core as ref_core
+        import fasterlmm.io as ref_io
+    except Exception:  # an install that does not import here (another Python, a missing dependency)
+        return None
+    finally:
+        if stub is not None and sys.modules.get("pandas") is stub:
+            del sys.modules["pandas"]
+    return ref_core, ref_io
+
+
+def cpu_sample_run(d, w, B_sample: int, chrom_id: int = 1, ref=None) -> tuple[float, int]:
+    """
+    One CLI-sized batch (B_sample phenotypes + their permutations) through one LOCO chromosome on the CPU: the
+    kinship without the chromosome, the compat rotation, the delta fit and the Wald scan of its variants
+    (fasterlmm/core.py:712-716).  ``ref`` = (fasterlmm.core, fasterlmm.io) runs the reference's own functions in
+    FP64 torch on the host threads; None runs the oracle's numpy restatement.  Standardisation and the
+    permutation packing happen before the clock starts.
+    """
     import flmm_oracle as orc
-    Z = orc.standardise_columns(d.Z_float())
+    Zn = orc.standardise_columns(d.Z_float())
     n_perm = w["n_perm"]
-    orders = orc.perm_orders(Z.shape[0], range(B_sample), n_perm)
+    orders = orc.perm_orders(Zn.shape[0], range(B_sample), n_perm)
     Y_all = orc.pack_perms(d.Y[:, :B_sample], orders)
-    t0 = time.perf_counter()
     mask = d.chrom == chrom_id
-    K = orc.grm(Z[:, ~mask])
+    tests = int(mask.sum()) * B_sample * (1 + n_perm)
+    grid_kw = dict(n_grid=w["n_grid"], log_delta_min=w["log_delta_min"], log_delta_max=w["log_delta_max"])
+    if ref is not None:
+        import torch
+        core, fio = ref
+        Z = torch.from_numpy(np.ascontiguousarray(Zn))
+        X = torch.from_numpy(np.ascontiguousarray(d.X))
+        Yt = torch.from_numpy(np.ascontiguousarray(Y_all))
+        Zk = Z[:, torch.from_numpy(~mask)].contiguous()
+        Zc = Z[:, torch.from_numpy(mask)].contiguous()
+        t0 = time.perf_counter()
+        K = fio.grm(Zk)
+        spec = core.fastlmm_compat_rotate(K, X, Yt)
+        ld = core.fit_delta_grid_compat(spec, **grid_kw)
+        core.snp_wald_scan_compat(spec, ld, Zc, n_real=B_sample)
+        return time.perf_counter() - t0, tests
+    t0 = time.perf_counter()
+    K = orc.grm(Zn[:, ~mask])
     spec = orc.compat_rotate(K, d.X, Y_all)
-    ld = orc.fit_delta_grid_compat(spec["s"], spec["UY"], n_grid=w["n_grid"], log_delta_min=w["log_delta_min"],
-                                   log_delta_max=w["log_delta_max"])
-    orc.snp_wald_scan_compat(spec, ld, Z[:, mask], n_real=B_sample)
-    dt = time.perf_counter() - t0
-    return dt, int(mask.sum()) * B_sample * (1 + n_perm)
+    ld = orc.fit_delta_grid_compat(spec["s"], spec["UY"], **grid_kw)
+    orc.snp_wald_scan_compat(spec, ld, Zn[:, mask], n_real=B_sample)
+    return time.perf_counter() - t0, tests
+
+
+def _host_cores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def _cpu_kind():
+    """(kind, ref modules, description) of the CPU path the baseline times."""
+    ref = _reference_modules()
+    if ref is not None:
+        return "reference", ref, "the reference's own fasterlmm.core / fasterlmm.io functions, FP64 torch"
+    return "port", None, "the oracle's numpy FP64 restatement (the reference is not installed here)"
+
+
+class _TorchThreads:
+    """torch's intra-op thread count set to the host's cores for the duration (the reference CLI's --device cpu
+    setting, fasterlmm/cli.py:221), then put back."""
+
+    def __init__(self, n: int):
+        self.n = n
+
+    def __enter__(self):
+        import torch
+        self.prev = torch.get_num_threads()
+        torch.set_num_threads(self.n)
+
+    def __exit__(self, *exc):
+        import torch
+        torch.set_num_threads(self.prev)
 
 
 def cpu_baseline(d, w, target_s: float = 12.0) -> dict:
     B_sample = min(256, w["B"])
     total_t, total_tests, runs = 0.0, 0, 0
     chroms = sorted(np.unique(d.chrom).tolist())
-    while total_t < target_s and runs < len(chroms):
-        dt, n = cpu_sample_run(d, w, B_sample, chroms[runs])
-        total_t += dt
-        total_tests += n
-        runs += 1
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    return {"value": total_tests / total_t, "unit": UNIT, "cores": cores, "kind": "port",
+    cores = _host_cores()
+    kind, ref, what = _cpu_kind()
+    with _TorchThreads(cores):
+        while total_t < target_s and runs < len(chroms):
+            dt, n = cpu_sample_run(d, w, B_sample, chroms[runs], ref)
+            total_t += dt
+            total_tests += n
+            runs += 1
+    return {"value": total_tests / total_t, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{runs} LOCO chromosome(s) x one {B_sample}-phenotype batch with {w['n_perm']} permutations each "
-                      f"(GRM, compat rotation, 64-point grid + golden section, Wald), numpy FP64 on {cores} host "
+                      f"(GRM, compat rotation, 64-point grid + golden section, Wald) through {what} on {cores} host "
                       f"threads; {total_tests} tests in {total_t:.1f} s"}
 
 
@@ -196,22 +280,24 @@ def run_reference(args):
     d, w = make_inputs(args.B, args.M)
     B_sample = min(256, w["B"])
     chroms = sorted(np.unique(d.chrom).tolist())
-    for i in range(args.warmup):
-        cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)])
+    cores = _host_cores()
+    kind, ref, what = _cpu_kind()
     times, tests = [], []
-    for i in range(args.steps):
-        dt, n = cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)])
-        times.append(dt)
-        tests.append(n)
+    with _TorchThreads(cores):
+        for i in range(args.warmup):
+            cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)], ref)
+        for i in range(args.steps):
+            dt, n = cpu_sample_run(d, w, B_sample, chroms[i % len(chroms)], ref)
+            times.append(dt)
+            tests.append(n)
     value = sum(tests) / sum(times)
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "N": w["N"], "M": w["M"], "B": w["B"], "n_perm": w["n_perm"],
                        "step": f"one LOCO chromosome x one {B_sample}-phenotype batch (+{w['n_perm']} perms each)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"one chromosome x {B_sample} phenotypes per step, numpy FP64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"one chromosome x {B_sample} phenotypes per step through {what}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -21,3 +21,25 @@ def test_reference_arm_prints_its_line():
     assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["steps"] == 1 and line["warmup"] == 1
+
+
+def test_cpu_path_is_the_installed_reference_where_present(tmp_path, monkeypatch):
+    """The CPU baseline times the reference's own functions when the package is installed under baseline/_ref,
+    and the oracle port otherwise; both run a tiny sample to the end."""
+    import pytest
+    sys.path.insert(0, str(REPO))
+    import bench
+    d, w = bench.make_inputs(8, 2000)
+    monkeypatch.setattr(bench, "REF_DIR", tmp_path)  # an empty directory: no install
+    kind, ref, _ = bench._cpu_kind()
+    assert kind == "port" and ref is None
+    dt, n = bench.cpu_sample_run(d, w, 4, 1, None)
+    assert dt > 0 and n > 0
+    monkeypatch.setattr(bench, "REF_DIR", REPO / "baseline" / "_ref")
+    if not (REPO / "baseline" / "_ref" / "fasterlmm" / "core.py").exists():
+        pytest.skip("the reference is not installed under baseline/_ref")
+    kind, ref, _ = bench._cpu_kind()
+    assert kind == "reference" and ref[0].__name__ == "fasterlmm.core"
+    dt2, n2 = bench.cpu_sample_run(d, w, 4, 1, ref)
+    assert dt2 > 0 and n2 == n
+    assert "pandas" not in sys.modules or sys.modules["pandas"].__dict__.get("__file__")  # no stand-in left behind
