@@ -86,6 +86,7 @@ SIGNATURES: dict[str, list] = {
     "flmm_chisq1_from_f": [_p, _i64, _i, _p, _p],
     "flmm_perm_threshold_p": [_p, _i, _i, _i, _d, _p, _p],
     "flmm_f_pvalue": [_p, _i64, _i, _p, _p],
+    "flmm_epi_setup_f64": [_p, _i, _p, _i64, _i, _p, _i64, _p, _i, _p, _p, _p, _p, _p, _p],
     "flmm_epi_wald_f32": [_p, _i64, _p, _i64, _p, _i, _i, _i, _i, _i, _i, _d, _d, _p, _p, _p, _i64, _p, _p, _p],
     "flmm_format_f64": [_p, _i64, _p, _i64, _p],
     "flmm_write_gwas_tsv": [_s, _i64, _p, _p, _p, _p, _p, _d, _p, _p, _p, _p, _p, _i64, _p, _i64, _s, _i64],

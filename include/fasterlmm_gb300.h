@@ -526,6 +526,18 @@ int flmm_perm_threshold_p(const double* perm_max_F, int B, int n_perm, int df2, 
  * F <= 0 gives 1, +inf gives 0, NaN stays NaN. */
 int flmm_f_pvalue(const double* F, int64_t n, int df2, double* out, void* stream);
 
+/* Per-phenotype setup of the batched epistasis Wald for one anchor and a chunk of Pc phenotypes
+ * (lux/src/fasterlmm_lux/epi/_kernel.py:21-150, the FP64 block before the test-column loop), all FP64: with
+ * w_p = 1 / (s + exp(log_delta[p])) (N,), A_p = X^T W_p X = L_p L_p^T, beta_x = A_p^-1 X^T W_p y_p and
+ * r_p = y_p - X beta_x, it writes R1 (Pc (C + 1), N; phenotype p's C rows Q_p = L_p^-1 X^T W_p, then w_p o r_p),
+ * W (Pc, N) = w_p, rWr (Pc,) = max(sum w r^2, 1e-300) and L (Pc C (C + 1) / 2 doubles, caller-allocated scratch:
+ * each L_p's packed lower triangle, row by row).  X is (N, C) with row stride ldx, y_p = Y[n * ldy + p].  When a
+ * pivot of some A_p is not positive (A_p not positive definite) *info is set to 1 (it is never cleared) and that
+ * phenotype's outputs are NaN; the reference's batched Cholesky raises for the batch.  1 <= C <= 200. */
+int flmm_epi_setup_f64(const double* s, int N, const double* X, int64_t ldx, int C, const double* Y, int64_t ldy,
+                       const double* log_delta, int Pc, double* R1, double* W, double* rWr, double* L, int* info,
+                       void* stream);
+
 /* Batched epistasis Wald, per anchor and phenotype chunk (lux/src/fasterlmm_lux/epi/_kernel.py:21-150): from
  * G1 (Pc (C + 1), Mc) FP32 = [Q_p; (w_p o r_p)] S (Q_p = L_p^-1 X^T W_p, C rows per phenotype), G2 (Pc, Mc) FP32 =
  * W (S o S) and rWr (Pc,): quad = ||Q_p s_m||^2, denom = max(sWs - quad, 1e-300), beta, SE, F (F = 0 where
