@@ -14,7 +14,8 @@
 //    matrix is read and written once per column; the next pivot row gets its last update in registers in every
 //    CTA, which forms the next reflector from it.  Both products of an update term are rounded before the add, so
 //    W stays exactly symmetric.  One cluster barrier per column.
-// 2. k_tridiag_bisect: each eigenvalue of T by bisection on FP32 Sturm counts (ascending, by index).
+// 2. k_tridiag_bisect: each eigenvalue of T by multisection on FP32 Sturm counts (ascending, by index; three points
+//    per step, so 24 steps narrow the bracket as 48 halvings would).
 // 3. k_tridiag_invit: each eigenvector of T by inverse iteration in FP64 (LDL^T of T - lambda I with a pivot floor,
 //    three solves from a fixed pseudo-random start, the first fused with the factorisation), one thread each.
 // 4. k_cluster_orth: eigenvalues closer than kClusterTol * ||T|| form a cluster; one warp orthonormalises its
@@ -50,7 +51,9 @@ constexpr int kChunk = 128;        // rows of a V block staged at a time in the 
 constexpr int kInvitSolves = 3;
 constexpr int kInvitBlock = 16;     // elements whose loads a recurrence pass issues ahead
 constexpr double kClusterTol = 1e-5;
-constexpr int kBisectSteps = 48;
+constexpr int kSectPts = 3;        // points per multisection step of the eigenvalue brackets (its quarters)
+constexpr int kBisectSteps = 24;   // 4^-24 = 2^-48 of the Gershgorin interval
+constexpr int kBisectThreads = 128;
 
 __device__ __forceinline__ uint32_t cta_rank() {
     uint32_t r;
@@ -298,24 +301,44 @@ k_sytrd_cluster(float* __restrict__ W, int N, float* __restrict__ d_out, float* 
     cluster_barrier();  // no CTA leaves while another may still read its shared memory
 }
 
-// ---- eigenvalues of T: bisection on Sturm counts ---------------------------------------------------------------
+// ---- eigenvalues of T: multisection on Sturm counts ------------------------------------------------------------
 
-// number of eigenvalues of T below x (FP32, pivots floored at pivmin in magnitude)
-__device__ __forceinline__ int sturm_count(const float* d, const float* e2, int N, float x, float pivmin) {
-    int cnt = 0;
-    float q = d[0] - x;
-    if (fabsf(q) < pivmin) q = -pivmin;
-    cnt += q < 0.0f;
-    for (int i = 1; i < N; ++i) {
-        q = (d[i] - x) - e2[i - 1] / q;
-        if (fabsf(q) < pivmin) q = -pivmin;
-        cnt += q < 0.0f;
-    }
-    return cnt;
+// 1 / x by the hardware reciprocal (within 1 ulp; |x| >= pivmin >= 1e-30 is normal here)
+__device__ __forceinline__ float rcp_hw(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-// grid (ceil(N / 256), batch): eigenvalue j of matrix b into evals[b][j], ascending
-__global__ void __launch_bounds__(256)
+// Numbers of eigenvalues of T below each of K points (FP32, pivots floored at pivmin in magnitude).  The quotient
+// e^2 / q takes the hardware reciprocal: the division's full-precision sequence made the search bound by its
+// instruction count, and a count from quotients within 1 ulp is the exact count of a T whose e^2 differ by that
+// much.  The K recurrences are independent, so their latencies overlap.
+template <int K>
+__device__ __forceinline__ void sturm_counts(const float* d, const float* e2, int N, const float (&x)[K], float pivmin,
+                                             int (&cnt)[K]) {
+    float q[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        q[k] = d[0] - x[k];
+        if (fabsf(q[k]) < pivmin) q[k] = -pivmin;
+        cnt[k] = q[k] < 0.0f;
+    }
+    for (int i = 1; i < N; ++i) {
+        const float di = d[i], ei = e2[i - 1];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            q[k] = (di - x[k]) - ei * rcp_hw(q[k]);
+            if (fabsf(q[k]) < pivmin) q[k] = -pivmin;
+            cnt[k] += q[k] < 0.0f;
+        }
+    }
+}
+
+// grid (ceil(N / kBisectThreads), batch): eigenvalue j of matrix b into evals[b][j], ascending.  Each step splits
+// the bracket at kSectPts equispaced points (multisection: kBisectSteps steps narrow it by 2^-48, as 48 halvings
+// would); a thread's recurrences run interleaved, and the small blocks spread the eigenvalues over every SM.
+__global__ void __launch_bounds__(kBisectThreads)
 k_tridiag_bisect(const float* __restrict__ d_all, const float* __restrict__ e_all, int N, float* __restrict__ evals,
                  float* __restrict__ tnorm_out) {
     extern __shared__ float sm[];
@@ -366,9 +389,28 @@ k_tridiag_bisect(const float* __restrict__ d_all, const float* __restrict__ e_al
     float a = gl - 1e-6f * tnorm - 1e-30f, z = gu + 1e-6f * tnorm + 1e-30f;
     // the interval [a, z) holds the (j+1)-th smallest eigenvalue: count(a) <= j < count(z)
     for (int it = 0; it < kBisectSteps; ++it) {
-        const float m = 0.5f * (a + z);
-        if (m <= a || m >= z) break;
-        if (sturm_count(d, e2, N, m, pivmin) > j) z = m; else a = m;
+        const float w = z - a;
+        float m[kSectPts];
+        bool inside = false;
+#pragma unroll
+        for (int k = 0; k < kSectPts; ++k) {
+            m[k] = a + w * (static_cast<float>(k + 1) / static_cast<float>(kSectPts + 1));
+            inside |= m[k] > a && m[k] < z;
+        }
+        if (!inside) break;  // the bracket is down to adjacent floats
+        int cnt[kSectPts];
+        sturm_counts<kSectPts>(d, e2, N, m, pivmin, cnt);
+        // the points rise with k (a + w t is monotone in t), and so do their counts: the lowest point above index j
+        // closes the bracket, the highest one at or below it opens it
+        float na = a, nz = z;
+#pragma unroll
+        for (int k = kSectPts - 1; k >= 0; --k)
+            if (cnt[k] > j) nz = m[k];
+#pragma unroll
+        for (int k = 0; k < kSectPts; ++k)
+            if (cnt[k] <= j) na = m[k];
+        a = na;
+        z = nz;
     }
     evals[static_cast<int64_t>(b) * N + j] = 0.5f * (a + z);
 }
@@ -727,7 +769,8 @@ int eigh_own_f32(float* A, int N, int batch, float* evals, void* work, cudaStrea
     int rc = check_launch("k_sytrd_cluster");
     if (rc) return rc;
     // 2. eigenvalues
-    k_tridiag_bisect<<<dim3(ceil_div(N, 256), batch), 256, sizeof(float) * 2 * static_cast<size_t>(N), st>>>(
+    k_tridiag_bisect<<<dim3(ceil_div(N, kBisectThreads), batch), kBisectThreads,
+                       sizeof(float) * 2 * static_cast<size_t>(N), st>>>(
         d, e, N, evals, tn);
     if ((rc = check_launch("k_tridiag_bisect"))) return rc;
     // 3. eigenvectors of T
