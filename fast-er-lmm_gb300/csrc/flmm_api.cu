@@ -96,7 +96,7 @@ extern "C" int flmm_context_create(int device, flmm_context** out) {
     cudaDeviceProp prop;
     FLMM_CUDA(cudaGetDeviceProperties(&prop, device));
     if (prop.major != 10 || prop.minor != 3)
-        return fail(FLMM_ERR_DEVICE, "device %d is sm_%d%d (%s); this build targets sm_103a", device, prop.major,
+        return fail(FLMM_ERR_DEVICE, "device %d is sm_%d%d (%s); the library is compiled for sm_103a only", device, prop.major,
                     prop.minor, prop.name);
     FLMM_CUDA(cudaSetDevice(device));
     flmm_context* ctx = new (std::nothrow) flmm_context();

@@ -10,7 +10,8 @@ scan never calls), runs ``shim.install()`` on its actual modules and checks
 * ``uninstall()`` puts the reference's own objects back.
 
 It runs in a child interpreter so the imported reference does not leak into the other tests' modules, and is
-skipped where the reference checkout is absent (FASTERLMM_REFERENCE names it).
+skipped where the reference is absent (FASTERLMM_REFERENCE names a checkout; by default it is the offline install
+under baseline/_ref).
 """
 from __future__ import annotations
 
@@ -23,7 +24,8 @@ from pathlib import Path
 import pytest
 
 REPO = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("FASTERLMM_REFERENCE", "/root/reference"))
+# the reference package: FASTERLMM_REFERENCE (a checkout), else its offline install under baseline/_ref
+REF = Path(os.environ.get("FASTERLMM_REFERENCE", str(REPO / "baseline" / "_ref")))
 
 CHILD = r"""
 import inspect, json, sys, tempfile, pathlib, functools
@@ -72,7 +74,7 @@ print(json.dumps(report))
 """
 
 
-@pytest.mark.skipif(not (REF / "fasterlmm" / "core.py").exists(), reason="reference checkout not present")
+@pytest.mark.skipif(not (REF / "fasterlmm" / "core.py").exists(), reason="the reference is neither checked out nor installed")
 def test_install_on_the_real_reference_modules():
     r = subprocess.run([sys.executable, "-c", CHILD, str(REF), str(REPO / "fast-er-lmm_gb300")],
                        capture_output=True, text=True, timeout=600)
