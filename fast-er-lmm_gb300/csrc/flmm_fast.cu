@@ -816,7 +816,12 @@ constexpr int kPrepCache = 32;  // per-lane register cache of k_wald_prep_column
 // rounding to matter are re-evaluated in FP64).
 constexpr int kPrepCols = 8;
 
-__global__ void __launch_bounds__(32 * kPrepCols)
+// 1 / prod_{m != k} (k - m) over m = 0 .. 9, i.e. (-1)^(9-k) / (k! (9-k)!)
+__constant__ double kLagrangeInvDen[kInterpPoints] = {
+    -1.0 / 362880.0, 1.0 / 40320.0, -1.0 / 10080.0, 1.0 / 4320.0, -1.0 / 2880.0,
+    1.0 / 2880.0,    -1.0 / 4320.0, 1.0 / 10080.0,  -1.0 / 40320.0, 1.0 / 362880.0};
+
+__global__ void __launch_bounds__(32 * kPrepCols, 2)
 k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __restrict__ UYt, int64_t ldu,
                     const double* __restrict__ ld, int P, const float* __restrict__ shat_p, double x0, double h,
                     double inv_h, int R, __half* __restrict__ A1h, __half* __restrict__ A1l, int64_t lda,
@@ -824,32 +829,26 @@ k_wald_prep_columns(const float* __restrict__ s32, int Neff, const float* __rest
                     float* __restrict__ sl, float* __restrict__ rWr, float* __restrict__ rWr0) {
     __shared__ float lw[kPrepCols][kInterpPoints];
     __shared__ int lbase[kPrepCols];
-    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * kPrepCols;
-    // Lagrange weights on nodes base .. base + 9 around x: w_k = prod_{m != k} (t - m) / prod_{m != k} (k - m)
-    if (threadIdx.x < kPrepCols * kInterpPoints) {
-        const int j = threadIdx.x / kInterpPoints, k = threadIdx.x % kInterpPoints;
-        const int64_t p = p0 + j;
-        if (p < P) {
-            const double x = ld[p];
-            int base = static_cast<int>(floor((x - x0) * inv_h)) - (kInterpPoints / 2 - 1);
-            base = max(0, min(base, R - kInterpPoints));
-            const double t = (x - (x0 + base * h)) * inv_h;
-            double num = 1.0, den = 1.0;
-#pragma unroll
-            for (int m = 0; m < kInterpPoints; ++m) {
-                if (m == k) continue;
-                num *= t - m;
-                den *= static_cast<double>(k - m);  // integer products up to 9!, exact
-            }
-            lw[j][k] = static_cast<float>(num / den);
-            if (k == 0) lbase[j] = base;
-        }
-    }
-    __syncthreads();
     const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
-    const int64_t p = p0 + j;
+    const int64_t p = static_cast<int64_t>(blockIdx.x) * kPrepCols + j;
     if (p >= P) return;
     const double x = ld[p];
+    // Lagrange weights of the column's warp on nodes base .. base + 9 around x, by its lanes 0..9:
+    // w_k = prod_{m != k} (t - m) / prod_{m != k} (k - m), the denominators' reciprocals being constants (the FP64
+    // pipe is GB300's narrowest, and a division is many of its instructions); only this warp reads them
+    if (lane < kInterpPoints) {
+        const int k = lane;
+        int base = static_cast<int>(floor((x - x0) * inv_h)) - (kInterpPoints / 2 - 1);
+        base = max(0, min(base, R - kInterpPoints));
+        const double t = (x - (x0 + base * h)) * inv_h;
+        double num = 1.0;
+#pragma unroll
+        for (int m = 0; m < kInterpPoints; ++m)
+            if (m != k) num *= t - m;
+        lw[j][k] = static_cast<float>(num * kLagrangeInvDen[k]);
+        if (k == 0) lbase[j] = base;
+    }
+    __syncwarp();
     const float xh = static_cast<float>(x);
     const float xl = static_cast<float>(x - static_cast<double>(xh));
     const float delta = expf(xh) * (1.0f + xl);
