@@ -202,14 +202,16 @@ __global__ void k_refine_coeffs(const float* __restrict__ M, const double* __res
     const int b = blockIdx.y;
     const double* lb = lam + static_cast<int64_t>(b) * N;
     const int j = static_cast<int>(t / N), i = static_cast<int>(t % N);
-    const double tau = 1e-6 * fmax(fabs(lb[0]), fabs(lb[N - 1]));
     float v;
     if (i == j) {
         v = static_cast<float>(0.5 * (1.0 - nrm[static_cast<int64_t>(b) * N + j]));
     } else {
-        const double gap = lb[j] - lb[i];
-        const double m = static_cast<double>(M[b * nn + static_cast<int64_t>(i) * N + j]);
-        v = (fabs(gap) > tau && fabs(m) <= kMaxRotation * fabs(gap)) ? static_cast<float>(m / gap) : 0.0f;
+        // the gap is formed in FP64 (close eigenvalues cancel), the rest in FP32: T is stored in FP32, and FP64 is
+        // GB300's narrowest pipe (a division is many of its instructions)
+        const float tau = 1e-6f * fmaxf(fabsf(static_cast<float>(lb[0])), fabsf(static_cast<float>(lb[N - 1])));
+        const float gap = static_cast<float>(lb[j] - lb[i]);
+        const float m = M[b * nn + static_cast<int64_t>(i) * N + j];
+        v = (fabsf(gap) > tau && fabsf(m) <= static_cast<float>(kMaxRotation) * fabsf(gap)) ? m / gap : 0.0f;
     }
     T[b * nn + t] = v;
 }
