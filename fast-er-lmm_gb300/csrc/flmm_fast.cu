@@ -747,6 +747,8 @@ __global__ void __launch_bounds__(kPairThreads, 1) k_pair(const __grid_constant_
 
 // ---- operand preparation ---------------------------------------------------------------------------------------
 
+constexpr int kSplitCache = 32;  // per-lane register cache of k_split_rows: rows up to 1,024 entries
+
 // One warp per row, eight rows per 256-thread block: the row's largest |x|, then the split.  FP64 inputs are rounded
 // to FP32 first (2^-24 relative, below the split's 2^-22), which keeps the per-element work off the FP64 pipe (a
 // small fraction of the FP32 rate on this GPU).
@@ -758,15 +760,36 @@ k_split_rows(const T* __restrict__ X, int64_t ldx, int rows, int K, __half* __re
     const int64_t r = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     if (r >= rows) return;
     const T* x = X + r * ldx;
+    // rows of up to 32 * kSplitCache entries are read and rounded once, into registers, for both passes
+    float xv[kSplitCache];
+    const bool cached = K <= 32 * kSplitCache;
     float amax = 0.0f;
+    if (cached) {
+#pragma unroll
+        for (int i = 0; i < kSplitCache; ++i) {
+            const int k = lane + 32 * i;
+            xv[i] = k < K ? static_cast<float>(x[k]) : 0.0f;
+        }
+#pragma unroll
+        for (int i = 0; i < kSplitCache; ++i) amax = fmaxf(amax, fabsf(xv[i]));
+    } else {
 #pragma unroll 4
-    for (int k = lane; k < K; k += 32) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
+        for (int k = lane; k < K; k += 32) amax = fmaxf(amax, fabsf(static_cast<float>(x[k])));
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     int e;
     const float mul = row_scale_exp(amax, &e);
+    if (cached) {
+#pragma unroll
+        for (int i = 0; i < kSplitCache; ++i) {
+            const int k = lane + 32 * i;
+            if (k < K) split_store(xv[i], mul, hi, lo, r * ldo + k);
+        }
+    } else {
 #pragma unroll 4
-    for (int k = lane; k < K; k += 32) split_store(static_cast<float>(x[k]), mul, hi, lo, r * ldo + k);
+        for (int k = lane; k < K; k += 32) split_store(static_cast<float>(x[k]), mul, hi, lo, r * ldo + k);
+    }
     if (lane == 0) scale[r] = ldexpf(1.0f, -e);
 }
 
